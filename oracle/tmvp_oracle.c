@@ -1,0 +1,604 @@
+/*
+ * tmvp_oracle.c — CPU oracle for the batched Saber/Sable KEM path.
+ *
+ * TEST INFRASTRUCTURE ONLY: a plain-C restatement of the reference's serial
+ * algorithms, used by the tests, the smoke check and the CPU-baseline leg of
+ * the benchmark as the checker.  Nothing in the product links it.
+ *
+ * Each function cites the reference code it restates (paths relative to the
+ * reference repository).  Parameter sets:
+ *   Saber family  TMVP-Saber/SABER-GPU/include/params.h:1-50
+ *   Sable family  TMVP_SABLE/include/SABLE_params.h:1-73 (Saber_type 1/2/3)
+ */
+#include "tmvp_oracle.h"
+
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------------ */
+/* Parameters                                                                */
+/* ------------------------------------------------------------------------ */
+
+int orc_get_params(int set, orc_params *p) {
+  /* l, eq, ep, et, mu, sable */
+  static const int tab[ORC_NSETS][6] = {
+      {2, 13, 10, 3, 10, 0}, /* LightSaber  params.h:9-11, :21-24        */
+      {3, 13, 10, 4, 8, 0},  /* Saber       params.h:12-14               */
+      {4, 13, 10, 6, 6, 0},  /* FireSaber   params.h:15-17               */
+      {2, 11, 9, 3, 2, 1},   /* Sable l=2   SABLE_params.h:8-12, :26-30  */
+      {3, 11, 9, 5, 2, 1},   /* Sable l=3   SABLE_params.h:14-18         */
+      {4, 11, 10, 3, 2, 1},  /* Sable l=4   SABLE_params.h:20-24         */
+  };
+  if (set < 0 || set >= ORC_NSETS || !p) return -1;
+  memset(p, 0, sizeof *p);
+  p->l = tab[set][0];
+  p->eq = tab[set][1];
+  p->ep = tab[set][2];
+  p->et = tab[set][3];
+  p->mu = tab[set][4];
+  p->sable = tab[set][5];
+  p->polybytes = p->eq * 32;
+  p->polyvecbytes = p->l * p->polybytes;
+  p->polycompbytes = p->ep * 32;
+  p->scalebytes = p->et * 32;
+  p->coinbytes = p->mu * 32;
+  p->pk_bytes = p->l * p->polycompbytes + 32;
+  /* Saber: 13-bit secret (params.h:41); Sable: 2-bit secret (SABLE_params.h:61) */
+  p->indcpa_sk_bytes = p->sable ? p->l * 64 : p->l * p->polybytes;
+  p->sk_bytes = p->indcpa_sk_bytes + p->pk_bytes + 32 + 32;
+  p->ct_bytes = p->l * p->polycompbytes + p->scalebytes;
+  /* h1, h2: TMVP-Saber/SABER-GPU/src/poly.cu:15-16, TMVP_SABLE/src/pack.cu:15-16 */
+  p->h1 = 1 << (p->eq - p->ep - 1);
+  p->h2 = (1 << (p->ep - 2)) - (1 << (p->ep - p->et - 1)) + (1 << (p->eq - p->ep - 1));
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Keccak-f[1600] and the FIPS 202 sponge                                    */
+/* Restates TMVP_SABLE/src/fips202.cu:15-405 and :535-578 (identical to      */
+/* TMVP-Saber/SABER-GPU/src/poly.cu:405-797, :1076-1114).  The round         */
+/* constants and rotation offsets are derived from the FIPS 202 definitions  */
+/* (rc LFSR, rho walk) at first use instead of being tabulated.              */
+/* ------------------------------------------------------------------------ */
+
+static uint64_t g_rc[24];
+static int g_rho[25];
+static pthread_once_t g_keccak_once = PTHREAD_ONCE_INIT;
+
+static int rc_bit(int t) {
+  /* FIPS 202 Algorithm 5: LFSR x^8 + x^6 + x^5 + x^4 + 1 */
+  unsigned r = 1;
+  if (t % 255 == 0) return 1;
+  for (int i = 1; i <= t % 255; i++) {
+    r <<= 1;
+    if (r & 0x100) r ^= 0x171;
+  }
+  return r & 1;
+}
+
+static void keccak_init_tables(void) {
+  for (int ir = 0; ir < 24; ir++) {
+    uint64_t rc = 0;
+    for (int j = 0; j <= 6; j++)
+      if (rc_bit(j + 7 * ir)) rc |= (uint64_t)1 << ((1 << j) - 1);
+    g_rc[ir] = rc;
+  }
+  /* FIPS 202 Algorithm 2 (rho offsets) */
+  g_rho[0] = 0;
+  int x = 1, y = 0;
+  for (int t = 0; t < 24; t++) {
+    g_rho[x + 5 * y] = ((t + 1) * (t + 2) / 2) % 64;
+    int nx = y, ny = (2 * x + 3 * y) % 5;
+    x = nx;
+    y = ny;
+  }
+}
+
+static inline uint64_t rol64(uint64_t v, int n) {
+  return n ? (v << n) | (v >> (64 - n)) : v;
+}
+
+void orc_keccakf1600(uint64_t A[25]) {
+  pthread_once(&g_keccak_once, keccak_init_tables);
+  for (int ir = 0; ir < 24; ir++) {
+    uint64_t C[5], D[5], B[25];
+    for (int x = 0; x < 5; x++)
+      C[x] = A[x] ^ A[x + 5] ^ A[x + 10] ^ A[x + 15] ^ A[x + 20];
+    for (int x = 0; x < 5; x++) D[x] = C[(x + 4) % 5] ^ rol64(C[(x + 1) % 5], 1);
+    for (int i = 0; i < 25; i++) A[i] ^= D[i % 5];
+    /* rho + pi: B[y, 2x+3y] = rot(A[x,y], r[x,y]) */
+    for (int x = 0; x < 5; x++)
+      for (int y = 0; y < 5; y++)
+        B[y + 5 * ((2 * x + 3 * y) % 5)] = rol64(A[x + 5 * y], g_rho[x + 5 * y]);
+    /* chi */
+    for (int y = 0; y < 5; y++)
+      for (int x = 0; x < 5; x++)
+        A[x + 5 * y] = B[x + 5 * y] ^ (~B[(x + 1) % 5 + 5 * y] & B[(x + 2) % 5 + 5 * y]);
+    /* iota */
+    A[0] ^= g_rc[ir];
+  }
+}
+
+static uint64_t load64le(const uint8_t *x) {
+  uint64_t r = 0;
+  for (int i = 0; i < 8; i++) r |= (uint64_t)x[i] << (8 * i);
+  return r;
+}
+
+static void store64le(uint8_t *x, uint64_t v) {
+  for (int i = 0; i < 8; i++) x[i] = (uint8_t)(v >> (8 * i));
+}
+
+/* keccak_absorb: fips202.cu:338-362 */
+static void sponge_absorb(uint64_t s[25], int rate, const uint8_t *m, size_t mlen,
+                          uint8_t pad) {
+  memset(s, 0, 25 * sizeof(uint64_t));
+  while (mlen >= (size_t)rate) {
+    for (int i = 0; i < rate / 8; i++) s[i] ^= load64le(m + 8 * i);
+    orc_keccakf1600(s);
+    m += rate;
+    mlen -= rate;
+  }
+  uint8_t t[200];
+  memset(t, 0, sizeof t);
+  memcpy(t, m, mlen);
+  t[mlen] = pad;
+  t[rate - 1] |= 0x80;
+  for (int i = 0; i < rate / 8; i++) s[i] ^= load64le(t + 8 * i);
+}
+
+/* keccak_squeezeblocks + tail: fips202.cu:364-405 */
+static void sponge_squeeze(uint8_t *out, size_t outlen, uint64_t s[25], int rate) {
+  uint8_t t[200];
+  while (outlen > 0) {
+    orc_keccakf1600(s);
+    for (int i = 0; i < rate / 8; i++) store64le(t + 8 * i, s[i]);
+    size_t k = outlen < (size_t)rate ? outlen : (size_t)rate;
+    memcpy(out, t, k);
+    out += k;
+    outlen -= k;
+  }
+}
+
+void orc_sha3_256(uint8_t out[32], const uint8_t *in, size_t inlen) {
+  uint64_t s[25];
+  sponge_absorb(s, 136, in, inlen, 0x06);
+  sponge_squeeze(out, 32, s, 136);
+}
+
+void orc_sha3_512(uint8_t out[64], const uint8_t *in, size_t inlen) {
+  uint64_t s[25];
+  sponge_absorb(s, 72, in, inlen, 0x06);
+  sponge_squeeze(out, 64, s, 72);
+}
+
+void orc_shake128(uint8_t *out, size_t outlen, const uint8_t *in, size_t inlen) {
+  uint64_t s[25];
+  sponge_absorb(s, 168, in, inlen, 0x1F);
+  sponge_squeeze(out, outlen, s, 168);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Bit packing.  Every packer of the reference is a little-endian bit       */
+/* stream of w-bit fields: 13-bit BS2POLq (SABER poly.cu:799-816), 11-bit   */
+/* BS2POLq_gpu2 (SABLE pack.cu:22-37), 10-bit BS2POLp/POLp2BS (SABER        */
+/* pack.cu:7-32), 9-bit (SABLE pack.cu:182-246), 4-bit POLT2BS/BS2POLT      */
+/* (SABER pack.cu:101-197, incl. the ET=3/6 variants), 5-bit (SABLE         */
+/* pack.cu:339-421), 2-bit secret (SABLE pack.cu:366-377) and 1-bit message */
+/* (SABER pack.cu:86-97, :201-212).                                          */
+/* ------------------------------------------------------------------------ */
+
+void orc_pack_bits(uint8_t *out, const uint16_t *in, int n, int w) {
+  memset(out, 0, (size_t)(n * w + 7) / 8);
+  for (int i = 0; i < n; i++) {
+    uint32_t v = in[i] & ((1u << w) - 1);
+    for (int b = 0; b < w; b++) {
+      int bit = i * w + b;
+      if ((v >> b) & 1) out[bit >> 3] |= (uint8_t)(1u << (bit & 7));
+    }
+  }
+}
+
+void orc_unpack_bits(uint16_t *out, const uint8_t *in, int n, int w) {
+  for (int i = 0; i < n; i++) {
+    uint32_t v = 0;
+    for (int b = 0; b < w; b++) {
+      int bit = i * w + b;
+      v |= (uint32_t)((in[bit >> 3] >> (bit & 7)) & 1) << b;
+    }
+    out[i] = (uint16_t)v;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* CBD: coefficient i takes bits [mu*i, mu*i+mu) of the LE stream; the      */
+/* result is popcount(first mu/2 bits) - popcount(next mu/2 bits).          */
+/* This is the common rule behind SABER poly.cu:836-916 (mu = 6, 8, 10) and */
+/* SABLE fips202.cu:625-651 (mu = 2).                                       */
+/* ------------------------------------------------------------------------ */
+
+void orc_cbd(int mu, uint16_t s[256], const uint8_t *buf) {
+  int h = mu / 2;
+  for (int i = 0; i < 256; i++) {
+    int a = 0, b = 0;
+    for (int k = 0; k < h; k++) {
+      int bit = mu * i + k;
+      a += (buf[bit >> 3] >> (bit & 7)) & 1;
+      bit = mu * i + h + k;
+      b += (buf[bit >> 3] >> (bit & 7)) & 1;
+    }
+    s[i] = (uint16_t)(a - b);
+  }
+}
+
+/* GenMatrix: SABER poly.cu:1047-1059 (GenMatrix_gpu2) / SABLE
+ * SABLE_indcpa.cu:149-150 (shake128_gpu + BS2POLVECq_gpu2):
+ * A[i][j] = unpack_eq(SHAKE128(seed)[(i*l+j)*polybytes ...]). */
+void orc_gen_matrix(int set, uint16_t *A, const uint8_t seed[32]) {
+  orc_params P;
+  orc_get_params(set, &P);
+  size_t len = (size_t)P.l * P.l * P.polybytes;
+  uint8_t *buf = (uint8_t *)malloc(len);
+  orc_shake128(buf, len, seed, 32);
+  for (int ij = 0; ij < P.l * P.l; ij++)
+    orc_unpack_bits(A + 256 * ij, buf + (size_t)ij * P.polybytes, 256, P.eq);
+  free(buf);
+}
+
+/* GenSecret: SABER poly.cu:1062-1073, SABLE fips202.cu:655-668.
+ * Sable masks each coefficient mod q (fips202.cu:645-648). */
+void orc_gen_secret(int set, uint16_t *s, const uint8_t seed[32]) {
+  orc_params P;
+  orc_get_params(set, &P);
+  size_t len = (size_t)P.l * P.coinbytes;
+  uint8_t *buf = (uint8_t *)malloc(len);
+  orc_shake128(buf, len, seed, 32);
+  for (int j = 0; j < P.l; j++) {
+    orc_cbd(P.mu, s + 256 * j, buf + (size_t)j * P.coinbytes);
+    if (P.sable)
+      for (int k = 0; k < 256; k++) s[256 * j + k] &= (uint16_t)((1u << P.eq) - 1);
+  }
+  free(buf);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Negacyclic multiplication in Z_{2^16}[x]/(x^256+1)                       */
+/* ------------------------------------------------------------------------ */
+
+/* Schoolbook: SABER poly.cu:227-248 (VecVecMul_gpu_shared inner loops). */
+void orc_polmul_schoolbook(uint16_t r[256], const uint16_t a[256], const uint16_t b[256]) {
+  for (int t = 0; t < 256; t++) {
+    uint16_t sum = 0;
+    for (int k = 0; k <= t; k++) sum += (uint16_t)(b[t - k] * a[k]);
+    for (int k = 1; k < 256 - t; k++) sum -= (uint16_t)(b[t + k] * a[256 - k]);
+    r[t] = sum;
+  }
+}
+
+/* One-level 2-way TMVP: SABER poly.cu:1116-1129 (Toeplitz of b),
+ * :1131-1151 / :1295-1311 (operands), :1315-1392 (three 128x128 products and
+ * the recombination r_lo = P1 + P2, r_hi = P1 - P3). */
+void orc_polmul_tmvp2(uint16_t r[256], const uint16_t a[256], const uint16_t b[256]) {
+  /* T[row][col] = b[row-col] (row >= col) else -b[row-col+256] */
+#define TOEP(row, col) ((row) >= (col) ? b[(row) - (col)] : (uint16_t)(-b[(row) - (col) + 256]))
+  uint16_t v01[128];
+  for (int k = 0; k < 128; k++) v01[k] = (uint16_t)(a[k] + a[128 + k]);
+  for (int row = 0; row < 128; row++) {
+    uint16_t p1 = 0, p2 = 0, p3 = 0;
+    for (int col = 0; col < 128; col++) {
+      uint16_t t00 = TOEP(row, col);
+      uint16_t t01 = TOEP(row, col + 128);
+      uint16_t t10 = TOEP(row + 128, col);
+      p1 += (uint16_t)(t00 * v01[col]);
+      p2 += (uint16_t)((uint16_t)(t01 - t00) * a[128 + col]);
+      p3 += (uint16_t)((uint16_t)(t00 - t10) * a[col]);
+    }
+    r[row] = (uint16_t)(p1 + p2);
+    r[128 + row] = (uint16_t)(p1 - p3);
+  }
+#undef TOEP
+}
+
+/* ------------------------------------------------------------------------ */
+/* Raw matrix-vector product (the TMVP benchmark shape).                     */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+  size_t lo, hi;
+  int l, eq, transpose;
+  uint16_t *out;
+  const uint16_t *A;
+  const int8_t *s;
+} mv_job;
+
+static void *mv_worker(void *arg) {
+  mv_job *J = (mv_job *)arg;
+  int l = J->l;
+  uint16_t mask = (uint16_t)((1u << J->eq) - 1);
+  uint16_t sv[256], prod[256];
+  for (size_t n = J->lo; n < J->hi; n++) {
+    const uint16_t *A = J->A + n * (size_t)l * l * 256;
+    const int8_t *s = J->s + n * (size_t)l * 256;
+    uint16_t *o = J->out + n * (size_t)l * 256;
+    for (int i = 0; i < l; i++) {
+      uint16_t acc[256];
+      memset(acc, 0, sizeof acc);
+      for (int j = 0; j < l; j++) {
+        const uint16_t *a = J->transpose ? A + 256 * (j * l + i) : A + 256 * (i * l + j);
+        for (int k = 0; k < 256; k++) sv[k] = (uint16_t)(int16_t)s[256 * j + k];
+        orc_polmul_schoolbook(prod, a, sv);
+        for (int k = 0; k < 256; k++) acc[k] += prod[k];
+      }
+      for (int k = 0; k < 256; k++) o[256 * i + k] = acc[k] & mask;
+    }
+  }
+  return NULL;
+}
+
+static void run_parallel(void *(*fn)(void *), void *jobs, size_t jobsz, int nthreads) {
+  if (nthreads <= 1) {
+    fn(jobs);
+    return;
+  }
+  pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+  for (int t = 0; t < nthreads; t++) pthread_create(&th[t], NULL, fn, (char *)jobs + t * jobsz);
+  for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+  free(th);
+}
+
+void orc_matvec_batch(size_t n, int l, int eq, int transpose, uint16_t *out,
+                      const uint16_t *A, const int8_t *s, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  mv_job *jobs = (mv_job *)calloc(nthreads, sizeof(mv_job));
+  for (int t = 0; t < nthreads; t++) {
+    jobs[t].lo = n * t / nthreads;
+    jobs[t].hi = n * (t + 1) / nthreads;
+    jobs[t].l = l;
+    jobs[t].eq = eq;
+    jobs[t].transpose = transpose;
+    jobs[t].out = out;
+    jobs[t].A = A;
+    jobs[t].s = s;
+  }
+  run_parallel(mv_worker, jobs, sizeof(mv_job), nthreads);
+  free(jobs);
+}
+
+/* ------------------------------------------------------------------------ */
+/* IND-CPA                                                                   */
+/* ------------------------------------------------------------------------ */
+
+/* Secret-key packing: Saber 13-bit (SABER pack.cu:34-46 is the unpacker),
+ * Sable 2-bit two's complement (SABLE pack.cu:366-377 is the unpacker). */
+static void pack_secret(const orc_params *P, uint8_t *out, const uint16_t *s) {
+  for (int j = 0; j < P->l; j++) {
+    if (P->sable)
+      orc_pack_bits(out + 64 * j, s + 256 * j, 256, 2);
+    else
+      orc_pack_bits(out + P->polybytes * j, s + 256 * j, 256, P->eq);
+  }
+}
+
+static void unpack_secret(const orc_params *P, uint16_t *s, const uint8_t *in) {
+  for (int j = 0; j < P->l; j++) {
+    if (P->sable) {
+      orc_unpack_bits(s + 256 * j, in + 64 * j, 256, 2);
+      /* ((b & 3) ^ 2) - 2: SABLE pack.cu:371-376 */
+      for (int k = 0; k < 256; k++) s[256 * j + k] = (uint16_t)((s[256 * j + k] ^ 2) - 2);
+    } else {
+      orc_unpack_bits(s + 256 * j, in + P->polybytes * j, 256, P->eq);
+    }
+  }
+}
+
+/* acc[i] = sum_j M[i][j] * v[j] over Z_{2^16} (transpose: M[j][i]). */
+static void matvec_u16(const orc_params *P, uint16_t *acc, const uint16_t *M,
+                       const uint16_t *v, int transpose) {
+  uint16_t prod[256];
+  int l = P->l;
+  memset(acc, 0, sizeof(uint16_t) * 256 * l);
+  for (int i = 0; i < l; i++)
+    for (int j = 0; j < l; j++) {
+      const uint16_t *a = transpose ? M + 256 * (j * l + i) : M + 256 * (i * l + j);
+      orc_polmul_schoolbook(prod, a, v + 256 * j);
+      for (int k = 0; k < 256; k++) acc[256 * i + k] += prod[k];
+    }
+}
+
+static void innerprod_u16(const orc_params *P, uint16_t acc[256], const uint16_t *b,
+                          const uint16_t *s) {
+  uint16_t prod[256];
+  memset(acc, 0, sizeof(uint16_t) * 256);
+  for (int j = 0; j < P->l; j++) {
+    orc_polmul_schoolbook(prod, b + 256 * j, s + 256 * j);
+    for (int k = 0; k < 256; k++) acc[k] += prod[k];
+  }
+}
+
+/* Key generation is not in the reference (it has no keypair); this follows
+ * the Saber round-3 specification: seed_A is hashed with SHAKE-128 before use,
+ * b = round(A^T s).  The published test keys (SABER tv.h:8,10; SABLE
+ * tv.h:15,19) satisfy pk = pack_p(round(A^T s)) with s unpacked from sk. */
+void orc_indcpa_keypair(int set, uint8_t *pk, uint8_t *sk_indcpa,
+                        const uint8_t seed_a_in[32], const uint8_t seed_s[32]) {
+  orc_params P;
+  orc_get_params(set, &P);
+  int l = P.l;
+  uint8_t seed_a[32];
+  orc_shake128(seed_a, 32, seed_a_in, 32);
+  uint16_t *A = (uint16_t *)malloc(sizeof(uint16_t) * 256 * l * l);
+  uint16_t s[4 * 256], b[4 * 256];
+  orc_gen_matrix(set, A, seed_a);
+  orc_gen_secret(set, s, seed_s);
+  matvec_u16(&P, b, A, s, 1);
+  uint16_t qmask = (uint16_t)((1u << P.eq) - 1);
+  for (int k = 0; k < 256 * l; k++)
+    b[k] = (uint16_t)(((b[k] + P.h1) & qmask) >> (P.eq - P.ep));
+  for (int i = 0; i < l; i++)
+    orc_pack_bits(pk + P.polycompbytes * i, b + 256 * i, 256, P.ep);
+  memcpy(pk + (size_t)l * P.polycompbytes, seed_a, 32);
+  pack_secret(&P, sk_indcpa, s);
+  free(A);
+}
+
+/* indcpa_kem_enc as launched by saber_enc (SABER cuda_kernel.cu:124-178) and
+ * SABLE_enc (SABLE_indcpa.cu:149-224):
+ *   b' = round(A s'), c_m = ((v' + h1 - (m << (ep-1))) mod p) >> (ep - et)
+ *   with v' = sum_j b_j s'_j mod p. */
+void orc_indcpa_enc(int set, uint8_t *ct, const uint8_t m[32], const uint8_t noiseseed[32],
+                    const uint8_t *pk) {
+  orc_params P;
+  orc_get_params(set, &P);
+  int l = P.l;
+  uint16_t *A = (uint16_t *)malloc(sizeof(uint16_t) * 256 * l * l);
+  uint16_t sp[4 * 256], bp[4 * 256], b[4 * 256], vp[256], cm[256];
+  orc_gen_matrix(set, A, pk + (size_t)l * P.polycompbytes);
+  orc_gen_secret(set, sp, noiseseed);
+  matvec_u16(&P, bp, A, sp, 0);
+  uint16_t qmask = (uint16_t)((1u << P.eq) - 1), pmask = (uint16_t)((1u << P.ep) - 1);
+  /* post_process: SABER poly.cu:381-389, SABLE pack.cu:167-178 */
+  for (int k = 0; k < 256 * l; k++)
+    bp[k] = (uint16_t)(((bp[k] + P.h1) & qmask) >> (P.eq - P.ep));
+  for (int i = 0; i < l; i++) {
+    orc_pack_bits(ct + P.polycompbytes * i, bp + 256 * i, 256, P.ep);
+    orc_unpack_bits(b + 256 * i, pk + P.polycompbytes * i, 256, P.ep);
+  }
+  innerprod_u16(&P, vp, b, sp);
+  /* post_process2 (SABER poly.cu:391-395) / post_process3+4 (SABLE
+   * pack.cu:290-335): encode the message bit at position ep-1. */
+  for (int k = 0; k < 256; k++) {
+    uint16_t mb = (m[k >> 3] >> (k & 7)) & 1;
+    cm[k] = (uint16_t)((((uint16_t)(vp[k] + P.h1 - (mb << (P.ep - 1)))) & pmask) >> (P.ep - P.et));
+  }
+  orc_pack_bits(ct + (size_t)l * P.polycompbytes, cm, 256, P.et);
+  free(A);
+}
+
+/* indcpa_kem_dec as launched by saber_dec (SABER cuda_kernel.cu:341-370) and
+ * SABLE_dec (SABLE_indcpa.cu:428-461):
+ *   v = sum_j b'_j s_j mod p, m'_k = ((v + h2 - (c_m << (ep-et))) mod p) >> (ep-1). */
+void orc_indcpa_dec(int set, uint8_t m[32], const uint8_t *sk_indcpa, const uint8_t *ct) {
+  orc_params P;
+  orc_get_params(set, &P);
+  int l = P.l;
+  uint16_t s[4 * 256], bp[4 * 256], v[256], cm[256];
+  unpack_secret(&P, s, sk_indcpa);
+  for (int i = 0; i < l; i++) orc_unpack_bits(bp + 256 * i, ct + P.polycompbytes * i, 256, P.ep);
+  orc_unpack_bits(cm, ct + (size_t)l * P.polycompbytes, 256, P.et);
+  innerprod_u16(&P, v, bp, s);
+  uint16_t pmask = (uint16_t)((1u << P.ep) - 1);
+  memset(m, 0, 32);
+  for (int k = 0; k < 256; k++) {
+    uint16_t t = (uint16_t)(((uint16_t)(v[k] + P.h2 - (cm[k] << (P.ep - P.et)))) & pmask);
+    m[k >> 3] |= (uint8_t)(((t >> (P.ep - 1)) & 1) << (k & 7));
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* FO KEM                                                                    */
+/* ------------------------------------------------------------------------ */
+
+void orc_kem_keypair(int set, uint8_t *pk, uint8_t *sk, const uint8_t coins[96]) {
+  orc_params P;
+  orc_get_params(set, &P);
+  orc_indcpa_keypair(set, pk, sk, coins, coins + 32);
+  memcpy(sk + P.indcpa_sk_bytes, pk, P.pk_bytes);
+  orc_sha3_256(sk + P.sk_bytes - 64, pk, P.pk_bytes);
+  memcpy(sk + P.sk_bytes - 32, coins + 64, 32);
+}
+
+/* saber_enc: SABER cuda_kernel.cu:116-186; SABLE_enc: SABLE_indcpa.cu:139-232. */
+void orc_kem_enc(int set, uint8_t *ct, uint8_t ss[32], const uint8_t *pk,
+                 const uint8_t coins[32]) {
+  orc_params P;
+  orc_get_params(set, &P);
+  uint8_t buf[64], kr[64];
+  orc_sha3_256(buf, coins, 32);
+  orc_sha3_256(buf + 32, pk, P.pk_bytes);
+  orc_sha3_512(kr, buf, 64);
+  orc_indcpa_enc(set, ct, buf, kr + 32, pk);
+  orc_sha3_256(kr + 32, ct, P.ct_bytes);
+  orc_sha3_256(ss, kr, 64);
+}
+
+/* saber_dec: SABER cuda_kernel.cu:341-450; SABLE_dec: SABLE_indcpa.cu:428-557.
+ * The reference runs its compare and conditional move after hashing and with
+ * a zero-trip loop (pack.cu:225-255); this follows the specification instead:
+ * the re-encryption is compared in full and z replaces kr[0:32] before the
+ * final hash when it differs.  For valid ciphertexts both give the same key. */
+int orc_kem_dec(int set, uint8_t ss[32], const uint8_t *ct, const uint8_t *sk) {
+  orc_params P;
+  orc_get_params(set, &P);
+  uint8_t buf[64], kr[64];
+  uint8_t *cmp = (uint8_t *)malloc(P.ct_bytes);
+  const uint8_t *pk = sk + P.indcpa_sk_bytes;
+  orc_indcpa_dec(set, buf, sk, ct);
+  memcpy(buf + 32, sk + P.sk_bytes - 64, 32);
+  orc_sha3_512(kr, buf, 64);
+  orc_indcpa_enc(set, cmp, buf, kr + 32, pk);
+  uint8_t diff = 0;
+  for (int i = 0; i < P.ct_bytes; i++) diff |= (uint8_t)(ct[i] ^ cmp[i]);
+  int fail = diff != 0;
+  orc_sha3_256(kr + 32, ct, P.ct_bytes);
+  if (fail) memcpy(kr, sk + P.sk_bytes - 32, 32);
+  orc_sha3_256(ss, kr, 64);
+  free(cmp);
+  return fail;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Batched drivers (CPU baseline)                                            */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+  int op, set;
+  size_t lo, hi;
+  uint8_t *o1, *o2, *o3;
+  const uint8_t *i1, *i2;
+} kem_job;
+
+static void *kem_worker(void *arg) {
+  kem_job *J = (kem_job *)arg;
+  orc_params P;
+  orc_get_params(J->set, &P);
+  for (size_t n = J->lo; n < J->hi; n++) {
+    if (J->op == 0) {
+      orc_kem_keypair(J->set, J->o1 + n * P.pk_bytes, J->o2 + n * P.sk_bytes, J->i1 + n * 96);
+    } else if (J->op == 1) {
+      orc_kem_enc(J->set, J->o1 + n * P.ct_bytes, J->o2 + n * 32, J->i1 + n * P.pk_bytes,
+                  J->i2 + n * 32);
+    } else {
+      int f = orc_kem_dec(J->set, J->o1 + n * 32, J->i1 + n * P.ct_bytes, J->i2 + n * P.sk_bytes);
+      if (J->o3) J->o3[n] = (uint8_t)f;
+    }
+  }
+  return NULL;
+}
+
+static void kem_batch(int op, int set, size_t n, uint8_t *o1, uint8_t *o2, uint8_t *o3,
+                      const uint8_t *i1, const uint8_t *i2, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  kem_job *jobs = (kem_job *)calloc(nthreads, sizeof(kem_job));
+  for (int t = 0; t < nthreads; t++) {
+    kem_job J = {op, set, n * t / nthreads, n * (t + 1) / nthreads, o1, o2, o3, i1, i2};
+    jobs[t] = J;
+  }
+  run_parallel(kem_worker, jobs, sizeof(kem_job), nthreads);
+  free(jobs);
+}
+
+void orc_kem_keypair_batch(int set, size_t n, uint8_t *pk, uint8_t *sk, const uint8_t *coins,
+                           int nthreads) {
+  kem_batch(0, set, n, pk, sk, NULL, coins, NULL, nthreads);
+}
+
+void orc_kem_enc_batch(int set, size_t n, uint8_t *ct, uint8_t *ss, const uint8_t *pk,
+                       const uint8_t *coins, int nthreads) {
+  kem_batch(1, set, n, ct, ss, NULL, pk, coins, nthreads);
+}
+
+void orc_kem_dec_batch(int set, size_t n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk,
+                       uint8_t *fail, int nthreads) {
+  kem_batch(2, set, n, ss, NULL, fail, ct, sk, nthreads);
+}
