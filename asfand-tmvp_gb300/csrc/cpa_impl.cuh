@@ -1,0 +1,365 @@
+// cpa_impl.cuh — the IND-CPA kernel template (one CTA per instance) shared by
+// the per-form translation units cpa_fp8.cu, cpa_int8.cu and cpa_cc.cu.
+//
+// Per instance:
+//   1. 16-byte copies of the packed inputs into shared memory;
+//   2. secrets unpacked (sk: 13-bit SABER pack.cu:34-46 / 2-bit SABLE
+//      pack.cu:366-377) or sampled (CBD of the GenSecret stream,
+//      SABER poly.cu:836-916 / SABLE fips202.cu:625-651);
+//   3. public polynomials unpacked (13/11-bit A, SABER poly.cu:799-816;
+//      10/9-bit b, b', SABER pack.cu:7-17) straight into the engine's layout;
+//   4. the engine (cpa_engine.cuh) computes res[r] = sum_j P[r][j] * s_j;
+//   5. the op's epilogue: rounding (post_process, SABER poly.cu:381-389),
+//      message encoding (post_process2, :391-395), decoding (post_process3,
+//      :398-403), bit packing, and the full ciphertext compare.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include "cpa_engine.cuh"
+#include "cpa_kernels.cuh"
+
+namespace tmvp {
+
+template <int FORM, int OP, int L>
+struct CpaCfg {
+  static constexpr int R = OP == kDecrypt ? 1 : ((OP == kEncrypt || OP == kReenc) ? L + 1 : L);
+  static constexpr bool TC = FORM == kInt8TC || FORM == kFp8TC;
+  static constexpr int D = (FORM == kFp8TC && OP != kDecrypt) ? 3 : 2;
+  static constexpr int Q = tc_ntiles<D>(R);
+  static constexpr int WARPS = Q >= 3 ? 4 : 2;
+  static constexpr int RP = R <= 4 ? 4 : 8;
+  static constexpr bool TMVP = FORM == kCudaCore;
+  static constexpr int NPROD = TMVP ? 3 : 1;
+  static constexpr int NCOL = TMVP ? 128 : 256;
+  static constexpr int NT = TC ? 32 * WARPS : (TMVP ? 96 : 64);
+};
+
+struct CpaLayout {
+  int raw_a, raw_s, raw_b, raw_msg, raw_ct, raw_sk;  // byte offsets (-1: absent)
+  int sec, eng, res, total;
+};
+
+__host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
+
+// Shared-memory layout of one CTA.  eng holds the engine operands (TC: digit
+// columns then Toeplitz copies; CC: Toeplitz sequences, vectors, products).
+template <int FORM, int OP, int L>
+__host__ __device__ inline CpaLayout cpa_layout(const KemParams &P) {
+  using C = CpaCfg<FORM, OP, L>;
+  CpaLayout o;
+  int off = 0;
+  auto take = [&](int bytes) { int r = off; off = align16(off + bytes + 16); return r; };
+  o.raw_a = o.raw_s = o.raw_b = o.raw_msg = o.raw_ct = o.raw_sk = -1;
+  if (OP == kEncrypt || OP == kReenc || OP == kKeygen) {
+    o.raw_a = take(P.gm_bytes);
+    o.raw_s = take(P.gs_bytes);
+  }
+  if (OP == kEncrypt || OP == kReenc) {
+    o.raw_b = take(L * P.polycompbytes);
+    o.raw_msg = take(32);
+  }
+  if (OP == kReenc || OP == kDecrypt) o.raw_ct = take(P.ct_bytes);
+  if (OP == kDecrypt) o.raw_sk = take(P.indcpa_sk_bytes);
+  o.sec = take(L * 256 * 2);
+  int eng;
+  if (C::TC) {
+    eng = L * C::Q * 8 * kColStride + L * kTzBytesPerPoly;
+  } else {
+    eng = L * C::NPROD * 512 * 2 + L * C::NPROD * C::NCOL * C::RP * 2 +
+          (C::TMVP ? 3 * C::RP * 128 * 4 : 0);
+  }
+  o.eng = take(eng);
+  o.res = take(C::R * 256 * 2);
+  o.total = off;
+  return o;
+}
+
+__device__ __forceinline__ void copy16(uint8_t *dst, const uint8_t *src, int nbytes) {
+  const uint4 *s = reinterpret_cast<const uint4 *>(src);
+  uint4 *d = reinterpret_cast<uint4 *>(dst);
+  for (int i = threadIdx.x; i < (nbytes >> 4); i += blockDim.x) d[i] = s[i];
+}
+
+// Byte `ob` of the little-endian w-bit stream of values f(k).
+template <class F>
+__device__ __forceinline__ uint8_t pack_byte(int ob, int w, F f) {
+  int bit0 = 8 * ob;
+  int k0 = bit0 / w, k1 = (bit0 + 7) / w;
+  uint32_t acc = 0;
+  for (int k = k0; k <= k1; k++) {
+    int sh = k * w - bit0;
+    uint32_t v = f(k) & ((1u << w) - 1u);
+    acc |= sh >= 0 ? (v << sh) : (v >> (-sh));
+  }
+  return (uint8_t)acc;
+}
+
+template <int FORM, int OP, int L>
+__global__ void __launch_bounds__(CpaCfg<FORM, OP, L>::NT) k_cpa(CpaArgs a) {
+  using C = CpaCfg<FORM, OP, L>;
+  extern __shared__ __align__(16) uint8_t sm[];
+  const KemParams &P = a.P;
+  const size_t inst = blockIdx.x;
+  const CpaLayout lo = cpa_layout<FORM, OP, L>(P);
+  const int tid = threadIdx.x;
+
+  // 1. packed inputs to shared memory
+  if (lo.raw_a >= 0) copy16(sm + lo.raw_a, a.a_stream + inst * P.gm_bytes, P.gm_bytes);
+  if (lo.raw_s >= 0) copy16(sm + lo.raw_s, a.s_stream + inst * P.gs_bytes, P.gs_bytes);
+  if (lo.raw_b >= 0) copy16(sm + lo.raw_b, a.pk + inst * a.pk_stride + a.pk_off, L * P.polycompbytes);
+  if (lo.raw_msg >= 0) copy16(sm + lo.raw_msg, a.msg + inst * a.msg_stride, 32);
+  if (lo.raw_ct >= 0) copy16(sm + lo.raw_ct, a.ct + inst * P.ct_bytes, P.ct_bytes);
+  if (lo.raw_sk >= 0) copy16(sm + lo.raw_sk, a.sk + inst * P.sk_bytes, P.indcpa_sk_bytes);
+  __syncthreads();
+
+  // 2. secrets, int16 [L][256]
+  int16_t *sec = reinterpret_cast<int16_t *>(sm + lo.sec);
+  {
+    bool bad = false;
+    for (int idx = tid; idx < L * 256; idx += C::NT) {
+      int v;
+      if (OP == kDecrypt) {
+        const uint8_t *rs = sm + lo.raw_sk;
+        if (P.sable) {
+          uint32_t x = get_bits(rs, idx * 2, 2);
+          v = (int)(x ^ 2u) - 2;  // SABLE pack.cu:371-376
+        } else {
+          uint32_t x = get_bits(rs, idx * P.eq, P.eq);
+          v = (int)x - (int)((x >> (P.eq - 1)) << P.eq);
+        }
+      } else if (OP == kMatvec) {
+        v = a.mv_s[inst * (L * 256) + idx];
+      } else {
+        uint32_t x = get_bits(sm + lo.raw_s, idx * P.mu, P.mu);
+        int h = P.mu >> 1;
+        v = __popc(x & ((1u << h) - 1u)) - __popc(x >> h);
+      }
+      if (C::TC && (v > 8 || v < -8)) bad = true;
+      sec[idx] = (int16_t)v;
+    }
+    if (bad && a.err) atomicOr(a.err, 1);
+  }
+
+  // public coefficient (r, j, k) and its bit width
+  auto pub = [&](int r, int j, int k, int &w) -> uint32_t {
+    if (OP == kDecrypt) {
+      w = P.ep;
+      return get_bits(sm + lo.raw_ct, (j * 256 + k) * P.ep, P.ep);
+    } else if (OP == kMatvec) {
+      w = a.mv_eq;
+      size_t base = inst * (size_t)(L * L * 256);
+      int ij = a.mv_transpose ? (j * L + r) : (r * L + j);
+      return a.mv_A[base + ij * 256 + k] & ((1u << a.mv_eq) - 1u);
+    } else if (r == L) {
+      w = P.ep;
+      return get_bits(sm + lo.raw_b, (j * 256 + k) * P.ep, P.ep);
+    } else {
+      w = P.eq;
+      int ij = (OP == kKeygen) ? (j * L + r) : (r * L + j);
+      return get_bits(sm + lo.raw_a, (ij * 256 + k) * P.eq, P.eq);
+    }
+  };
+
+  uint16_t *res = reinterpret_cast<uint16_t *>(sm + lo.res);
+  if (C::TC) {
+    uint32_t *colw = reinterpret_cast<uint32_t *>(sm + lo.eng);
+    uint32_t *tz = colw + L * C::Q * 8 * (kColStride / 4);
+    // zero padding columns
+    for (int idx = tid; idx < L * C::Q * 8 * 64; idx += C::NT) {
+      int w = idx & 63, c = (idx >> 6) % (C::Q * 8), j = idx / (64 * C::Q * 8);
+      int poly, digit;
+      tc_slot<C::D>(c >> 3, c & 7, poly, digit);
+      if (poly >= C::R) colw[(j * C::Q * 8 + c) * (kColStride / 4) + w] = 0u;
+    }
+    // digit columns, four coefficients per word
+    for (int idx = tid; idx < C::R * L * 64; idx += C::NT) {
+      int k4 = idx & 63, j = (idx >> 6) % L, r = idx / (64 * L);
+      int dg[4][C::D];
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        int w;
+        uint32_t x = pub(r, j, 4 * k4 + e, w);
+        public_digits<FORM, C::D>(x, w, dg[e]);
+      }
+#pragma unroll
+      for (int d = 0; d < C::D; d++) {
+        int q, c;
+        if (C::D == 2) {
+          q = r >> 2;
+          c = 2 * (r & 3) + d;
+        } else {
+          int s = 3 * (r >> 2) + d;
+          q = s >> 1;
+          c = 2 * (r & 3) + (s & 1);
+        }
+        colw[(j * C::Q * 8 + q * 8 + c) * (kColStride / 4) + k4] =
+            pack4_small<FORM>(dg[0][d], dg[1][d], dg[2][d], dg[3][d]);
+      }
+    }
+    __syncthreads();  // sec complete
+    for (int j = 0; j < L; j++) stage_toeplitz<FORM>(tz + j * 4 * kTzCopyWords, sec + j * 256);
+    __syncthreads();
+    tc_engine<FORM, C::D, C::Q, C::WARPS>(tz, colw, L, C::R, res);
+  } else {
+    int16_t *tseq = reinterpret_cast<int16_t *>(sm + lo.eng);
+    uint16_t *wv = reinterpret_cast<uint16_t *>(tseq + L * C::NPROD * 512);
+    int *pp = reinterpret_cast<int *>(wv + L * C::NPROD * C::NCOL * C::RP);
+    // vectors
+    for (int idx = tid; idx < L * C::NCOL * C::RP; idx += C::NT) {
+      int r = idx % C::RP, c = (idx / C::RP) % C::NCOL, j = idx / (C::RP * C::NCOL);
+      uint16_t v0 = 0, v1 = 0;
+      if (r < C::R) {
+        int w;
+        v0 = (uint16_t)pub(r, j, c, w);
+        if (C::TMVP) v1 = (uint16_t)pub(r, j, c + 128, w);
+      }
+      if (C::TMVP) {
+        wv[((j * 3 + 0) * C::NCOL + c) * C::RP + r] = (uint16_t)(v0 + v1);
+        wv[((j * 3 + 1) * C::NCOL + c) * C::RP + r] = v1;
+        wv[((j * 3 + 2) * C::NCOL + c) * C::RP + r] = v0;
+      } else {
+        wv[(j * C::NCOL + c) * C::RP + r] = v0;
+      }
+    }
+    __syncthreads();  // sec complete
+    // Toeplitz defining sequences; se(i) = s_ext[i]
+    auto se = [&](int j, int i) -> int {
+      return i >= 255 ? (int)sec[j * 256 + i - 255] : -(int)sec[j * 256 + i + 1];
+    };
+    for (int idx = tid; idx < L * C::NPROD * 512; idx += C::NT) {
+      int e = idx & 511, p = (idx >> 9) % C::NPROD, j = idx / (512 * C::NPROD);
+      int v = 0;
+      if (C::TMVP) {
+        int x = e - 128;
+        if (x >= -127 && x <= 127) {
+          if (p == 0) v = se(j, x + 255);
+          else if (p == 1) v = se(j, x + 127) - se(j, x + 255);
+          else v = se(j, x + 255) - se(j, x + 383);
+        }
+      } else {
+        int x = e - 256;
+        if (x >= -255) v = se(j, x + 255);
+      }
+      tseq[idx] = (int16_t)v;
+    }
+    __syncthreads();
+    cc_engine<C::TMVP, C::RP>(tseq, wv, L, C::R, pp, res);
+  }
+  __syncthreads();
+
+  // 5. epilogues
+  const uint32_t qmask = (1u << P.eq) - 1u, pmask = (1u << P.ep) - 1u;
+  if (OP == kDecrypt) {
+    // decode: m'_k = ((v + h2 - (c_m << (ep-et))) mod p) >> (ep-1)
+    const uint8_t *cmb = sm + lo.raw_ct + L * P.polycompbytes;
+    if (tid < 32) {
+      uint32_t byte = 0;
+#pragma unroll
+      for (int b = 0; b < 8; b++) {
+        int k = 8 * tid + b;
+        uint32_t cm = get_bits(cmb, k * P.et, P.et);
+        uint32_t t = ((uint32_t)res[k] + P.h2 - (cm << (P.ep - P.et))) & pmask;
+        byte |= ((t >> (P.ep - 1)) & 1u) << b;
+      }
+      uint8_t *mo = a.m_out + inst * a.m_out_stride;
+      mo[tid] = (uint8_t)byte;
+      if (a.copy_hpk) mo[32 + tid] = a.sk[inst * P.sk_bytes + P.sk_bytes - 64 + tid];
+    }
+  } else if (OP == kEncrypt || OP == kReenc) {
+    const uint8_t *msg = sm + lo.raw_msg;
+    const int bbytes = L * P.polycompbytes;
+    auto bval = [&](int k) -> uint32_t {  // rounded b'
+      return ((res[k] + P.h1) & qmask) >> (P.eq - P.ep);
+    };
+    auto cval = [&](int k) -> uint32_t {  // encoded message
+      uint32_t mb = (msg[k >> 3] >> (k & 7)) & 1u;
+      return (((uint32_t)res[L * 256 + k] + P.h1 - (mb << (P.ep - 1))) & pmask) >> (P.ep - P.et);
+    };
+    int diff = 0;
+    for (int ob = tid; ob < P.ct_bytes; ob += C::NT) {
+      uint8_t v = ob < bbytes ? pack_byte(ob, P.ep, bval) : pack_byte(ob - bbytes, P.et, cval);
+      if (OP == kEncrypt) a.ct_out[inst * P.ct_bytes + ob] = v;
+      else diff |= (v != sm[lo.raw_ct + ob]);
+    }
+    if (OP == kReenc) {
+      int any = __syncthreads_or(diff);
+      if (tid == 0) a.fail[inst] = (uint8_t)(any != 0);
+    }
+  } else if (OP == kKeygen) {
+    const int bbytes = L * P.polycompbytes;
+    uint8_t *pko = a.pk_out + inst * P.pk_bytes;
+    uint8_t *sko = a.sk_out + inst * a.sk_stride;
+    auto bval = [&](int k) -> uint32_t { return ((res[k] + P.h1) & qmask) >> (P.eq - P.ep); };
+    for (int ob = tid; ob < bbytes; ob += C::NT) {
+      uint8_t v = pack_byte(ob, P.ep, bval);
+      pko[ob] = v;
+      sko[P.indcpa_sk_bytes + ob] = v;
+    }
+    if (tid < 32) sko[P.indcpa_sk_bytes + bbytes + tid] = pko[bbytes + tid];  // seed_A
+    auto sval = [&](int k) -> uint32_t { return (uint32_t)(int)sec[k]; };
+    const int sw = P.sable ? 2 : P.eq;
+    for (int ob = tid; ob < P.indcpa_sk_bytes; ob += C::NT) sko[ob] = pack_byte(ob, sw, sval);
+  } else {  // kMatvec
+    const uint32_t m = (1u << a.mv_eq) - 1u;
+    uint16_t *o = a.mv_out + inst * (size_t)(L * 256);
+    for (int idx = tid; idx < L * 256; idx += C::NT) o[idx] = (uint16_t)(res[idx] & m);
+  }
+}
+
+template <int FORM, int OP, int L>
+inline int launch_one(const CpaArgs &a, cudaStream_t s) {
+  using C = CpaCfg<FORM, OP, L>;
+  const CpaLayout lo = cpa_layout<FORM, OP, L>(a.P);
+  cudaError_t e = cudaFuncSetAttribute(k_cpa<FORM, OP, L>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, lo.total);
+  if (e != cudaSuccess) return (int)e;
+  k_cpa<FORM, OP, L><<<a.n, C::NT, lo.total, s>>>(a);
+  return (int)cudaGetLastError();
+}
+
+template <int FORM, int OP>
+inline int launch_l(const CpaArgs &a, cudaStream_t s) {
+  switch (a.P.l) {
+    case 2: return launch_one<FORM, OP, 2>(a, s);
+    case 3: return launch_one<FORM, OP, 3>(a, s);
+    case 4: return launch_one<FORM, OP, 4>(a, s);
+  }
+  return (int)cudaErrorInvalidValue;
+}
+
+template <int FORM>
+inline int launch_form(int op, const CpaArgs &a, cudaStream_t s) {
+  switch (op) {
+    case kDecrypt: return launch_l<FORM, kDecrypt>(a, s);
+    case kEncrypt: return launch_l<FORM, kEncrypt>(a, s);
+    case kReenc: return launch_l<FORM, kReenc>(a, s);
+    case kKeygen: return launch_l<FORM, kKeygen>(a, s);
+    case kMatvec: return launch_l<FORM, kMatvec>(a, s);
+  }
+  return (int)cudaErrorInvalidValue;
+}
+
+template <int FORM, int OP>
+inline size_t smem_l(const KemParams &P) {
+  switch (P.l) {
+    case 2: return cpa_layout<FORM, OP, 2>(P).total;
+    case 3: return cpa_layout<FORM, OP, 3>(P).total;
+    case 4: return cpa_layout<FORM, OP, 4>(P).total;
+  }
+  return 0;
+}
+
+template <int FORM>
+inline size_t smem_form(int op, const KemParams &P) {
+  switch (op) {
+    case kDecrypt: return smem_l<FORM, kDecrypt>(P);
+    case kEncrypt: return smem_l<FORM, kEncrypt>(P);
+    case kReenc: return smem_l<FORM, kReenc>(P);
+    case kKeygen: return smem_l<FORM, kKeygen>(P);
+    case kMatvec: return smem_l<FORM, kMatvec>(P);
+  }
+  return 0;
+}
+
+}  // namespace tmvp

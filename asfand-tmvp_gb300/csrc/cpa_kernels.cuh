@@ -1,0 +1,57 @@
+// cpa_kernels.cuh — IND-CPA kernels of the batched KEM (one CTA per instance).
+//
+// Ops (reference launch sequences they replace):
+//   kDecrypt  indcpa_kem_dec   SABER cuda_kernel.cu:341-370 / SABLE_indcpa.cu:428-461
+//   kEncrypt  indcpa_kem_enc   SABER cuda_kernel.cu:124-178 / SABLE_indcpa.cu:149-224
+//   kReenc    the re-encryption + compare of decapsulation
+//                              SABER cuda_kernel.cu:383-445 / SABLE_indcpa.cu:473-551
+//   kKeygen   indcpa_kem_keypair (Saber round 3; not in the reference)
+//   kMatvec   MatrixVectorMul alone (SABER poly.cu:269-376, :1396-1453)
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include "kem_common.cuh"
+
+namespace tmvp {
+
+enum CpaOp : int { kDecrypt = 0, kEncrypt = 1, kReenc = 2, kKeygen = 3, kMatvec = 4 };
+
+struct CpaArgs {
+  KemParams P;
+  int n;
+  // kEncrypt / kReenc / kKeygen: raw SHAKE streams
+  const uint8_t *a_stream;  // [n][gm_bytes]
+  const uint8_t *s_stream;  // [n][gs_bytes]
+  // public vector b (pk's packed part): pk + i*pk_stride + pk_off
+  const uint8_t *pk;
+  size_t pk_stride, pk_off;
+  // message (32 bytes): msg + i*msg_stride
+  const uint8_t *msg;
+  size_t msg_stride;
+  const uint8_t *ct;  // [n][ct_bytes] (kDecrypt input, kReenc compare)
+  const uint8_t *sk;  // [n][sk_bytes] (kDecrypt)
+  uint8_t *ct_out;    // kEncrypt
+  uint8_t *fail;      // kReenc: 1 where the re-encryption differs
+  uint8_t *m_out;     // kDecrypt: [n][64] = m' || H(pk) (H(pk) only if sk has one)
+  size_t m_out_stride;
+  int copy_hpk;       // kDecrypt: copy sk's H(pk) into m_out[32:64]
+  uint8_t *pk_out, *sk_out;  // kKeygen (sk_out: indcpa part || pk; stride sk_stride)
+  size_t sk_stride;
+  // kMatvec
+  const uint16_t *mv_A;
+  const int8_t *mv_s;
+  uint16_t *mv_out;
+  int mv_eq, mv_transpose;
+  int *err;           // set when a secret coefficient is outside the form's range
+};
+
+// Dynamic shared memory the kernel for (form, op, l) needs with params P.
+size_t cpa_smem_bytes(int form, int op, const KemParams &P);
+// Threads per CTA.
+int cpa_threads(int form, int op, int l);
+// Launch over a.n instances (one CTA each) on `stream`.  Returns a CUDA error
+// code (0 on success).
+int cpa_launch(int form, int op, const CpaArgs &a, void *stream);
+
+}  // namespace tmvp

@@ -1,0 +1,145 @@
+// hash_kernels.cu — the Keccak stages of the batched KEM: one thread per
+// sponge, register-resident state, 8-byte global accesses.
+//
+// Replaces the reference's single-block hash kernels and its 25-lane
+// shake128_gpu (TMVP-Saber/SABER-GPU/src/poly.cu:918-1114,
+// TMVP_SABLE/src/fips202.cu:409-668), which cap the batch at 1024 and rely
+// on implicit warp synchrony.  Every kernel here covers any batch size with a
+// 1-D grid and has no inter-thread communication.
+#include "hash_kernels.cuh"
+#include "keccak.cuh"
+
+namespace tmvp {
+
+__device__ __forceinline__ void load_words(uint64_t *dst, const uint8_t *src, int nw) {
+  const uint64_t *s = reinterpret_cast<const uint64_t *>(src);
+#pragma unroll 4
+  for (int i = 0; i < nw; i++) dst[i] = s[i];
+}
+
+__device__ __forceinline__ void run_shake_job(const ShakeJob &J, size_t i) {
+  uint64_t seed[4];
+  load_words(seed, J.src + i * J.src_stride + J.src_off, 4);
+  if (J.prehash) {
+    // seed_A <- SHAKE-128(seed_A)[0:32] (Saber round-3 key generation)
+    uint64_t h[4];
+    shake128_32(h, 32, seed);
+#pragma unroll
+    for (int k = 0; k < 4; k++) seed[k] = h[k];
+    if (J.seed_out) {
+      uint64_t *so = reinterpret_cast<uint64_t *>(J.seed_out + i * J.seed_out_stride + J.seed_out_off);
+#pragma unroll
+      for (int k = 0; k < 4; k++) so[k] = seed[k];
+    }
+  }
+  shake128_32(reinterpret_cast<uint64_t *>(J.out + i * J.out_stride), J.out_bytes, seed);
+}
+
+__global__ void __launch_bounds__(128) k_shake_jobs(ShakeJob j0, ShakeJob j1, int n) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (size_t)n) {
+    run_shake_job(j0, t);
+  } else if (j1.out && t < 2 * (size_t)n) {
+    run_shake_job(j1, t - n);
+  }
+}
+
+// Encapsulation front (saber_enc, cuda_kernel.cu:116-127): thread i < n runs
+// m = H(coins), H(pk), kr = G(m || H(pk)) and the GenSecret stream
+// SHAKE-128(kr[32:64]); threads n..2n-1 expand GenMatrix from pk's seed.
+__global__ void __launch_bounds__(128) k_enc_front(KemParams P, const uint8_t *pk,
+                                                    const uint8_t *coins, uint8_t *mbuf,
+                                                    uint8_t *kr, uint8_t *s_stream,
+                                                    uint8_t *a_stream, int n) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (size_t)n) {
+    uint64_t c[4], buf[8], g[8];
+    load_words(c, coins + t * 32, 4);
+    sha3_256_32(buf, c);  // m
+    sha3_256_words(buf + 4, reinterpret_cast<const uint64_t *>(pk + t * P.pk_bytes), P.pk_bytes);
+    sha3_512_64(g, buf);
+    uint64_t *mo = reinterpret_cast<uint64_t *>(mbuf + t * 64);
+    uint64_t *ko = reinterpret_cast<uint64_t *>(kr + t * 64);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      mo[k] = buf[k];
+      ko[k] = g[k];
+    }
+    shake128_32(reinterpret_cast<uint64_t *>(s_stream + t * P.gs_bytes), P.gs_bytes, g + 4);
+  } else if (t < 2 * (size_t)n) {
+    size_t i = t - n;
+    uint64_t seed[4];
+    load_words(seed, pk + i * P.pk_bytes + (size_t)P.l * P.polycompbytes, 4);
+    shake128_32(reinterpret_cast<uint64_t *>(a_stream + i * P.gm_bytes), P.gm_bytes, seed);
+  }
+}
+
+// Decapsulation step after decryption (saber_dec, cuda_kernel.cu:378-385):
+// kr = G(m' || H(pk)) and the GenSecret stream SHAKE-128(kr[32:64]).
+__global__ void __launch_bounds__(128) k_dec_g(KemParams P, const uint8_t *mbuf, uint8_t *kr,
+                                                uint8_t *s_stream, int n) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)n) return;
+  uint64_t buf[8], g[8];
+  load_words(buf, mbuf + t * 64, 8);
+  sha3_512_64(g, buf);
+  uint64_t *ko = reinterpret_cast<uint64_t *>(kr + t * 64);
+#pragma unroll
+  for (int k = 0; k < 8; k++) ko[k] = g[k];
+  shake128_32(reinterpret_cast<uint64_t *>(s_stream + t * P.gs_bytes), P.gs_bytes, g + 4);
+}
+
+// Final key derivation.  Encapsulation (cuda_kernel.cu:185-186):
+// K = H(kr[0:32] || H(c)).  Decapsulation (cuda_kernel.cu:445-450, with the
+// FO selection done as specified): K = H((fail ? z : kr[0:32]) || H(c)), the
+// selection made with a mask so that it does not branch on `fail`.
+__global__ void __launch_bounds__(128) k_final_key(KemParams P, const uint8_t *ct,
+                                                    const uint8_t *kr, const uint8_t *fail,
+                                                    const uint8_t *sk, uint8_t *ss, int n) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)n) return;
+  uint64_t buf[8], k[4];
+  load_words(buf, kr + t * 64, 4);
+  if (fail) {
+    uint64_t mask = 0ull - (uint64_t)(fail[t] != 0);
+    uint64_t z[4];
+    load_words(z, sk + t * P.sk_bytes + P.sk_bytes - 32, 4);
+#pragma unroll
+    for (int w = 0; w < 4; w++) buf[w] ^= mask & (buf[w] ^ z[w]);
+  }
+  sha3_256_words(buf + 4, reinterpret_cast<const uint64_t *>(ct + t * P.ct_bytes), P.ct_bytes);
+  sha3_256_64(k, buf);
+  uint64_t *o = reinterpret_cast<uint64_t *>(ss + t * 32);
+#pragma unroll
+  for (int w = 0; w < 4; w++) o[w] = k[w];
+}
+
+// Key-generation tail: sk[SK-64 : SK-32] = H(pk), sk[SK-32 : SK] = z.
+__global__ void __launch_bounds__(128) k_kp_final(KemParams P, const uint8_t *pk, uint8_t *sk,
+                                                   const uint8_t *coins, int n) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)n) return;
+  uint64_t h[4], z[4];
+  sha3_256_words(h, reinterpret_cast<const uint64_t *>(pk + t * P.pk_bytes), P.pk_bytes);
+  load_words(z, coins + t * 96 + 64, 4);
+  uint64_t *o = reinterpret_cast<uint64_t *>(sk + t * P.sk_bytes + P.sk_bytes - 64);
+#pragma unroll
+  for (int w = 0; w < 4; w++) {
+    o[w] = h[w];
+    o[4 + w] = z[w];
+  }
+}
+
+// Standalone SHA3-256 / SHA3-512 / SHAKE-128 over a batch (used by tests and
+// by the single-instance API).
+__global__ void k_sha3_256_batch(const uint8_t *in, int inbytes, uint8_t *out, int n) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)n) return;
+  uint64_t h[4];
+  sha3_256_words(h, reinterpret_cast<const uint64_t *>(in + t * inbytes), inbytes);
+  uint64_t *o = reinterpret_cast<uint64_t *>(out + t * 32);
+#pragma unroll
+  for (int w = 0; w < 4; w++) o[w] = h[w];
+}
+
+}  // namespace tmvp

@@ -1,0 +1,35 @@
+// hash_kernels.cuh — declarations of the Keccak-stage kernels.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include "kem_common.cuh"
+
+namespace tmvp {
+
+// One SHAKE-128 expansion per instance: 32-byte seed at
+// src + i*src_stride + src_off (8-byte aligned), out_bytes (multiple of 8)
+// written to out + i*out_stride.  prehash: the seed is first replaced by
+// SHAKE-128(seed)[0:32] and, if seed_out is set, stored there.
+struct ShakeJob {
+  const uint8_t *src;
+  size_t src_stride, src_off;
+  uint8_t *out;
+  size_t out_stride;
+  int out_bytes;
+  int prehash;
+  uint8_t *seed_out;
+  size_t seed_out_stride, seed_out_off;
+};
+
+__global__ void k_shake_jobs(ShakeJob j0, ShakeJob j1, int n);
+__global__ void k_enc_front(KemParams P, const uint8_t *pk, const uint8_t *coins, uint8_t *mbuf,
+                            uint8_t *kr, uint8_t *s_stream, uint8_t *a_stream, int n);
+__global__ void k_dec_g(KemParams P, const uint8_t *mbuf, uint8_t *kr, uint8_t *s_stream, int n);
+__global__ void k_final_key(KemParams P, const uint8_t *ct, const uint8_t *kr,
+                            const uint8_t *fail, const uint8_t *sk, uint8_t *ss, int n);
+__global__ void k_kp_final(KemParams P, const uint8_t *pk, uint8_t *sk, const uint8_t *coins,
+                           int n);
+__global__ void k_sha3_256_batch(const uint8_t *in, int inbytes, uint8_t *out, int n);
+
+}  // namespace tmvp

@@ -1,0 +1,863 @@
+// tmvp_kem_api.cu — the C ABI of libtmvpkem (include/tmvp_kem.h): contexts,
+// device workspace, the batched KEM / IND-CPA pipelines, the single-instance
+// NIST-style API and the reference-compatible shims.
+//
+// Pipelines (kernels in launch order, all on the caller's stream):
+//   keypair : k_shake_jobs (seed_A' = SHAKE(seed_A), GenMatrix; GenSecret)
+//             -> k_cpa<kKeygen> -> k_kp_final (H(pk), z)
+//   encaps  : k_enc_front (H(coins), H(pk), G, GenSecret; GenMatrix)
+//             -> k_cpa<kEncrypt> -> k_final_key
+//   decaps  : k_shake_jobs (GenMatrix) -> k_cpa<kDecrypt> -> k_dec_g
+//             -> k_cpa<kReenc> -> k_final_key (implicit rejection)
+// They replace the launch sequences of saber_enc / saber_dec
+// (TMVP-Saber/SABER-GPU/src/cuda_kernel.cu:25-479) and SABLE_enc / SABLE_dec
+// (TMVP_SABLE/src/SABLE_indcpa.cu:24-610).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cerrno>
+#include <climits>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include <sys/random.h>
+
+#include "../../include/tmvp_kem.h"
+#include "cpa_kernels.cuh"
+#include "hash_kernels.cuh"
+#include "kem_common.cuh"
+
+namespace tmvp {
+int cpa_launch_fp8(int op, const CpaArgs &a, cudaStream_t s);
+int cpa_launch_int8(int op, const CpaArgs &a, cudaStream_t s);
+int cpa_launch_cc(int op, const CpaArgs &a, cudaStream_t s);
+int cpa_launch_sb(int op, const CpaArgs &a, cudaStream_t s);
+size_t cpa_smem_fp8(int op, const KemParams &P);
+size_t cpa_smem_int8(int op, const KemParams &P);
+size_t cpa_smem_cc(int op, const KemParams &P);
+size_t cpa_smem_sb(int op, const KemParams &P);
+}  // namespace tmvp
+
+using namespace tmvp;
+
+static thread_local int g_last_error = TMVP_OK;
+
+static int set_err(int code) {
+  g_last_error = code;
+  return code;
+}
+
+struct StageStat {
+  std::string name;
+  uint64_t launches = 0;
+  double total_ms = 0;
+};
+
+struct tmvp_ctx {
+  int device = 0;
+  size_t budget = 0;
+  uint8_t *ws = nullptr;  // device workspace
+  size_t ws_cap = 0;
+  int *d_err = nullptr;   // device-side input-range flag
+  uint64_t launches = 0;
+  std::mutex mu;
+  // optional per-stage timing: CUDA events recorded on the launching stream
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  std::vector<StageStat> stages;
+};
+
+namespace {
+
+constexpr size_t kAlign = 256;
+inline size_t up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
+
+struct Arena {
+  uint8_t *base;
+  size_t off = 0;
+  uint8_t *take(size_t bytes) {
+    uint8_t *p = base + off;
+    off += up(bytes);
+    return p;
+  }
+};
+
+int cuda_err(cudaError_t e) {
+  if (e == cudaSuccess) return TMVP_OK;
+  if (e == cudaErrorMemoryAllocation) return TMVP_ENOMEM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return TMVP_ENOTSUP;
+  return TMVP_EDEVICE;
+}
+
+#define TRY_CUDA(x)                         \
+  do {                                      \
+    cudaError_t e_ = (x);                   \
+    if (e_ != cudaSuccess) return cuda_err(e_); \
+  } while (0)
+
+#define TRY(x)                 \
+  do {                         \
+    int r_ = (x);              \
+    if (r_ != TMVP_OK) return r_; \
+  } while (0)
+
+int ensure_ws(tmvp_ctx *c, size_t bytes) {
+  if (bytes <= c->ws_cap) return TMVP_OK;
+  if (c->budget && bytes > c->budget) return TMVP_ENOMEM;
+  size_t cap = std::max(bytes, c->ws_cap + c->ws_cap / 2);
+  if (c->budget) cap = std::min(cap, c->budget);
+  if (c->ws) {
+    TRY_CUDA(cudaDeviceSynchronize());
+    cudaFree(c->ws);
+    c->ws = nullptr;
+    c->ws_cap = 0;
+  }
+  TRY_CUDA(cudaMalloc(&c->ws, cap));
+  c->ws_cap = cap;
+  return TMVP_OK;
+}
+
+// A caller buffer: used in place if it is 16-byte-aligned device memory of
+// this GPU, else staged through the workspace.
+struct Buf {
+  void *user;
+  size_t bytes;
+  bool host;
+  uint8_t *dev;
+};
+
+bool is_device_ptr(const void *p, int device) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) &&
+         at.device == device;
+}
+
+Buf classify(const void *p, size_t bytes, int device) {
+  Buf b{const_cast<void *>(p), bytes, true, nullptr};
+  if (is_device_ptr(p, device) && ((uintptr_t)p & 15) == 0) {
+    b.host = false;
+    b.dev = (uint8_t *)p;
+  }
+  return b;
+}
+
+size_t stage_bytes(const Buf &b) { return b.host ? up(b.bytes) : 0; }
+
+void stage_assign(Buf &b, Arena &A) {
+  if (b.host) b.dev = A.take(b.bytes);
+}
+
+int upload(const Buf &b, cudaStream_t s) {
+  if (b.host) TRY_CUDA(cudaMemcpyAsync(b.dev, b.user, b.bytes, cudaMemcpyDefault, s));
+  return TMVP_OK;
+}
+
+int download(const Buf &b, cudaStream_t s) {
+  if (b.host) TRY_CUDA(cudaMemcpyAsync(b.user, b.dev, b.bytes, cudaMemcpyDefault, s));
+  return TMVP_OK;
+}
+
+int resolve_form(int form) {
+  if (form == kAuto) return kFp8TC;
+  return form;
+}
+
+cudaEvent_t pool_event(tmvp_ctx *c) {
+  if (!c->ev_pool.empty()) {
+    cudaEvent_t e = c->ev_pool.back();
+    c->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+int stage_index(tmvp_ctx *c, const char *name) {
+  for (size_t i = 0; i < c->stages.size(); i++)
+    if (c->stages[i].name == name) return (int)i;
+  c->stages.push_back(StageStat{name, 0, 0.0});
+  return (int)c->stages.size() - 1;
+}
+
+// Brackets one kernel launch with events when the context's timing is on.
+struct StageTimer {
+  tmvp_ctx *c;
+  cudaStream_t s;
+  int idx = -1;
+  cudaEvent_t a = nullptr, b = nullptr;
+  StageTimer(tmvp_ctx *cc, const char *name, cudaStream_t ss) : c(cc), s(ss) {
+    if (!c->timing) return;
+    idx = stage_index(c, name);
+    a = pool_event(c);
+    b = pool_event(c);
+    cudaEventRecord(a, s);
+  }
+  ~StageTimer() {
+    if (idx < 0) return;
+    cudaEventRecord(b, s);
+    c->pending.push_back({idx, {a, b}});
+  }
+};
+
+void collect_stage_times(tmvp_ctx *c) {
+  for (auto &p : c->pending) {
+    cudaEventSynchronize(p.second.second);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+    c->stages[p.first].launches++;
+    c->stages[p.first].total_ms += ms;
+    c->ev_pool.push_back(p.second.first);
+    c->ev_pool.push_back(p.second.second);
+  }
+  c->pending.clear();
+}
+
+const char *form_tag(int form, int op) {
+  static const char *names[4][5] = {
+      {"cpa_decrypt_cuda_core", "cpa_encrypt_cuda_core", "cpa_reenc_cuda_core", "cpa_keygen_cuda_core", "cpa_matvec_cuda_core"},
+      {"cpa_decrypt_int8_tc", "cpa_encrypt_int8_tc", "cpa_reenc_int8_tc", "cpa_keygen_int8_tc", "cpa_matvec_int8_tc"},
+      {"cpa_decrypt_fp8_tc", "cpa_encrypt_fp8_tc", "cpa_reenc_fp8_tc", "cpa_keygen_fp8_tc", "cpa_matvec_fp8_tc"},
+      {"cpa_decrypt_schoolbook", "cpa_encrypt_schoolbook", "cpa_reenc_schoolbook", "cpa_keygen_schoolbook", "cpa_matvec_schoolbook"}};
+  int f = form == kSchoolbook ? 3 : form;
+  return names[f][op];
+}
+
+int run_cpa(tmvp_ctx *c, int form, int op, CpaArgs &a, cudaStream_t s) {
+  a.err = c->d_err;
+  int e;
+  StageTimer tm(c, form_tag(resolve_form(form), op), s);
+  switch (resolve_form(form)) {
+    case kFp8TC: e = cpa_launch_fp8(op, a, s); break;
+    case kInt8TC: e = cpa_launch_int8(op, a, s); break;
+    case kCudaCore: e = cpa_launch_cc(op, a, s); break;
+    case kSchoolbook: e = cpa_launch_sb(op, a, s); break;
+    default: return TMVP_EINVAL;
+  }
+  c->launches++;
+  return e == 0 ? TMVP_OK : TMVP_EDEVICE;
+}
+
+inline unsigned blocks_for(size_t threads, unsigned bs) { return (unsigned)((threads + bs - 1) / bs); }
+
+int check_common(tmvp_ctx *c, int set, size_t n, int form, KemParams *P) {
+  if (!c) return TMVP_EINVAL;
+  if (!make_params(set, P)) return TMVP_EINVAL;
+  if (n > (size_t)(INT_MAX / 2)) return TMVP_EINVAL;
+  int f = resolve_form(form);
+  if (f != kFp8TC && f != kInt8TC && f != kCudaCore && f != kSchoolbook) return TMVP_EINVAL;
+  return TMVP_OK;
+}
+
+// Reads and clears the device-side input-range flag; a set flag means some
+// secret coefficient was outside the tensor-core forms' exact range.
+int finish(tmvp_ctx *c, cudaStream_t s, bool host_sync) {
+  TRY_CUDA(cudaGetLastError());
+  if (host_sync) {
+    int h = 0;
+    TRY_CUDA(cudaMemcpyAsync(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TRY_CUDA(cudaStreamSynchronize(s));
+    if (h) {
+      cudaMemsetAsync(c->d_err, 0, sizeof(int), s);
+      cudaStreamSynchronize(s);
+      return TMVP_EINVAL;
+    }
+  }
+  return TMVP_OK;
+}
+
+struct Guard {
+  tmvp_ctx *c;
+  int prev = -1;
+  explicit Guard(tmvp_ctx *cc) : c(cc) {
+    cudaGetDevice(&prev);
+    if (prev != c->device) cudaSetDevice(c->device);
+  }
+  ~Guard() {
+    if (prev >= 0 && prev != c->device) cudaSetDevice(prev);
+  }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int tmvp_param_sizes(tmvp_param_set set, tmvp_sizes *out) {
+  KemParams P;
+  if (!out || !make_params(set, &P)) return set_err(TMVP_EINVAL);
+  out->l = P.l;
+  out->eq = P.eq;
+  out->ep = P.ep;
+  out->et = P.et;
+  out->mu = P.mu;
+  out->pk_bytes = P.pk_bytes;
+  out->sk_bytes = P.sk_bytes;
+  out->ct_bytes = P.ct_bytes;
+  out->ss_bytes = 32;
+  out->indcpa_pk_bytes = P.pk_bytes;
+  out->indcpa_sk_bytes = P.indcpa_sk_bytes;
+  return set_err(TMVP_OK);
+}
+
+const char *tmvp_strerror(int code) {
+  switch (code) {
+    case TMVP_OK: return "ok";
+    case TMVP_EINVAL: return "invalid argument";
+    case TMVP_ENOMEM: return "device workspace exceeds the memory budget";
+    case TMVP_EDEVICE: return "CUDA runtime error";
+    case TMVP_ETIMEOUT: return "bounded device wait timed out";
+    case TMVP_ENOTSUP: return "no usable GPU";
+  }
+  return "unknown error";
+}
+
+int tmvp_last_error(void) { return g_last_error; }
+
+int tmvp_ctx_create(int device, size_t mem_budget, tmvp_ctx **out) {
+  if (!out) return set_err(TMVP_EINVAL);
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return set_err(TMVP_ENOTSUP);
+  }
+  if (device < 0 || device >= ndev) return set_err(TMVP_EINVAL);
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return set_err(TMVP_EDEVICE);
+  if (prop.major < 10) return set_err(TMVP_ENOTSUP);  // built for sm_103a only
+  tmvp_ctx *c = new tmvp_ctx();
+  c->device = device;
+  c->budget = mem_budget;
+  Guard g(c);
+  if (cudaMalloc(&c->d_err, sizeof(int)) != cudaSuccess || cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) {
+    delete c;
+    return set_err(TMVP_EDEVICE);
+  }
+  *out = c;
+  return set_err(TMVP_OK);
+}
+
+void tmvp_ctx_destroy(tmvp_ctx *c) {
+  if (!c) return;
+  {
+    Guard g(c);
+    cudaDeviceSynchronize();
+    collect_stage_times(c);
+    for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+    if (c->ws) cudaFree(c->ws);
+    if (c->d_err) cudaFree(c->d_err);
+  }
+  delete c;
+}
+
+size_t tmvp_ctx_workspace_bytes(const tmvp_ctx *c) { return c ? c->ws_cap : 0; }
+
+int tmvp_ctx_set_timing(tmvp_ctx *c, int enable) {
+  if (!c) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  collect_stage_times(c);
+  c->timing = enable != 0;
+  if (!c->timing) c->stages.clear();
+  return set_err(TMVP_OK);
+}
+
+int tmvp_ctx_stage_stats(tmvp_ctx *c, int idx, char *name, size_t name_len, uint64_t *launches,
+                         double *total_ms) {
+  if (!c) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  collect_stage_times(c);
+  if (idx < 0) return (int)c->stages.size();
+  if ((size_t)idx >= c->stages.size()) return set_err(TMVP_EINVAL);
+  const StageStat &st = c->stages[idx];
+  if (name && name_len) {
+    size_t k = std::min(name_len - 1, st.name.size());
+    memcpy(name, st.name.data(), k);
+    name[k] = 0;
+  }
+  if (launches) *launches = st.launches;
+  if (total_ms) *total_ms = st.total_ms;
+  return set_err(TMVP_OK);
+}
+uint64_t tmvp_ctx_launch_count(const tmvp_ctx *c) { return c ? c->launches : 0; }
+
+int tmvp_kem_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *pk, uint8_t *sk,
+                           const uint8_t *coins, tmvp_form form, void *stream) {
+  KemParams P;
+  int r = check_common(c, set, n, form, &P);
+  if (r) return set_err(r);
+  if (n == 0) return set_err(TMVP_OK);
+  if (!pk || !sk || !coins) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  cudaStream_t s = (cudaStream_t)stream;
+  Buf bpk = classify(pk, n * P.pk_bytes, c->device), bsk = classify(sk, n * P.sk_bytes, c->device),
+      bco = classify(coins, n * 96, c->device);
+  size_t need = up(n * P.gm_bytes) + up(n * P.gs_bytes) + stage_bytes(bpk) + stage_bytes(bsk) +
+                stage_bytes(bco);
+  if ((r = ensure_ws(c, need))) return set_err(r);
+  Arena A{c->ws};
+  uint8_t *a_stream = A.take(n * P.gm_bytes), *s_stream = A.take(n * P.gs_bytes);
+  stage_assign(bpk, A);
+  stage_assign(bsk, A);
+  stage_assign(bco, A);
+  if ((r = upload(bco, s))) return set_err(r);
+  ShakeJob j0{bco.dev, 96, 0, a_stream, (size_t)P.gm_bytes, P.gm_bytes, 1, bpk.dev,
+              (size_t)P.pk_bytes, (size_t)P.l * P.polycompbytes};
+  ShakeJob j1{bco.dev, 96, 32, s_stream, (size_t)P.gs_bytes, P.gs_bytes, 0, nullptr, 0, 0};
+  {
+    StageTimer tm_(c, "shake_jobs", s);
+    k_shake_jobs<<<blocks_for(2 * n, 128), 128, 0, s>>>(j0, j1, (int)n);
+  }
+  c->launches++;
+  CpaArgs a{};
+  a.P = P;
+  a.n = (int)n;
+  a.a_stream = a_stream;
+  a.s_stream = s_stream;
+  a.pk_out = bpk.dev;
+  a.sk_out = bsk.dev;
+  a.sk_stride = P.sk_bytes;
+  if ((r = run_cpa(c, form, kKeygen, a, s))) return set_err(r);
+  {
+    StageTimer tm_(c, "kp_final", s);
+    k_kp_final<<<blocks_for(n, 128), 128, 0, s>>>(P, bpk.dev, bsk.dev, bco.dev, (int)n);
+  }
+  c->launches++;
+  if ((r = download(bpk, s)) || (r = download(bsk, s))) return set_err(r);
+  return set_err(finish(c, s, bpk.host || bsk.host));
+}
+
+int tmvp_kem_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, uint8_t *ss,
+                       const uint8_t *pk, const uint8_t *coins, tmvp_form form, void *stream) {
+  KemParams P;
+  int r = check_common(c, set, n, form, &P);
+  if (r) return set_err(r);
+  if (n == 0) return set_err(TMVP_OK);
+  if (!ct || !ss || !pk || !coins) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  cudaStream_t s = (cudaStream_t)stream;
+  Buf bct = classify(ct, n * P.ct_bytes, c->device), bss = classify(ss, n * 32, c->device),
+      bpk = classify(pk, n * P.pk_bytes, c->device), bco = classify(coins, n * 32, c->device);
+  size_t need = up(n * P.gm_bytes) + up(n * P.gs_bytes) + 2 * up(n * 64) + stage_bytes(bct) +
+                stage_bytes(bss) + stage_bytes(bpk) + stage_bytes(bco);
+  if ((r = ensure_ws(c, need))) return set_err(r);
+  Arena A{c->ws};
+  uint8_t *a_stream = A.take(n * P.gm_bytes), *s_stream = A.take(n * P.gs_bytes);
+  uint8_t *mbuf = A.take(n * 64), *kr = A.take(n * 64);
+  stage_assign(bct, A);
+  stage_assign(bss, A);
+  stage_assign(bpk, A);
+  stage_assign(bco, A);
+  if ((r = upload(bpk, s)) || (r = upload(bco, s))) return set_err(r);
+  {
+    StageTimer tm_(c, "enc_front", s);
+    k_enc_front<<<blocks_for(2 * n, 128), 128, 0, s>>>(P, bpk.dev, bco.dev, mbuf, kr, s_stream,
+                                                       a_stream, (int)n);
+  }
+  c->launches++;
+  CpaArgs a{};
+  a.P = P;
+  a.n = (int)n;
+  a.a_stream = a_stream;
+  a.s_stream = s_stream;
+  a.pk = bpk.dev;
+  a.pk_stride = P.pk_bytes;
+  a.pk_off = 0;
+  a.msg = mbuf;
+  a.msg_stride = 64;
+  a.ct_out = bct.dev;
+  if ((r = run_cpa(c, form, kEncrypt, a, s))) return set_err(r);
+  {
+    StageTimer tm_(c, "final_key", s);
+    k_final_key<<<blocks_for(n, 128), 128, 0, s>>>(P, bct.dev, kr, nullptr, nullptr, bss.dev, (int)n);
+  }
+  c->launches++;
+  if ((r = download(bct, s)) || (r = download(bss, s))) return set_err(r);
+  return set_err(finish(c, s, bct.host || bss.host));
+}
+
+int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, const uint8_t *ct,
+                       const uint8_t *sk, tmvp_form form, void *stream) {
+  KemParams P;
+  int r = check_common(c, set, n, form, &P);
+  if (r) return set_err(r);
+  if (n == 0) return set_err(TMVP_OK);
+  if (!ss || !ct || !sk) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  cudaStream_t s = (cudaStream_t)stream;
+  Buf bss = classify(ss, n * 32, c->device), bct = classify(ct, n * P.ct_bytes, c->device),
+      bsk = classify(sk, n * P.sk_bytes, c->device);
+  size_t need = up(n * P.gm_bytes) + up(n * P.gs_bytes) + 2 * up(n * 64) + up(n) +
+                stage_bytes(bss) + stage_bytes(bct) + stage_bytes(bsk);
+  if ((r = ensure_ws(c, need))) return set_err(r);
+  Arena A{c->ws};
+  uint8_t *a_stream = A.take(n * P.gm_bytes), *s_stream = A.take(n * P.gs_bytes);
+  uint8_t *mbuf = A.take(n * 64), *kr = A.take(n * 64), *fail = A.take(n);
+  stage_assign(bss, A);
+  stage_assign(bct, A);
+  stage_assign(bsk, A);
+  if ((r = upload(bct, s)) || (r = upload(bsk, s))) return set_err(r);
+  // GenMatrix from the seed of the pk embedded in sk
+  ShakeJob j0{bsk.dev, (size_t)P.sk_bytes,
+              (size_t)P.indcpa_sk_bytes + (size_t)P.l * P.polycompbytes, a_stream,
+              (size_t)P.gm_bytes, P.gm_bytes, 0, nullptr, 0, 0};
+  ShakeJob none{};
+  {
+    StageTimer tm_(c, "shake_jobs", s);
+    k_shake_jobs<<<blocks_for(n, 128), 128, 0, s>>>(j0, none, (int)n);
+  }
+  c->launches++;
+  CpaArgs a{};
+  a.P = P;
+  a.n = (int)n;
+  a.ct = bct.dev;
+  a.sk = bsk.dev;
+  a.m_out = mbuf;
+  a.m_out_stride = 64;
+  a.copy_hpk = 1;
+  if ((r = run_cpa(c, form, kDecrypt, a, s))) return set_err(r);
+  {
+    StageTimer tm_(c, "dec_g", s);
+    k_dec_g<<<blocks_for(n, 128), 128, 0, s>>>(P, mbuf, kr, s_stream, (int)n);
+  }
+  c->launches++;
+  CpaArgs b{};
+  b.P = P;
+  b.n = (int)n;
+  b.a_stream = a_stream;
+  b.s_stream = s_stream;
+  b.pk = bsk.dev;
+  b.pk_stride = P.sk_bytes;
+  b.pk_off = P.indcpa_sk_bytes;
+  b.msg = mbuf;
+  b.msg_stride = 64;
+  b.ct = bct.dev;
+  b.fail = fail;
+  if ((r = run_cpa(c, form, kReenc, b, s))) return set_err(r);
+  {
+    StageTimer tm_(c, "final_key", s);
+    k_final_key<<<blocks_for(n, 128), 128, 0, s>>>(P, bct.dev, kr, fail, bsk.dev, bss.dev, (int)n);
+  }
+  c->launches++;
+  if ((r = download(bss, s))) return set_err(r);
+  return set_err(finish(c, s, bss.host));
+}
+
+int tmvp_indcpa_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *pk, uint8_t *sk,
+                              const uint8_t *seeds, tmvp_form form, void *stream) {
+  KemParams P;
+  int r = check_common(c, set, n, form, &P);
+  if (r) return set_err(r);
+  if (n == 0) return set_err(TMVP_OK);
+  if (!pk || !sk || !seeds) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  cudaStream_t s = (cudaStream_t)stream;
+  Buf bpk = classify(pk, n * P.pk_bytes, c->device),
+      bsk = classify(sk, n * P.indcpa_sk_bytes, c->device),
+      bse = classify(seeds, n * 64, c->device);
+  // the keygen kernel also writes pk behind the indcpa secret; give it a full-size sk scratch
+  size_t need = up(n * P.gm_bytes) + up(n * P.gs_bytes) + up(n * P.sk_bytes) + stage_bytes(bpk) +
+                stage_bytes(bse);
+  if ((r = ensure_ws(c, need))) return set_err(r);
+  Arena A{c->ws};
+  uint8_t *a_stream = A.take(n * P.gm_bytes), *s_stream = A.take(n * P.gs_bytes);
+  uint8_t *skfull = A.take(n * P.sk_bytes);
+  stage_assign(bpk, A);
+  stage_assign(bse, A);
+  if ((r = upload(bse, s))) return set_err(r);
+  ShakeJob j0{bse.dev, 64, 0, a_stream, (size_t)P.gm_bytes, P.gm_bytes, 1, bpk.dev,
+              (size_t)P.pk_bytes, (size_t)P.l * P.polycompbytes};
+  ShakeJob j1{bse.dev, 64, 32, s_stream, (size_t)P.gs_bytes, P.gs_bytes, 0, nullptr, 0, 0};
+  {
+    StageTimer tm_(c, "shake_jobs", s);
+    k_shake_jobs<<<blocks_for(2 * n, 128), 128, 0, s>>>(j0, j1, (int)n);
+  }
+  c->launches++;
+  CpaArgs a{};
+  a.P = P;
+  a.n = (int)n;
+  a.a_stream = a_stream;
+  a.s_stream = s_stream;
+  a.pk_out = bpk.dev;
+  a.sk_out = skfull;
+  a.sk_stride = P.sk_bytes;
+  if ((r = run_cpa(c, form, kKeygen, a, s))) return set_err(r);
+  TRY_CUDA(cudaMemcpy2DAsync(bsk.user, P.indcpa_sk_bytes, skfull, P.sk_bytes, P.indcpa_sk_bytes, n,
+                             cudaMemcpyDefault, s));
+  if ((r = download(bpk, s))) return set_err(r);
+  return set_err(finish(c, s, bpk.host || bsk.host));
+}
+
+int tmvp_indcpa_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, const uint8_t *m,
+                          const uint8_t *noiseseed, const uint8_t *pk, tmvp_form form,
+                          void *stream) {
+  KemParams P;
+  int r = check_common(c, set, n, form, &P);
+  if (r) return set_err(r);
+  if (n == 0) return set_err(TMVP_OK);
+  if (!ct || !m || !noiseseed || !pk) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  cudaStream_t s = (cudaStream_t)stream;
+  Buf bct = classify(ct, n * P.ct_bytes, c->device), bm = classify(m, n * 32, c->device),
+      bns = classify(noiseseed, n * 32, c->device), bpk = classify(pk, n * P.pk_bytes, c->device);
+  size_t need = up(n * P.gm_bytes) + up(n * P.gs_bytes) + stage_bytes(bct) + stage_bytes(bm) +
+                stage_bytes(bns) + stage_bytes(bpk);
+  if ((r = ensure_ws(c, need))) return set_err(r);
+  Arena A{c->ws};
+  uint8_t *a_stream = A.take(n * P.gm_bytes), *s_stream = A.take(n * P.gs_bytes);
+  stage_assign(bct, A);
+  stage_assign(bm, A);
+  stage_assign(bns, A);
+  stage_assign(bpk, A);
+  if ((r = upload(bm, s)) || (r = upload(bns, s)) || (r = upload(bpk, s))) return set_err(r);
+  ShakeJob j0{bns.dev, 32, 0, s_stream, (size_t)P.gs_bytes, P.gs_bytes, 0, nullptr, 0, 0};
+  ShakeJob j1{bpk.dev, (size_t)P.pk_bytes, (size_t)P.l * P.polycompbytes, a_stream,
+              (size_t)P.gm_bytes, P.gm_bytes, 0, nullptr, 0, 0};
+  {
+    StageTimer tm_(c, "shake_jobs", s);
+    k_shake_jobs<<<blocks_for(2 * n, 128), 128, 0, s>>>(j0, j1, (int)n);
+  }
+  c->launches++;
+  CpaArgs a{};
+  a.P = P;
+  a.n = (int)n;
+  a.a_stream = a_stream;
+  a.s_stream = s_stream;
+  a.pk = bpk.dev;
+  a.pk_stride = P.pk_bytes;
+  a.msg = bm.dev;
+  a.msg_stride = 32;
+  a.ct_out = bct.dev;
+  if ((r = run_cpa(c, form, kEncrypt, a, s))) return set_err(r);
+  if ((r = download(bct, s))) return set_err(r);
+  return set_err(finish(c, s, bct.host));
+}
+
+int tmvp_indcpa_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *m, const uint8_t *sk,
+                          const uint8_t *ct, tmvp_form form, void *stream) {
+  KemParams P;
+  int r = check_common(c, set, n, form, &P);
+  if (r) return set_err(r);
+  if (n == 0) return set_err(TMVP_OK);
+  if (!m || !sk || !ct) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  cudaStream_t s = (cudaStream_t)stream;
+  // the decrypt kernel reads sk with stride sk_bytes; the indcpa secret key is
+  // repacked into a full-stride scratch
+  Buf bm = classify(m, n * 32, c->device), bct = classify(ct, n * P.ct_bytes, c->device),
+      bsk = classify(sk, n * P.indcpa_sk_bytes, c->device);
+  size_t need = up(n * P.sk_bytes) + stage_bytes(bm) + stage_bytes(bct);
+  if ((r = ensure_ws(c, need))) return set_err(r);
+  Arena A{c->ws};
+  uint8_t *skfull = A.take(n * P.sk_bytes);
+  stage_assign(bm, A);
+  stage_assign(bct, A);
+  if ((r = upload(bct, s))) return set_err(r);
+  TRY_CUDA(cudaMemcpy2DAsync(skfull, P.sk_bytes, bsk.user, P.indcpa_sk_bytes, P.indcpa_sk_bytes, n,
+                             cudaMemcpyDefault, s));
+  CpaArgs a{};
+  a.P = P;
+  a.n = (int)n;
+  a.ct = bct.dev;
+  a.sk = skfull;
+  a.m_out = bm.dev;
+  a.m_out_stride = 32;
+  a.copy_hpk = 0;
+  if ((r = run_cpa(c, form, kDecrypt, a, s))) return set_err(r);
+  if ((r = download(bm, s))) return set_err(r);
+  return set_err(finish(c, s, bm.host));
+}
+
+int tmvp_matvec_batch(tmvp_ctx *c, size_t n, int l, int eq, int transpose, uint16_t *out,
+                      const uint16_t *A_, const int8_t *s_, tmvp_form form, void *stream) {
+  if (!c || l < 2 || l > 4 || eq < 2 || eq > 13 || n > (size_t)INT_MAX) return set_err(TMVP_EINVAL);
+  if (n == 0) return set_err(TMVP_OK);
+  if (!out || !A_ || !s_) return set_err(TMVP_EINVAL);
+  int f = resolve_form(form);
+  if (f != kFp8TC && f != kInt8TC && f != kCudaCore && f != kSchoolbook) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  cudaStream_t st = (cudaStream_t)stream;
+  Buf bo = classify(out, n * l * 256 * 2, c->device), ba = classify(A_, n * l * l * 256 * 2, c->device),
+      bs = classify(s_, n * l * 256, c->device);
+  int r;
+  if ((r = ensure_ws(c, stage_bytes(bo) + stage_bytes(ba) + stage_bytes(bs) + kAlign))) return set_err(r);
+  Arena Ar{c->ws};
+  stage_assign(bo, Ar);
+  stage_assign(ba, Ar);
+  stage_assign(bs, Ar);
+  if ((r = upload(ba, st)) || (r = upload(bs, st))) return set_err(r);
+  KemParams P{};
+  P.l = l;
+  P.eq = eq;
+  CpaArgs a{};
+  a.P = P;
+  a.n = (int)n;
+  a.mv_A = (const uint16_t *)ba.dev;
+  a.mv_s = (const int8_t *)bs.dev;
+  a.mv_out = (uint16_t *)bo.dev;
+  a.mv_eq = eq;
+  a.mv_transpose = transpose;
+  if ((r = run_cpa(c, form, kMatvec, a, st))) return set_err(r);
+  if ((r = download(bo, st))) return set_err(r);
+  return set_err(finish(c, st, bo.host || ba.host || bs.host));
+}
+
+// ---------------------------------------------------------------------------
+// Single-instance API and reference shims (one process-wide context)
+// ---------------------------------------------------------------------------
+static std::mutex g_mu;
+static tmvp_ctx *g_ctx = nullptr;
+static tmvp_param_set g_set = TMVP_SABER;
+static tmvp_randombytes_fn g_rb = nullptr;
+static size_t g_ref_batch[2] = {1, 512};
+
+static void os_randombytes(uint8_t *out, size_t len) {
+  while (len > 0) {
+    ssize_t k = getrandom(out, len, 0);
+    if (k < 0) {
+      if (errno == EINTR) continue;
+      abort();
+    }
+    out += k;
+    len -= (size_t)k;
+  }
+}
+
+static void randombytes(uint8_t *out, size_t len) { (g_rb ? g_rb : os_randombytes)(out, len); }
+
+static tmvp_ctx *default_ctx() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_ctx) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (tmvp_ctx_create(dev, 0, &g_ctx) != TMVP_OK) g_ctx = nullptr;
+  }
+  return g_ctx;
+}
+
+void tmvp_set_randombytes(tmvp_randombytes_fn fn) { g_rb = fn; }
+
+int tmvp_set_default_param_set(tmvp_param_set set) {
+  KemParams P;
+  if (!make_params(set, &P)) return set_err(TMVP_EINVAL);
+  g_set = set;
+  return set_err(TMVP_OK);
+}
+
+int crypto_kem_keypair(uint8_t *pk, uint8_t *sk) {
+  tmvp_ctx *c = default_ctx();
+  if (!c) return set_err(TMVP_ENOTSUP);
+  uint8_t coins[96];
+  randombytes(coins, 96);
+  return tmvp_kem_keypair_batch(c, g_set, 1, pk, sk, coins, TMVP_FORM_AUTO, nullptr);
+}
+
+int crypto_kem_enc(uint8_t *ct, uint8_t *ss, const uint8_t *pk) {
+  tmvp_ctx *c = default_ctx();
+  if (!c) return set_err(TMVP_ENOTSUP);
+  uint8_t coins[32];
+  randombytes(coins, 32);
+  return tmvp_kem_enc_batch(c, g_set, 1, ct, ss, pk, coins, TMVP_FORM_AUTO, nullptr);
+}
+
+int crypto_kem_dec(uint8_t *ss, const uint8_t *ct, const uint8_t *sk) {
+  tmvp_ctx *c = default_ctx();
+  if (!c) return set_err(TMVP_ENOTSUP);
+  return tmvp_kem_dec_batch(c, g_set, 1, ss, ct, sk, TMVP_FORM_AUTO, nullptr);
+}
+
+int indcpa_kem_keypair(uint8_t *pk, uint8_t *sk) {
+  tmvp_ctx *c = default_ctx();
+  if (!c) return set_err(TMVP_ENOTSUP);
+  uint8_t seeds[64];
+  randombytes(seeds, 64);
+  return tmvp_indcpa_keypair_batch(c, g_set, 1, pk, sk, seeds, TMVP_FORM_AUTO, nullptr);
+}
+
+int indcpa_kem_enc(const uint8_t m[32], const uint8_t seed_sp[32], const uint8_t *pk,
+                   uint8_t *ciphertext) {
+  tmvp_ctx *c = default_ctx();
+  if (!c) return set_err(TMVP_ENOTSUP);
+  return tmvp_indcpa_enc_batch(c, g_set, 1, ciphertext, m, seed_sp, pk, TMVP_FORM_AUTO, nullptr);
+}
+
+int indcpa_kem_dec(const uint8_t *sk, const uint8_t *ciphertext, uint8_t m[32]) {
+  tmvp_ctx *c = default_ctx();
+  if (!c) return set_err(TMVP_ENOTSUP);
+  return tmvp_indcpa_dec_batch(c, g_set, 1, m, sk, ciphertext, TMVP_FORM_AUTO, nullptr);
+}
+
+int tmvp_ref_set_batch(int scheme, size_t n) {
+  if (scheme < 0 || scheme > 1 || n == 0) return set_err(TMVP_EINVAL);
+  g_ref_batch[scheme] = n;
+  return set_err(TMVP_OK);
+}
+
+size_t tmvp_ref_batch(int scheme) { return (scheme == 0 || scheme == 1) ? g_ref_batch[scheme] : 0; }
+
+static tmvp_form mode_form(int mode) {
+  return mode == 0 ? TMVP_FORM_AUTO : (mode == 1 ? TMVP_FORM_CUDA_CORE : TMVP_FORM_SCHOOLBOOK);
+}
+
+static void shim_enc(tmvp_param_set set, size_t B, int mode, uint8_t *h_k, uint8_t *h_pk,
+                     uint8_t *h_c) {
+  tmvp_ctx *c = default_ctx();
+  if (!c) {
+    set_err(TMVP_ENOTSUP);
+    return;
+  }
+  std::vector<uint8_t> coins(32 * B);
+  randombytes(coins.data(), coins.size());
+  tmvp_kem_enc_batch(c, set, B, h_c, h_k, h_pk, coins.data(), mode_form(mode), nullptr);
+}
+
+static void shim_dec(tmvp_param_set set, size_t B, int mode, uint8_t *h_c, uint8_t *h_sk,
+                     uint8_t *h_k) {
+  tmvp_ctx *c = default_ctx();
+  if (!c) {
+    set_err(TMVP_ENOTSUP);
+    return;
+  }
+  tmvp_kem_dec_batch(c, set, B, h_k, h_c, h_sk, mode_form(mode), nullptr);
+}
+
+void saber_enc(uint8_t mode, uint8_t *h_k, uint8_t *h_pk, uint8_t *h_c) {
+  shim_enc(TMVP_SABER, g_ref_batch[0], mode, h_k, h_pk, h_c);
+}
+
+void saber_dec(uint8_t mode, uint8_t *h_c, uint8_t *h_pk, uint8_t *h_sk, uint8_t *h_k) {
+  (void)h_pk;
+  shim_dec(TMVP_SABER, g_ref_batch[0], mode, h_c, h_sk, h_k);
+}
+
+void SABLE_enc(uint8_t *h_k, uint8_t *h_pk, uint8_t *h_c, int mode) {
+  shim_enc(TMVP_SABLE, g_ref_batch[1], mode, h_k, h_pk, h_c);
+}
+
+void SABLE_dec(uint8_t *h_c, uint8_t *h_pk, uint8_t *h_sk, uint8_t *h_k, int mode) {
+  (void)h_pk;
+  shim_dec(TMVP_SABLE, g_ref_batch[1], mode, h_c, h_sk, h_k);
+}
+
+}  // extern "C"

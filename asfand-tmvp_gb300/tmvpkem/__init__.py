@@ -1,0 +1,296 @@
+"""Python mirror of libtmvpkem's C ABI (include/tmvp_kem.h).
+
+The library is the product: hand-written sm_103a CUDA kernels behind a C ABI.
+This module only loads it with ctypes and wraps its entry points for numpy
+arrays (host buffers) and CUDA tensors / raw device pointers (device
+buffers).  There is no CPU fallback: if the shared library is missing the
+loader raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+LIGHTSABER, SABER, FIRESABER, LIGHTSABLE, SABLE, FIRESABLE = range(6)
+SET_NAMES = {LIGHTSABER: "LightSaber", SABER: "Saber", FIRESABER: "FireSaber",
+             LIGHTSABLE: "LightSable", SABLE: "Sable", FIRESABLE: "FireSable"}
+FORM_CUDA_CORE, FORM_INT8_TC, FORM_FP8_TC, FORM_AUTO, FORM_SCHOOLBOOK = range(5)
+FORM_NAMES = {FORM_CUDA_CORE: "cuda_core", FORM_INT8_TC: "int8_tc", FORM_FP8_TC: "fp8_tc",
+              FORM_AUTO: "auto", FORM_SCHOOLBOOK: "schoolbook"}
+
+OK, EINVAL, ENOMEM, EDEVICE, ETIMEOUT, ENOTSUP = 0, -1, -2, -3, -4, -5
+
+LIB_PATH = _build.LIB
+HEADER = os.path.join(_build.REPO, "include", "tmvp_kem.h")
+_lib = None
+
+
+class TmvpError(RuntimeError):
+    def __init__(self, code: int, what: str = ""):
+        self.code = code
+        msg = lib().tmvp_strerror(code).decode() if _lib is not None else str(code)
+        super().__init__(f"{what}: {msg} ({code})" if what else f"{msg} ({code})")
+
+
+class Sizes(ctypes.Structure):
+    _fields_ = [("l", ctypes.c_int), ("eq", ctypes.c_int), ("ep", ctypes.c_int),
+                ("et", ctypes.c_int), ("mu", ctypes.c_int), ("pk_bytes", ctypes.c_size_t),
+                ("sk_bytes", ctypes.c_size_t), ("ct_bytes", ctypes.c_size_t),
+                ("ss_bytes", ctypes.c_size_t), ("indcpa_pk_bytes", ctypes.c_size_t),
+                ("indcpa_sk_bytes", ctypes.c_size_t)]
+
+
+def exported_symbols() -> list[str]:
+    """Function names declared in include/tmvp_kem.h."""
+    import re
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    names = re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", txt)
+    skip = {"typedef", "if", "defined", "sizeof", "void"}
+    out = []
+    for nm in names:
+        if nm in skip or nm.isupper() or nm == "tmvp_randombytes_fn":
+            continue
+        if nm not in out:
+            out.append(nm)
+    return out
+
+
+def lib(build_if_missing: bool = False):
+    """Load libtmvpkem.so (in-tree build).  Raises if it is not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise RuntimeError(f"{LIB_PATH} is not built; run tmvpkem.build.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    P, S, I = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int
+    L.tmvp_strerror.restype = ctypes.c_char_p
+    L.tmvp_strerror.argtypes = [I]
+    L.tmvp_param_sizes.argtypes = [I, ctypes.POINTER(Sizes)]
+    L.tmvp_ctx_create.argtypes = [I, S, ctypes.POINTER(P)]
+    L.tmvp_ctx_destroy.argtypes = [P]
+    L.tmvp_ctx_destroy.restype = None
+    L.tmvp_ctx_workspace_bytes.argtypes = [P]
+    L.tmvp_ctx_workspace_bytes.restype = S
+    L.tmvp_ctx_launch_count.argtypes = [P]
+    L.tmvp_ctx_launch_count.restype = ctypes.c_uint64
+    L.tmvp_ctx_set_timing.argtypes = [P, I]
+    L.tmvp_ctx_stage_stats.argtypes = [P, I, ctypes.c_char_p, S, ctypes.POINTER(ctypes.c_uint64),
+                                       ctypes.POINTER(ctypes.c_double)]
+    L.tmvp_kem_keypair_batch.argtypes = [P, I, S, P, P, P, I, P]
+    L.tmvp_kem_enc_batch.argtypes = [P, I, S, P, P, P, P, I, P]
+    L.tmvp_kem_dec_batch.argtypes = [P, I, S, P, P, P, I, P]
+    L.tmvp_indcpa_keypair_batch.argtypes = [P, I, S, P, P, P, I, P]
+    L.tmvp_indcpa_enc_batch.argtypes = [P, I, S, P, P, P, P, I, P]
+    L.tmvp_indcpa_dec_batch.argtypes = [P, I, S, P, P, P, I, P]
+    L.tmvp_matvec_batch.argtypes = [P, S, I, I, I, P, P, P, I, P]
+    for nm in ("crypto_kem_keypair", "indcpa_kem_keypair"):
+        getattr(L, nm).argtypes = [P, P]
+    L.crypto_kem_enc.argtypes = [P, P, P]
+    L.crypto_kem_dec.argtypes = [P, P, P]
+    L.indcpa_kem_enc.argtypes = [P, P, P, P]
+    L.indcpa_kem_dec.argtypes = [P, P, P]
+    L.tmvp_set_randombytes.argtypes = [P]
+    L.tmvp_set_randombytes.restype = None
+    L.tmvp_set_default_param_set.argtypes = [I]
+    L.saber_enc.argtypes = [ctypes.c_uint8, P, P, P]
+    L.saber_dec.argtypes = [ctypes.c_uint8, P, P, P, P]
+    L.SABLE_enc.argtypes = [P, P, P, I]
+    L.SABLE_dec.argtypes = [P, P, P, P, I]
+    for nm in ("saber_enc", "saber_dec", "SABLE_enc", "SABLE_dec"):
+        getattr(L, nm).restype = None
+    L.tmvp_ref_set_batch.argtypes = [I, S]
+    L.tmvp_ref_batch.argtypes = [I]
+    L.tmvp_ref_batch.restype = S
+    _lib = L
+    return L
+
+
+def sizes(set_id: int) -> Sizes:
+    s = Sizes()
+    rc = lib().tmvp_param_sizes(set_id, ctypes.byref(s))
+    if rc:
+        raise TmvpError(rc, "tmvp_param_sizes")
+    return s
+
+
+RANDOMBYTES_FN = ctypes.CFUNCTYPE(None, ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t)
+
+
+def _ptr(x):
+    """Address of a numpy array, a CUDA tensor, or an int device pointer."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if isinstance(x, np.ndarray):
+        assert x.flags["C_CONTIGUOUS"]
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        assert x.is_contiguous()
+        return x.data_ptr()
+    raise TypeError(type(x))
+
+
+def _check(rc: int, what: str):
+    if rc != OK:
+        raise TmvpError(rc, what)
+
+
+def _u8(x, shape=None) -> np.ndarray:
+    a = np.ascontiguousarray(np.frombuffer(bytes(x), np.uint8) if isinstance(x, (bytes, bytearray))
+                             else x)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+class Context:
+    """A libtmvpkem context on one GPU (tmvp_ctx)."""
+
+    def __init__(self, device: int = 0, mem_budget: int = 0):
+        h = ctypes.c_void_p()
+        _check(lib().tmvp_ctx_create(device, mem_budget, ctypes.byref(h)), "tmvp_ctx_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().tmvp_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def workspace_bytes(self) -> int:
+        return lib().tmvp_ctx_workspace_bytes(self.h)
+
+    @property
+    def launches(self) -> int:
+        return lib().tmvp_ctx_launch_count(self.h)
+
+    def set_timing(self, enable: bool):
+        _check(lib().tmvp_ctx_set_timing(self.h, int(enable)), "tmvp_ctx_set_timing")
+
+    def stage_stats(self) -> dict:
+        """{kernel name: (launches, total device ms)} since timing was enabled."""
+        L = lib()
+        n = L.tmvp_ctx_stage_stats(self.h, -1, None, 0, None, None)
+        out = {}
+        for i in range(n):
+            name = ctypes.create_string_buffer(64)
+            la = ctypes.c_uint64()
+            ms = ctypes.c_double()
+            _check(L.tmvp_ctx_stage_stats(self.h, i, name, 64, ctypes.byref(la), ctypes.byref(ms)),
+                   "tmvp_ctx_stage_stats")
+            out[name.value.decode()] = (la.value, ms.value)
+        return out
+
+    # --- pointer-level calls (host or device buffers, caller-owned) --------
+    def kem_keypair_ptr(self, set_id, n, pk, sk, coins, form=FORM_AUTO, stream=None):
+        _check(lib().tmvp_kem_keypair_batch(self.h, set_id, n, _ptr(pk), _ptr(sk), _ptr(coins),
+                                            form, stream), "tmvp_kem_keypair_batch")
+
+    def kem_enc_ptr(self, set_id, n, ct, ss, pk, coins, form=FORM_AUTO, stream=None):
+        _check(lib().tmvp_kem_enc_batch(self.h, set_id, n, _ptr(ct), _ptr(ss), _ptr(pk),
+                                        _ptr(coins), form, stream), "tmvp_kem_enc_batch")
+
+    def kem_dec_ptr(self, set_id, n, ss, ct, sk, form=FORM_AUTO, stream=None):
+        _check(lib().tmvp_kem_dec_batch(self.h, set_id, n, _ptr(ss), _ptr(ct), _ptr(sk), form,
+                                        stream), "tmvp_kem_dec_batch")
+
+    def matvec_ptr(self, n, l, eq, transpose, out, A, s, form=FORM_AUTO, stream=None):
+        _check(lib().tmvp_matvec_batch(self.h, n, l, eq, int(transpose), _ptr(out), _ptr(A),
+                                       _ptr(s), form, stream), "tmvp_matvec_batch")
+
+    # --- numpy conveniences (host buffers) ---------------------------------
+    def kem_keypair(self, set_id, coins, form=FORM_AUTO):
+        z = sizes(set_id)
+        coins = _u8(coins).reshape(-1, 96)
+        n = coins.shape[0]
+        pk = np.zeros((n, z.pk_bytes), np.uint8)
+        sk = np.zeros((n, z.sk_bytes), np.uint8)
+        self.kem_keypair_ptr(set_id, n, pk, sk, coins, form)
+        return pk, sk
+
+    def kem_enc(self, set_id, pk, coins, form=FORM_AUTO):
+        z = sizes(set_id)
+        pk = _u8(pk).reshape(-1, z.pk_bytes)
+        coins = _u8(coins).reshape(-1, 32)
+        n = pk.shape[0]
+        ct = np.zeros((n, z.ct_bytes), np.uint8)
+        ss = np.zeros((n, 32), np.uint8)
+        self.kem_enc_ptr(set_id, n, ct, ss, pk, coins, form)
+        return ct, ss
+
+    def kem_dec(self, set_id, ct, sk, form=FORM_AUTO):
+        z = sizes(set_id)
+        ct = _u8(ct).reshape(-1, z.ct_bytes)
+        sk = _u8(sk).reshape(-1, z.sk_bytes)
+        n = ct.shape[0]
+        ss = np.zeros((n, 32), np.uint8)
+        self.kem_dec_ptr(set_id, n, ss, ct, sk, form)
+        return ss
+
+    def indcpa_keypair(self, set_id, seeds, form=FORM_AUTO):
+        z = sizes(set_id)
+        seeds = _u8(seeds).reshape(-1, 64)
+        n = seeds.shape[0]
+        pk = np.zeros((n, z.pk_bytes), np.uint8)
+        sk = np.zeros((n, z.indcpa_sk_bytes), np.uint8)
+        _check(lib().tmvp_indcpa_keypair_batch(self.h, set_id, n, _ptr(pk), _ptr(sk), _ptr(seeds),
+                                               form, None), "tmvp_indcpa_keypair_batch")
+        return pk, sk
+
+    def indcpa_enc(self, set_id, m, noiseseed, pk, form=FORM_AUTO):
+        z = sizes(set_id)
+        m = _u8(m).reshape(-1, 32)
+        ns = _u8(noiseseed).reshape(-1, 32)
+        pk = _u8(pk).reshape(-1, z.pk_bytes)
+        n = m.shape[0]
+        ct = np.zeros((n, z.ct_bytes), np.uint8)
+        _check(lib().tmvp_indcpa_enc_batch(self.h, set_id, n, _ptr(ct), _ptr(m), _ptr(ns), _ptr(pk),
+                                           form, None), "tmvp_indcpa_enc_batch")
+        return ct
+
+    def indcpa_dec(self, set_id, sk, ct, form=FORM_AUTO):
+        z = sizes(set_id)
+        sk = _u8(sk).reshape(-1, z.indcpa_sk_bytes)
+        ct = _u8(ct).reshape(-1, z.ct_bytes)
+        n = ct.shape[0]
+        m = np.zeros((n, 32), np.uint8)
+        _check(lib().tmvp_indcpa_dec_batch(self.h, set_id, n, _ptr(m), _ptr(sk), _ptr(ct), form,
+                                           None), "tmvp_indcpa_dec_batch")
+        return m
+
+    def matvec(self, A, s, eq=13, transpose=False, form=FORM_AUTO):
+        A = np.ascontiguousarray(A, dtype=np.uint16)
+        s = np.ascontiguousarray(s, dtype=np.int8)
+        n, l = A.shape[0], A.shape[1]
+        out = np.zeros((n, l, 256), np.uint16)
+        self.matvec_ptr(n, l, eq, transpose, out, A, s, form)
+        return out
+
+
+def splitmix_bytes(seed: int, n: int) -> np.ndarray:
+    """Deterministic seed bytes: SplitMix64 stream, little-endian words."""
+    nw = (n + 7) // 8
+    x = (np.uint64(seed & 0xFFFFFFFFFFFFFFFF) +
+         np.arange(1, nw + 1, dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15))
+    with np.errstate(over="ignore"):
+        z = x
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return z.astype("<u8").view(np.uint8)[:n].copy()

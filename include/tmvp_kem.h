@@ -1,0 +1,172 @@
+/*
+ * tmvp_kem.h — C ABI of libtmvpkem: batched Saber/Sable KEM on one GB300 GPU.
+ *
+ * The entry points replace the reference's host API and keep its byte
+ * layouts:
+ *   - saber_enc / saber_dec        TMVP-Saber/SABER-GPU/include/cuda_kernel.cuh:6-7
+ *                                  (bodies: TMVP-Saber/SABER-GPU/src/cuda_kernel.cu:25-479)
+ *   - SABLE_enc / SABLE_dec        TMVP_SABLE/include/SABLE_indcpa.cuh:8-10
+ *                                  (bodies: TMVP_SABLE/src/SABLE_indcpa.cu:24-610)
+ *   - crypto_kem_keypair/enc/dec and indcpa_kem_keypair/enc/dec: the Saber
+ *     reference C API whose byte layouts the reference's kernels implement
+ *     (pk = pack_p(b) || seed_A; sk = pack(s) || pk || H(pk) || z;
+ *      ct = pack_p(b') || pack_T(c_m); all little-endian bit streams).
+ *   - tmvp_kem_*_batch: derandomised batched forms of the same operations;
+ *     the reference's equivalent is its BATCH-wide launch sequence
+ *     (saber_enc / saber_dec above).
+ *   - tmvp_matvec_batch: the MatrixVectorMul step on its own
+ *     (TMVP-Saber/SABER-GPU/src/poly.cu:269-376 schoolbook,
+ *      :1396-1453 TMVP on CUDA cores, :1455-1500 TMVP on tensor cores).
+ *
+ * Conventions: caller-owned buffers, contiguous [n][bytes]; a buffer may be
+ * host memory (pageable or pinned) or device memory of the context's GPU.
+ * Calls return TMVP_OK or a negative TMVP_E* code; no exception crosses the
+ * ABI.  A context is safe to share between host threads (calls on one
+ * context are serialised).  The reference's void shims report their status
+ * through tmvp_last_error().
+ */
+#ifndef TMVP_KEM_H
+#define TMVP_KEM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Parameter sets.  Saber family: TMVP-Saber/SABER-GPU/include/params.h:1-50
+ * (L = 2, 3, 4).  Sable family: TMVP_SABLE/include/SABLE_params.h:1-73
+ * (Saber_type 1, 2, 3). */
+typedef enum {
+  TMVP_LIGHTSABER = 0,
+  TMVP_SABER = 1,
+  TMVP_FIRESABER = 2,
+  TMVP_LIGHTSABLE = 3,
+  TMVP_SABLE = 4,
+  TMVP_FIRESABLE = 5
+} tmvp_param_set;
+
+/* Polynomial-multiplication form (the reference's `mode` argument,
+ * TMVP-Saber/SABER-GPU/main.cu:25-33, cuda_kernel.cu:140-163):
+ *   CUDA_CORE   TMVP on CUDA cores (reference mode 1)
+ *   INT8_TC     TMVP on INT8 tensor cores: s8 secrets x u8 limbs, s32 accumulate
+ *   FP8_TC      TMVP on FP8 tensor cores: e4m3 secrets x balanced radix-32
+ *               digits, f32 accumulate; every partial sum is an integer below
+ *               2^24, so the result is exact
+ *   AUTO        the fastest exact tensor-core form on this GPU (FP8_TC)
+ *   SCHOOLBOOK  plain negacyclic schoolbook on CUDA cores (reference mode 2) */
+typedef enum {
+  TMVP_FORM_CUDA_CORE = 0,
+  TMVP_FORM_INT8_TC = 1,
+  TMVP_FORM_FP8_TC = 2,
+  TMVP_FORM_AUTO = 3,
+  TMVP_FORM_SCHOOLBOOK = 4
+} tmvp_form;
+
+enum {
+  TMVP_OK = 0,
+  TMVP_EINVAL = -1,   /* bad argument (null pointer, unknown set/form, n too large) */
+  TMVP_ENOMEM = -2,   /* device workspace does not fit the context's memory budget */
+  TMVP_EDEVICE = -3,  /* CUDA runtime error                                         */
+  TMVP_ETIMEOUT = -4, /* a bounded device-side wait gave up                         */
+  TMVP_ENOTSUP = -5   /* no usable GPU / unsupported architecture                  */
+};
+
+typedef struct {
+  int l, eq, ep, et, mu;
+  size_t pk_bytes, sk_bytes, ct_bytes, ss_bytes;
+  size_t indcpa_pk_bytes, indcpa_sk_bytes;
+} tmvp_sizes;
+
+typedef struct tmvp_ctx tmvp_ctx;
+
+/* Sizes of a parameter set. */
+int tmvp_param_sizes(tmvp_param_set set, tmvp_sizes *out);
+const char *tmvp_strerror(int code);
+/* Status of the last call on this host thread (for the void shims). */
+int tmvp_last_error(void);
+
+/* Context: owns device workspace on `device`.  mem_budget caps the workspace
+ * in bytes (0 = no cap).  Workspace grows on demand up to the cap. */
+int tmvp_ctx_create(int device, size_t mem_budget, tmvp_ctx **out);
+void tmvp_ctx_destroy(tmvp_ctx *ctx);
+/* Device bytes of workspace the context holds now. */
+size_t tmvp_ctx_workspace_bytes(const tmvp_ctx *ctx);
+/* Number of kernel launches the context issued since creation. */
+uint64_t tmvp_ctx_launch_count(const tmvp_ctx *ctx);
+/* Per-stage timing (profiling aid; no counterpart in the reference, which
+ * brackets whole operations with cudaEvent pairs, cuda_kernel.cu:114-188).
+ * When enabled, every kernel launch is bracketed by CUDA events on its own
+ * stream.  tmvp_ctx_stage_stats(ctx, -1, ...) returns the number of stages;
+ * for idx >= 0 it fills the stage's kernel name, launch count and summed
+ * device milliseconds (it waits for pending launches).  Disabling clears the
+ * statistics. */
+int tmvp_ctx_set_timing(tmvp_ctx *ctx, int enable);
+int tmvp_ctx_stage_stats(tmvp_ctx *ctx, int idx, char *name, size_t name_len,
+                         uint64_t *launches, double *total_ms);
+
+/* Batched, derandomised KEM.  stream: a cudaStream_t (NULL = legacy default).
+ * keypair coins per instance: seed_A(32) | seed_s(32) | z(32).
+ * enc coins per instance: 32 bytes (hashed into the message, as saber_enc
+ * does with its 32 random bytes, cuda_kernel.cu:116).
+ * The calls are asynchronous with respect to the host only when every buffer
+ * is device memory; with host buffers they return after the results are in
+ * host memory. */
+int tmvp_kem_keypair_batch(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *pk,
+                           uint8_t *sk, const uint8_t *coins, tmvp_form form, void *stream);
+int tmvp_kem_enc_batch(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *ct, uint8_t *ss,
+                       const uint8_t *pk, const uint8_t *coins, tmvp_form form, void *stream);
+int tmvp_kem_dec_batch(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *ss,
+                       const uint8_t *ct, const uint8_t *sk, tmvp_form form, void *stream);
+
+/* Batched IND-CPA (indcpa_kem_* of the Saber reference API, n instances). */
+int tmvp_indcpa_keypair_batch(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *pk,
+                              uint8_t *sk, const uint8_t *seeds /*[n][64]: seed_A|seed_s*/,
+                              tmvp_form form, void *stream);
+int tmvp_indcpa_enc_batch(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *ct,
+                          const uint8_t *m /*[n][32]*/, const uint8_t *noiseseed /*[n][32]*/,
+                          const uint8_t *pk, tmvp_form form, void *stream);
+int tmvp_indcpa_dec_batch(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *m,
+                          const uint8_t *sk, const uint8_t *ct, tmvp_form form, void *stream);
+
+/* MatrixVectorMul alone: out[i] = sum_j A[i][j] * s[j] mod 2^eq
+ * (transpose: A[j][i]); A uint16 [n][l][l][256] (values < 2^eq), s int8
+ * [n][l][256] with |s| <= 8, out uint16 [n][l][256].  l in 2..4, eq <= 13. */
+int tmvp_matvec_batch(tmvp_ctx *ctx, size_t n, int l, int eq, int transpose, uint16_t *out,
+                      const uint16_t *A, const int8_t *s, tmvp_form form, void *stream);
+
+/* NIST-style single-instance API for the default parameter set (Saber unless
+ * changed).  Randomness comes from the randombytes hook (default: the
+ * operating system's getrandom).  Return 0 on success. */
+int crypto_kem_keypair(uint8_t *pk, uint8_t *sk);
+int crypto_kem_enc(uint8_t *ct, uint8_t *ss, const uint8_t *pk);
+int crypto_kem_dec(uint8_t *ss, const uint8_t *ct, const uint8_t *sk);
+int indcpa_kem_keypair(uint8_t *pk, uint8_t *sk);
+int indcpa_kem_enc(const uint8_t m[32], const uint8_t seed_sp[32], const uint8_t *pk,
+                   uint8_t *ciphertext);
+int indcpa_kem_dec(const uint8_t *sk, const uint8_t *ciphertext, uint8_t m[32]);
+typedef void (*tmvp_randombytes_fn)(uint8_t *out, size_t len);
+void tmvp_set_randombytes(tmvp_randombytes_fn fn);
+int tmvp_set_default_param_set(tmvp_param_set set);
+
+/* Reference-compatible shims.  mode: 0 = tensor cores (AUTO), 1 = CUDA-core
+ * TMVP, other = schoolbook, as in the reference.  They process
+ * tmvp_ref_batch(scheme) instances (defaults: Saber 1 and Sable 512, the
+ * reference's BATCH values, cuda_kernel.cuh:1 and SABLE_indcpa.cuh:6) over
+ * contiguous [batch][bytes] host arrays.  Unlike the reference they do not
+ * overwrite h_pk / h_sk with built-in test vectors: the caller's keys are
+ * used, and the 32 random bytes per encapsulation come from the randombytes
+ * hook.  h_pk is unused by the decapsulation shims (sk embeds pk). */
+void saber_enc(uint8_t mode, uint8_t *h_k, uint8_t *h_pk, uint8_t *h_c);
+void saber_dec(uint8_t mode, uint8_t *h_c, uint8_t *h_pk, uint8_t *h_sk, uint8_t *h_k);
+void SABLE_enc(uint8_t *h_k, uint8_t *h_pk, uint8_t *h_c, int mode);
+void SABLE_dec(uint8_t *h_c, uint8_t *h_pk, uint8_t *h_sk, uint8_t *h_k, int mode);
+/* scheme: 0 = Saber shims, 1 = Sable shims. */
+int tmvp_ref_set_batch(int scheme, size_t n);
+size_t tmvp_ref_batch(int scheme);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TMVP_KEM_H */

@@ -1,0 +1,54 @@
+"""C ABI checks that need no GPU: the library loads, exports every entry point
+include/tmvp_kem.h declares, and agrees with the oracle on sizes."""
+import ctypes
+import subprocess
+
+import pytest
+
+
+@pytest.fixture(scope="module")
+def T():
+    import tmvpkem
+    tmvpkem.build.build()
+    return tmvpkem
+
+
+def test_exports_every_declared_symbol(T):
+    names = T.exported_symbols()
+    assert len(names) >= 25
+    L = T.lib()
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", T.LIB_PATH], capture_output=True, text=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    assert set(names) <= exported
+
+
+def test_param_sizes_match_oracle(T, oracle):
+    for s in range(6):
+        z, p = T.sizes(s), oracle.params(s)
+        assert (z.l, z.eq, z.ep, z.et, z.mu) == (p.l, p.eq, p.ep, p.et, p.mu)
+        assert (z.pk_bytes, z.sk_bytes, z.ct_bytes, z.indcpa_sk_bytes) == (
+            p.pk_bytes, p.sk_bytes, p.ct_bytes, p.indcpa_sk_bytes)
+    # Saber l=3 byte layout of the reference (params.h:32-48)
+    z = T.sizes(T.SABER)
+    assert (z.pk_bytes, z.sk_bytes, z.ct_bytes) == (992, 2304, 1088)
+    z = T.sizes(T.SABLE)
+    assert (z.pk_bytes, z.sk_bytes, z.ct_bytes) == (896, 1152, 1024)
+
+
+def test_invalid_arguments(T):
+    s = T.Sizes()
+    assert T.lib().tmvp_param_sizes(17, ctypes.byref(s)) == T.EINVAL
+    assert T.lib().tmvp_kem_dec_batch(None, 1, 1, None, None, None, 0, None) == T.EINVAL
+    assert T.lib().tmvp_strerror(T.ENOMEM).decode().startswith("device workspace")
+    assert T.lib().tmvp_ref_batch(0) == 1 and T.lib().tmvp_ref_batch(1) == 512
+
+
+def test_context_without_gpu_is_refused(T):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    assert T.lib().tmvp_ctx_create(0, 0, ctypes.byref(h)) == T.ENOTSUP
+    assert T.lib().crypto_kem_keypair(None, None) == T.ENOTSUP

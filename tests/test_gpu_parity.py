@@ -1,0 +1,221 @@
+"""CUDA library vs the oracle, bit-exact, through the C ABI (needs a GB300)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+ALL_FORMS = [0, 1, 2, 4]  # cuda_core, int8_tc, fp8_tc, schoolbook
+SETS = range(6)
+
+
+def _coins(seed, n, w):
+    import tmvpkem
+    return tmvpkem.splitmix_bytes(seed, n * w).reshape(n, w)
+
+
+@pytest.mark.parametrize("form", ALL_FORMS)
+@pytest.mark.parametrize("l,eq,transpose", [(2, 13, 0), (3, 13, 0), (3, 13, 1), (4, 13, 0),
+                                             (3, 11, 0), (4, 11, 1), (2, 10, 0)])
+def test_matvec_random(kem, oracle, form, l, eq, transpose):
+    T, ctx = kem
+    rng = np.random.default_rng(l * 100 + eq + transpose)
+    n = 40
+    A = rng.integers(0, 1 << eq, (n, l, l, 256), dtype=np.uint16)
+    s = rng.integers(-5, 6, (n, l, 256)).astype(np.int8)
+    got = ctx.matvec(A, s, eq=eq, transpose=bool(transpose), form=form)
+    want = oracle.matvec(A, s, eq=eq, transpose=bool(transpose), nthreads=4)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("form", ALL_FORMS)
+def test_matvec_extremes(kem, oracle, form):
+    """Largest exact inputs: |s| = 8 everywhere and public values at the digit
+    boundaries, so every tensor-core accumulator reaches its bound."""
+    T, ctx = kem
+    n, l, eq = 12, 4, 13
+    vals = np.array([0, 1, 15, 16, 17, 31, 32, 511, 512, 4095, 4096, 4097, 8176, 8191], np.uint16)
+    rng = np.random.default_rng(5)
+    A = vals[rng.integers(0, len(vals), (n, l, l, 256))]
+    s = np.where(rng.integers(0, 2, (n, l, 256)) == 1, 8, -8).astype(np.int8)
+    A[0] = 4096
+    s[0] = -8
+    A[1] = 8191
+    s[1] = 8
+    got = ctx.matvec(A, s, eq=eq, form=form)
+    assert np.array_equal(got, oracle.matvec(A, s, eq=eq, nthreads=4))
+
+
+@pytest.mark.parametrize("form", ALL_FORMS)
+def test_matvec_golden(kem, form):
+    T, ctx = kem
+    g = golden("matvec.npz")
+    for scheme, eq in (("saber", 13), ("sable", 11)):
+        out = ctx.matvec(g[f"{scheme}_A"], g[f"{scheme}_s"], eq=eq, form=form)
+        assert np.array_equal(out, g[f"{scheme}_out"])
+
+
+@pytest.mark.parametrize("form", ALL_FORMS)
+@pytest.mark.parametrize("set_id", SETS)
+def test_kem_parity(kem, oracle, set_id, form):
+    T, ctx = kem
+    n = 24
+    kc = _coins(1000 + set_id, n, 96)
+    pk, sk = ctx.kem_keypair(set_id, kc, form=form)
+    opk, osk = oracle.kem_keypair_batch(set_id, kc, nthreads=4)
+    assert np.array_equal(pk, opk) and np.array_equal(sk, osk)
+    ec = _coins(2000 + set_id, n, 32)
+    ct, ss = ctx.kem_enc(set_id, pk, ec, form=form)
+    oct_, oss = oracle.kem_enc_batch(set_id, opk, ec, nthreads=4)
+    assert np.array_equal(ct, oct_) and np.array_equal(ss, oss)
+    ss2 = ctx.kem_dec(set_id, ct, sk, form=form)
+    assert np.array_equal(ss2, ss)
+    # tampered ciphertexts: implicit rejection, same key as the oracle
+    bad = ct.copy()
+    rng = np.random.default_rng(set_id)
+    for i in range(n):
+        if i % 2 == 0:
+            bad[i, rng.integers(0, bad.shape[1])] ^= np.uint8(1 << rng.integers(0, 8))
+    ss3 = ctx.kem_dec(set_id, bad, sk, form=form)
+    oss3, fail = oracle.kem_dec_batch(set_id, bad, osk, nthreads=4)
+    assert np.array_equal(ss3, oss3)
+    assert fail[::2].all() and not fail[1::2].any()
+    assert (ss3[::2] != ss[::2]).any(axis=1).all()
+
+
+@pytest.mark.parametrize("form", ALL_FORMS)
+@pytest.mark.parametrize("name,set_id", [("saber_l3.npz", 1), ("sable_l3.npz", 4)])
+def test_reference_golden(kem, name, set_id, form):
+    """Test vectors and seeded instances produced by the reference's own kernels."""
+    T, ctx = kem
+    g = golden(name)
+    ct, ss = ctx.kem_enc(set_id, g["tv_pk"], g["tv_buf"][:32], form=form)
+    assert ct[0].tobytes() == g["tv_ct"].tobytes() and ss[0].tobytes() == g["tv_ss"].tobytes()
+    assert ctx.kem_dec(set_id, ct, g["tv_sk"], form=form)[0].tobytes() == g["tv_ss"].tobytes()
+    ct, ss = ctx.kem_enc(set_id, g["rnd_pk"], g["rnd_coins"], form=form)
+    assert np.array_equal(ct, g["rnd_ct"]) and np.array_equal(ss, g["rnd_ss"])
+    assert np.array_equal(ctx.kem_dec(set_id, g["rnd_ct"], g["rnd_sk"], form=form), g["rnd_ss"])
+    rej = ctx.kem_dec(set_id, g["rej_ct"], g["rnd_sk"][0], form=form)
+    assert rej[0].tobytes() == g["rej_ss"].tobytes()
+
+
+@pytest.mark.parametrize("form", [0, 2])
+@pytest.mark.parametrize("set_id", [1, 4])
+def test_indcpa_parity(kem, oracle, set_id, form):
+    T, ctx = kem
+    n = 8
+    seeds = _coins(77, n, 64)
+    pk, sk = ctx.indcpa_keypair(set_id, seeds, form=form)
+    for i in range(n):
+        opk, osk = oracle.indcpa_keypair(set_id, seeds[i, :32], seeds[i, 32:])
+        assert pk[i].tobytes() == opk and sk[i].tobytes() == osk
+    m = _coins(78, n, 32)
+    ns = _coins(79, n, 32)
+    ct = ctx.indcpa_enc(set_id, m, ns, pk, form=form)
+    for i in range(n):
+        assert ct[i].tobytes() == oracle.indcpa_enc(set_id, m[i], ns[i], pk[i])
+    m2 = ctx.indcpa_dec(set_id, sk, ct, form=form)
+    assert np.array_equal(m2, m)
+
+
+def test_nist_api_and_randombytes_hook(kem, oracle):
+    T, ctx = kem
+    L = T.lib()
+    z = T.sizes(T.SABER)
+    state = {"ctr": 0}
+
+    @T.RANDOMBYTES_FN
+    def rb(buf, n):
+        data = T.splitmix_bytes(4242 + state["ctr"], n)
+        state["ctr"] += 1
+        ctypes.memmove(buf, data.ctypes.data, n)
+
+    L.tmvp_set_randombytes(ctypes.cast(rb, ctypes.c_void_p))
+    try:
+        pk = np.zeros(z.pk_bytes, np.uint8)
+        sk = np.zeros(z.sk_bytes, np.uint8)
+        assert L.crypto_kem_keypair(pk.ctypes.data, sk.ctypes.data) == 0
+        opk, osk = oracle.kem_keypair(T.SABER, T.splitmix_bytes(4242, 96))
+        assert pk.tobytes() == opk and sk.tobytes() == osk
+        ct = np.zeros(z.ct_bytes, np.uint8)
+        ss = np.zeros(32, np.uint8)
+        assert L.crypto_kem_enc(ct.ctypes.data, ss.ctypes.data, pk.ctypes.data) == 0
+        oct_, oss = oracle.kem_enc(T.SABER, opk, T.splitmix_bytes(4243, 32))
+        assert ct.tobytes() == oct_ and ss.tobytes() == oss
+        ss2 = np.zeros(32, np.uint8)
+        assert L.crypto_kem_dec(ss2.ctypes.data, ct.ctypes.data, sk.ctypes.data) == 0
+        assert ss2.tobytes() == oss
+        # indcpa single-instance API
+        ipk = np.zeros(z.pk_bytes, np.uint8)
+        isk = np.zeros(z.indcpa_sk_bytes, np.uint8)
+        assert L.indcpa_kem_keypair(ipk.ctypes.data, isk.ctypes.data) == 0
+        m = T.splitmix_bytes(1, 32)
+        seed = T.splitmix_bytes(2, 32)
+        c = np.zeros(z.ct_bytes, np.uint8)
+        assert L.indcpa_kem_enc(m.ctypes.data, seed.ctypes.data, ipk.ctypes.data, c.ctypes.data) == 0
+        m2 = np.zeros(32, np.uint8)
+        assert L.indcpa_kem_dec(isk.ctypes.data, c.ctypes.data, m2.ctypes.data) == 0
+        assert np.array_equal(m, m2)
+    finally:
+        L.tmvp_set_randombytes(None)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_reference_shims(kem, oracle, mode):
+    """saber_enc/saber_dec and SABLE_enc/SABLE_dec with the reference's calling convention."""
+    T, ctx = kem
+    L = T.lib()
+    for scheme, set_id, B in ((0, T.SABER, 3), (1, T.SABLE, 5)):
+        assert L.tmvp_ref_set_batch(scheme, B) == 0
+        z = T.sizes(set_id)
+        pk, sk = ctx.kem_keypair(set_id, _coins(9 + scheme, B, 96))
+        h_c = np.zeros((B, z.ct_bytes), np.uint8)
+        h_k = np.zeros((B, 32), np.uint8)
+        h_k2 = np.zeros((B, 32), np.uint8)
+        if scheme == 0:
+            L.saber_enc(mode, h_k.ctypes.data, pk.ctypes.data, h_c.ctypes.data)
+            assert L.tmvp_last_error() == 0
+            L.saber_dec(mode, h_c.ctypes.data, pk.ctypes.data, sk.ctypes.data, h_k2.ctypes.data)
+        else:
+            L.SABLE_enc(h_k.ctypes.data, pk.ctypes.data, h_c.ctypes.data, mode)
+            assert L.tmvp_last_error() == 0
+            L.SABLE_dec(h_c.ctypes.data, pk.ctypes.data, sk.ctypes.data, h_k2.ctypes.data, mode)
+        assert L.tmvp_last_error() == 0
+        assert np.array_equal(h_k, h_k2) and h_k.any()
+        oss, fail = oracle.kem_dec_batch(set_id, h_c, sk)
+        assert np.array_equal(oss, h_k) and not fail.any()
+    L.tmvp_ref_set_batch(0, 1)
+    L.tmvp_ref_set_batch(1, 512)
+
+
+def test_empty_and_unaligned_buffers(kem, oracle):
+    T, ctx = kem
+    z = T.sizes(T.SABER)
+    # n = 0 is a no-op
+    ctx.kem_dec_ptr(T.SABER, 0, None, None, None)
+    # host buffers at odd offsets are staged, not read misaligned
+    n = 5
+    pk, sk = ctx.kem_keypair(T.SABER, _coins(31, n, 96))
+    raw = np.zeros(n * z.ct_bytes + 3, np.uint8)
+    ct_view = raw[3:]
+    ssb = np.zeros(n * 32 + 1, np.uint8)
+    ctx.kem_enc_ptr(T.SABER, n, ct_view, ssb[1:], pk, _coins(32, n, 32))
+    oct_, oss = oracle.kem_enc_batch(T.SABER, pk, _coins(32, n, 32))
+    assert np.array_equal(ct_view.reshape(n, -1), oct_) and np.array_equal(ssb[1:].reshape(n, -1), oss)
+
+
+def test_out_of_range_secret_is_reported(kem):
+    """The tensor-core forms refuse secrets outside their exact range."""
+    T, ctx = kem
+    A = np.zeros((2, 3, 3, 256), np.uint16)
+    s = np.zeros((2, 3, 256), np.int8)
+    s[1, 0, 7] = 100
+    with pytest.raises(T.TmvpError) as e:
+        ctx.matvec(A, s, eq=13, form=T.FORM_FP8_TC)
+    assert e.value.code == T.EINVAL
+    # the CUDA-core form computes it exactly
+    out = ctx.matvec(A, s, eq=13, form=T.FORM_CUDA_CORE)
+    assert not out.any()
