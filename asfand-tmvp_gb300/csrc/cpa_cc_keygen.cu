@@ -1,0 +1,8 @@
+// cpa_cc_keygen.cu — instantiates the IND-CPA kernel for form kCudaCore, op kKeygen
+// (template in cpa_impl.cuh; one translation unit per pair so that they
+// compile in parallel).
+#include "cpa_impl.cuh"
+
+namespace tmvp {
+int cpa_launch_cc_keygen(const CpaArgs &a, cudaStream_t s) { return launch_op<kCudaCore, kKeygen>(a, s); }
+}  // namespace tmvp

@@ -18,16 +18,19 @@
 
 #include "cpa_engine.cuh"
 #include "cpa_kernels.cuh"
+#include "cpa_tc.cuh"
+#include "cpa_tc_kernel.cuh"
 
 namespace tmvp {
 
-template <int FORM, int OP, int L>
+template <int FORM, int OP, int L, int Q_ = 1>
 struct CpaCfg {
   static constexpr int R = OP == kDecrypt ? 1 : ((OP == kEncrypt || OP == kReenc) ? L + 1 : L);
+  // public polys of width eq (A, or the matvec input); the rest are p-bit (b, b')
+  static constexpr int RA = OP == kDecrypt ? 0 : L;
   static constexpr bool TC = FORM == kInt8TC || FORM == kFp8TC;
-  static constexpr int D = (FORM == kFp8TC && OP != kDecrypt) ? 3 : 2;
-  static constexpr int Q = tc_ntiles<D>(R);
-  static constexpr int WARPS = Q >= 3 ? 4 : 2;
+  static constexpr int Q = Q_;
+  static constexpr int WARPS = 4;
   static constexpr int RP = R <= 4 ? 4 : 8;
   static constexpr bool TMVP = FORM == kCudaCore;
   static constexpr int NPROD = TMVP ? 3 : 1;
@@ -44,9 +47,9 @@ __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
 // Shared-memory layout of one CTA.  eng holds the engine operands (TC: digit
 // columns then Toeplitz copies; CC: Toeplitz sequences, vectors, products).
-template <int FORM, int OP, int L>
+template <int FORM, int OP, int L, int Q = 1>
 __host__ __device__ inline CpaLayout cpa_layout(const KemParams &P) {
-  using C = CpaCfg<FORM, OP, L>;
+  using C = CpaCfg<FORM, OP, L, Q>;
   CpaLayout o;
   int off = 0;
   auto take = [&](int bytes) { int r = off; off = align16(off + bytes + 16); return r; };
@@ -65,6 +68,7 @@ __host__ __device__ inline CpaLayout cpa_layout(const KemParams &P) {
   int eng;
   if (C::TC) {
     eng = L * C::Q * 8 * kColStride + L * kTzBytesPerPoly;
+    if (C::Q * 8 * 256 * 4 > eng) eng = C::Q * 8 * 256 * 4;  // int32 accumulators alias it
   } else {
     eng = L * C::NPROD * 512 * 2 + L * C::NPROD * C::NCOL * C::RP * 2 +
           (C::TMVP ? 3 * C::RP * 128 * 4 : 0);
@@ -73,12 +77,6 @@ __host__ __device__ inline CpaLayout cpa_layout(const KemParams &P) {
   o.res = take(C::R * 256 * 2);
   o.total = off;
   return o;
-}
-
-__device__ __forceinline__ void copy16(uint8_t *dst, const uint8_t *src, int nbytes) {
-  const uint4 *s = reinterpret_cast<const uint4 *>(src);
-  uint4 *d = reinterpret_cast<uint4 *>(dst);
-  for (int i = threadIdx.x; i < (nbytes >> 4); i += blockDim.x) d[i] = s[i];
 }
 
 // Byte `ob` of the little-endian w-bit stream of values f(k).
@@ -95,13 +93,13 @@ __device__ __forceinline__ uint8_t pack_byte(int ob, int w, F f) {
   return (uint8_t)acc;
 }
 
-template <int FORM, int OP, int L>
-__global__ void __launch_bounds__(CpaCfg<FORM, OP, L>::NT) k_cpa(CpaArgs a) {
-  using C = CpaCfg<FORM, OP, L>;
+template <int FORM, int OP, int L, int Q>
+__global__ void __launch_bounds__(CpaCfg<FORM, OP, L, Q>::NT) k_cpa(CpaArgs a) {
+  using C = CpaCfg<FORM, OP, L, Q>;
   extern __shared__ __align__(16) uint8_t sm[];
   const KemParams &P = a.P;
   const size_t inst = blockIdx.x;
-  const CpaLayout lo = cpa_layout<FORM, OP, L>(P);
+  const CpaLayout lo = cpa_layout<FORM, OP, L, Q>(P);
   const int tid = threadIdx.x;
 
   // 1. packed inputs to shared memory
@@ -165,42 +163,52 @@ __global__ void __launch_bounds__(CpaCfg<FORM, OP, L>::NT) k_cpa(CpaArgs a) {
   if (C::TC) {
     uint32_t *colw = reinterpret_cast<uint32_t *>(sm + lo.eng);
     uint32_t *tz = colw + L * C::Q * 8 * (kColStride / 4);
-    // zero padding columns
-    for (int idx = tid; idx < L * C::Q * 8 * 64; idx += C::NT) {
-      int w = idx & 63, c = (idx >> 6) % (C::Q * 8), j = idx / (64 * C::Q * 8);
-      int poly, digit;
-      tc_slot<C::D>(c >> 3, c & 7, poly, digit);
-      if (poly >= C::R) colw[(j * C::Q * 8 + c) * (kColStride / 4) + w] = 0u;
-    }
-    // digit columns, four coefficients per word
-    for (int idx = tid; idx < C::R * L * 64; idx += C::NT) {
-      int k4 = idx & 63, j = (idx >> 6) % L, r = idx / (64 * L);
-      int dg[4][C::D];
-#pragma unroll
-      for (int e = 0; e < 4; e++) {
-        int w;
-        uint32_t x = pub(r, j, 4 * k4 + e, w);
-        public_digits<FORM, C::D>(x, w, dg[e]);
+    const int wa = OP == kMatvec ? a.mv_eq : P.eq, wb = P.ep;
+    const int Da = tc_digits<FORM>(wa), Db = tc_digits<FORM>(wb);
+    const int c0 = FORM == kFp8TC ? 1 : 0;
+    const int ncols = tc_cols<FORM>(C::R, C::RA, wa, wb);
+    // digit columns: one work item = 8 coefficients of poly p, module index j
+    for (int idx = tid; idx < C::R * L * 32; idx += C::NT) {
+      const int grp = idx & 31, j = (idx >> 5) % L, p = idx / (32 * L);
+      uint32_t X[4];
+      if (OP == kMatvec) {
+        int ij = a.mv_transpose ? (j * L + p) : (p * L + j);
+        uint4 u = *reinterpret_cast<const uint4 *>(a.mv_A + inst * (size_t)(L * L * 256) + ij * 256 + 8 * grp);
+        const uint32_t m = ((1u << wa) - 1u) * 0x10001u;
+        X[0] = u.x & m; X[1] = u.y & m; X[2] = u.z & m; X[3] = u.w & m;
+      } else if (OP == kDecrypt) {
+        unpack8(sm + lo.raw_ct, (32 * j + grp) * wb, wb, X);
+      } else if (p < C::RA) {
+        int ij = (OP == kKeygen) ? (j * L + p) : (p * L + j);
+        unpack8(sm + lo.raw_a, (32 * ij + grp) * wa, wa, X);
+      } else {
+        unpack8(sm + lo.raw_b, (32 * j + grp) * wb, wb, X);
       }
-#pragma unroll
-      for (int d = 0; d < C::D; d++) {
-        int q, c;
-        if (C::D == 2) {
-          q = r >> 2;
-          c = 2 * (r & 3) + d;
-        } else {
-          int s = 3 * (r >> 2) + d;
-          q = s >> 1;
-          c = 2 * (r & 3) + (s & 1);
-        }
-        colw[(j * C::Q * 8 + q * 8 + c) * (kColStride / 4) + k4] =
-            pack4_small<FORM>(dg[0][d], dg[1][d], dg[2][d], dg[3][d]);
-      }
+      const int D = p < C::RA ? Da : Db;
+      const int cb = c0 + (p < C::RA ? p * Da : C::RA * Da + (p - C::RA) * Db);
+      uint2 *dst = reinterpret_cast<uint2 *>(colw + (size_t)(j * C::Q * 8 + cb) * (kColStride / 4) + 2 * grp);
+      for (int d = 0; d < D; d++) dst[d * (kColStride / 8)] = digit8<FORM>(X, d);
     }
     __syncthreads();  // sec complete
-    for (int j = 0; j < L; j++) stage_toeplitz<FORM>(tz + j * 4 * kTzCopyWords, sec + j * 256);
+    for (int j = 0; j < L; j++) stage_toeplitz_v2<FORM>(tz + j * 4 * kTzCopyWords, sec + j * 256, C::NT);
     __syncthreads();
-    tc_engine<FORM, C::D, C::Q, C::WARPS>(tz, colw, L, C::R, res);
+    int *accs = reinterpret_cast<int *>(sm + lo.eng);
+    tc_engine_v2<FORM, C::Q, C::WARPS>(tz, colw, L, ncols, accs);
+    __syncthreads();
+    // combine digit columns: res = sum_d w^d acc_d (- FP8 bias correction)
+    for (int idx = tid; idx < C::R * 256; idx += C::NT) {
+      const int p = idx >> 8, row = idx & 255;
+      const int D = p < C::RA ? Da : Db;
+      const int cb = c0 + (p < C::RA ? p * Da : C::RA * Da + (p - C::RA) * Db);
+      uint32_t v = 0, wgt = 1, wsum = 0;
+      for (int d = 0; d < D; d++) {
+        v += wgt * (uint32_t)accs[(cb + d) * 256 + row];
+        wsum += wgt;
+        wgt <<= (FORM == kFp8TC ? 3 : 8);
+      }
+      if (FORM == kFp8TC) v -= 8u * wsum * (uint32_t)accs[row];
+      res[p * 256 + row] = (uint16_t)v;
+    }
   } else {
     int16_t *tseq = reinterpret_cast<int16_t *>(sm + lo.eng);
     uint16_t *wv = reinterpret_cast<uint16_t *>(tseq + L * C::NPROD * 512);
@@ -307,59 +315,52 @@ __global__ void __launch_bounds__(CpaCfg<FORM, OP, L>::NT) k_cpa(CpaArgs a) {
   }
 }
 
-template <int FORM, int OP, int L>
+template <int FORM, int OP, int L, int Q>
 inline int launch_one(const CpaArgs &a, cudaStream_t s) {
+  if constexpr (FORM == kFp8TC || FORM == kInt8TC) {
+    return launch_tc<FORM, OP, L, Q>(a, s);
+  } else {
+    using C = CpaCfg<FORM, OP, L, Q>;
+    const CpaLayout lo = cpa_layout<FORM, OP, L, Q>(a.P);
+    cudaError_t e = cudaFuncSetAttribute(k_cpa<FORM, OP, L, Q>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, lo.total);
+    if (e != cudaSuccess) return (int)e;
+    k_cpa<FORM, OP, L, Q><<<a.n, C::NT, lo.total, s>>>(a);
+    return (int)cudaGetLastError();
+  }
+}
+
+// n-tiles the tensor-core forms need for (op, l) with the widths of P.
+template <int FORM, int OP, int L>
+inline int tc_q(const CpaArgs &a) {
   using C = CpaCfg<FORM, OP, L>;
-  const CpaLayout lo = cpa_layout<FORM, OP, L>(a.P);
-  cudaError_t e = cudaFuncSetAttribute(k_cpa<FORM, OP, L>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, lo.total);
-  if (e != cudaSuccess) return (int)e;
-  k_cpa<FORM, OP, L><<<a.n, C::NT, lo.total, s>>>(a);
-  return (int)cudaGetLastError();
+  int wa = OP == kMatvec ? a.mv_eq : a.P.eq;
+  return (tc_cols<FORM>(C::R, C::RA, wa, a.P.ep) + 7) / 8;
+}
+
+template <int FORM, int OP, int L>
+inline int launch_q(const CpaArgs &a, cudaStream_t s) {
+  if constexpr (FORM == kCudaCore || FORM == kSchoolbook) {
+    return launch_one<FORM, OP, L, 1>(a, s);
+  } else {
+    switch (tc_q<FORM, OP, L>(a)) {
+      case 1: return launch_one<FORM, OP, L, 1>(a, s);
+      case 2: return launch_one<FORM, OP, L, 2>(a, s);
+      case 3: if constexpr (FORM == kFp8TC) return launch_one<FORM, OP, L, 3>(a, s); break;
+      case 4: if constexpr (FORM == kFp8TC) return launch_one<FORM, OP, L, 4>(a, s); break;
+    }
+    return (int)cudaErrorInvalidValue;
+  }
 }
 
 template <int FORM, int OP>
-inline int launch_l(const CpaArgs &a, cudaStream_t s) {
+inline int launch_op(const CpaArgs &a, cudaStream_t s) {
   switch (a.P.l) {
-    case 2: return launch_one<FORM, OP, 2>(a, s);
-    case 3: return launch_one<FORM, OP, 3>(a, s);
-    case 4: return launch_one<FORM, OP, 4>(a, s);
+    case 2: return launch_q<FORM, OP, 2>(a, s);
+    case 3: return launch_q<FORM, OP, 3>(a, s);
+    case 4: return launch_q<FORM, OP, 4>(a, s);
   }
   return (int)cudaErrorInvalidValue;
-}
-
-template <int FORM>
-inline int launch_form(int op, const CpaArgs &a, cudaStream_t s) {
-  switch (op) {
-    case kDecrypt: return launch_l<FORM, kDecrypt>(a, s);
-    case kEncrypt: return launch_l<FORM, kEncrypt>(a, s);
-    case kReenc: return launch_l<FORM, kReenc>(a, s);
-    case kKeygen: return launch_l<FORM, kKeygen>(a, s);
-    case kMatvec: return launch_l<FORM, kMatvec>(a, s);
-  }
-  return (int)cudaErrorInvalidValue;
-}
-
-template <int FORM, int OP>
-inline size_t smem_l(const KemParams &P) {
-  switch (P.l) {
-    case 2: return cpa_layout<FORM, OP, 2>(P).total;
-    case 3: return cpa_layout<FORM, OP, 3>(P).total;
-    case 4: return cpa_layout<FORM, OP, 4>(P).total;
-  }
-  return 0;
-}
-
-template <int FORM>
-inline size_t smem_form(int op, const KemParams &P) {
-  switch (op) {
-    case kDecrypt: return smem_l<FORM, kDecrypt>(P);
-    case kEncrypt: return smem_l<FORM, kEncrypt>(P);
-    case kReenc: return smem_l<FORM, kReenc>(P);
-    case kKeygen: return smem_l<FORM, kKeygen>(P);
-    case kMatvec: return smem_l<FORM, kMatvec>(P);
-  }
-  return 0;
 }
 
 }  // namespace tmvp

@@ -46,10 +46,6 @@ struct CpaArgs {
   int *err;           // set when a secret coefficient is outside the form's range
 };
 
-// Dynamic shared memory the kernel for (form, op, l) needs with params P.
-size_t cpa_smem_bytes(int form, int op, const KemParams &P);
-// Threads per CTA.
-int cpa_threads(int form, int op, int l);
 // Launch over a.n instances (one CTA each) on `stream`.  Returns a CUDA error
 // code (0 on success).
 int cpa_launch(int form, int op, const CpaArgs &a, void *stream);

@@ -1,0 +1,8 @@
+// cpa_sb_decrypt.cu — instantiates the IND-CPA kernel for form kSchoolbook, op kDecrypt
+// (template in cpa_impl.cuh; one translation unit per pair so that they
+// compile in parallel).
+#include "cpa_impl.cuh"
+
+namespace tmvp {
+int cpa_launch_sb_decrypt(const CpaArgs &a, cudaStream_t s) { return launch_op<kSchoolbook, kDecrypt>(a, s); }
+}  // namespace tmvp

@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(128) k_enc_front(KemParams P, const uint8_t *p
       mo[k] = buf[k];
       ko[k] = g[k];
     }
-    shake128_32(reinterpret_cast<uint64_t *>(s_stream + t * P.gs_bytes), P.gs_bytes, g + 4);
+    uint64_t seed[4] = {g[4], g[5], g[6], g[7]};
+    shake128_32(reinterpret_cast<uint64_t *>(s_stream + t * P.gs_bytes), P.gs_bytes, seed);
   } else if (t < 2 * (size_t)n) {
     size_t i = t - n;
     uint64_t seed[4];
@@ -86,16 +87,39 @@ __global__ void __launch_bounds__(128) k_dec_g(KemParams P, const uint8_t *mbuf,
   uint64_t *ko = reinterpret_cast<uint64_t *>(kr + t * 64);
 #pragma unroll
   for (int k = 0; k < 8; k++) ko[k] = g[k];
-  shake128_32(reinterpret_cast<uint64_t *>(s_stream + t * P.gs_bytes), P.gs_bytes, g + 4);
+  uint64_t seed[4] = {g[4], g[5], g[6], g[7]};
+  shake128_32(reinterpret_cast<uint64_t *>(s_stream + t * P.gs_bytes), P.gs_bytes, seed);
+}
+
+// Decapsulation front, independent of the decryption: threads i < n expand
+// GenMatrix from the seed of the pk embedded in sk; threads n..2n-1 hash the
+// ciphertext, H(c) (saber_dec, cuda_kernel.cu:383-384 and :447).
+__global__ void __launch_bounds__(128) k_dec_front(KemParams P, const uint8_t *sk,
+                                                    const uint8_t *ct, uint8_t *a_stream,
+                                                    uint8_t *hc, int n) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (size_t)n) {
+    uint64_t seed[4];
+    load_words(seed, sk + t * P.sk_bytes + P.indcpa_sk_bytes + (size_t)P.l * P.polycompbytes, 4);
+    shake128_32(reinterpret_cast<uint64_t *>(a_stream + t * P.gm_bytes), P.gm_bytes, seed);
+  } else if (t < 2 * (size_t)n) {
+    size_t i = t - n;
+    uint64_t h[4];
+    sha3_256_words(h, reinterpret_cast<const uint64_t *>(ct + i * P.ct_bytes), P.ct_bytes);
+    uint64_t *o = reinterpret_cast<uint64_t *>(hc + i * 32);
+#pragma unroll
+    for (int w = 0; w < 4; w++) o[w] = h[w];
+  }
 }
 
 // Final key derivation.  Encapsulation (cuda_kernel.cu:185-186):
-// K = H(kr[0:32] || H(c)).  Decapsulation (cuda_kernel.cu:445-450, with the
+// K = H(kr[0:32] || H(c)); hc, when given, holds H(c) already.  Decapsulation (cuda_kernel.cu:445-450, with the
 // FO selection done as specified): K = H((fail ? z : kr[0:32]) || H(c)), the
 // selection made with a mask so that it does not branch on `fail`.
 __global__ void __launch_bounds__(128) k_final_key(KemParams P, const uint8_t *ct,
-                                                    const uint8_t *kr, const uint8_t *fail,
-                                                    const uint8_t *sk, uint8_t *ss, int n) {
+                                                    const uint8_t *hc, const uint8_t *kr,
+                                                    const uint8_t *fail, const uint8_t *sk,
+                                                    uint8_t *ss, int n) {
   size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (size_t)n) return;
   uint64_t buf[8], k[4];
@@ -107,7 +131,10 @@ __global__ void __launch_bounds__(128) k_final_key(KemParams P, const uint8_t *c
 #pragma unroll
     for (int w = 0; w < 4; w++) buf[w] ^= mask & (buf[w] ^ z[w]);
   }
-  sha3_256_words(buf + 4, reinterpret_cast<const uint64_t *>(ct + t * P.ct_bytes), P.ct_bytes);
+  if (hc)
+    load_words(buf + 4, hc + t * 32, 4);
+  else
+    sha3_256_words(buf + 4, reinterpret_cast<const uint64_t *>(ct + t * P.ct_bytes), P.ct_bytes);
   sha3_256_64(k, buf);
   uint64_t *o = reinterpret_cast<uint64_t *>(ss + t * 32);
 #pragma unroll

@@ -50,27 +50,39 @@ __device__ __forceinline__ uint64_t rotl64(uint64_t v, int n) {
   return n == 0 ? v : ((v << n) | (v >> (64 - n)));
 }
 
-// The 24-round permutation, fully unrolled over a register-resident state.
-__device__ __forceinline__ void keccak_f1600(uint64_t (&A)[25]) {
+// Round constants in the constant bank (the round loop is not unrolled, so
+// the constant is indexed by the round counter).
+__constant__ KeccakTables kKeccak = make_keccak_tables();
+
+// One round over a register-resident state (theta, rho+pi, chi, iota).
+__device__ __forceinline__ void keccak_round(uint64_t (&A)[25], uint64_t rc) {
   constexpr KeccakTables T = make_keccak_tables();
+  uint64_t C[5], D[5], B[25];
 #pragma unroll
-  for (int ir = 0; ir < 24; ir++) {
-    uint64_t C[5], D[5], B[25];
+  for (int x = 0; x < 5; x++) C[x] = A[x] ^ A[x + 5] ^ A[x + 10] ^ A[x + 15] ^ A[x + 20];
 #pragma unroll
-    for (int x = 0; x < 5; x++) C[x] = A[x] ^ A[x + 5] ^ A[x + 10] ^ A[x + 15] ^ A[x + 20];
+  for (int x = 0; x < 5; x++) D[x] = C[(x + 4) % 5] ^ rotl64(C[(x + 1) % 5], 1);
 #pragma unroll
-    for (int x = 0; x < 5; x++) D[x] = C[(x + 4) % 5] ^ rotl64(C[(x + 1) % 5], 1);
-#pragma unroll
-    for (int x = 0; x < 5; x++)
-#pragma unroll
-      for (int y = 0; y < 5; y++)
-        B[y + 5 * ((2 * x + 3 * y) % 5)] = rotl64(A[x + 5 * y] ^ D[x], T.rho[x + 5 * y]);
+  for (int x = 0; x < 5; x++)
 #pragma unroll
     for (int y = 0; y < 5; y++)
+      B[y + 5 * ((2 * x + 3 * y) % 5)] = rotl64(A[x + 5 * y] ^ D[x], T.rho[x + 5 * y]);
 #pragma unroll
-      for (int x = 0; x < 5; x++)
-        A[x + 5 * y] = B[x + 5 * y] ^ (~B[(x + 1) % 5 + 5 * y] & B[(x + 2) % 5 + 5 * y]);
-    A[0] ^= T.rc[ir];
+  for (int y = 0; y < 5; y++)
+#pragma unroll
+    for (int x = 0; x < 5; x++)
+      A[x + 5 * y] = B[x + 5 * y] ^ (~B[(x + 1) % 5 + 5 * y] & B[(x + 2) % 5 + 5 * y]);
+  A[0] ^= rc;
+}
+
+// The 24-round permutation.  The loop body is two rounds: a fully unrolled
+// permutation (~5k instructions) does not fit the instruction cache and
+// stalls every warp on instruction fetch.
+__device__ __forceinline__ void keccak_f1600(uint64_t (&A)[25]) {
+#pragma unroll 1
+  for (int ir = 0; ir < 24; ir += 2) {
+    keccak_round(A, kKeccak.rc[ir]);
+    keccak_round(A, kKeccak.rc[ir + 1]);
   }
 }
 

@@ -7,8 +7,9 @@
 //             -> k_cpa<kKeygen> -> k_kp_final (H(pk), z)
 //   encaps  : k_enc_front (H(coins), H(pk), G, GenSecret; GenMatrix)
 //             -> k_cpa<kEncrypt> -> k_final_key
-//   decaps  : k_shake_jobs (GenMatrix) -> k_cpa<kDecrypt> -> k_dec_g
-//             -> k_cpa<kReenc> -> k_final_key (implicit rejection)
+//   decaps  : k_dec_front (GenMatrix; H(c)) on a side stream, concurrent with
+//             k_cpa<kDecrypt> -> k_dec_g; then k_cpa<kReenc> -> k_final_key
+//             (implicit rejection)
 // They replace the launch sequences of saber_enc / saber_dec
 // (TMVP-Saber/SABER-GPU/src/cuda_kernel.cu:25-479) and SABLE_enc / SABLE_dec
 // (TMVP_SABLE/src/SABLE_indcpa.cu:24-610).
@@ -32,17 +33,6 @@
 #include "hash_kernels.cuh"
 #include "kem_common.cuh"
 
-namespace tmvp {
-int cpa_launch_fp8(int op, const CpaArgs &a, cudaStream_t s);
-int cpa_launch_int8(int op, const CpaArgs &a, cudaStream_t s);
-int cpa_launch_cc(int op, const CpaArgs &a, cudaStream_t s);
-int cpa_launch_sb(int op, const CpaArgs &a, cudaStream_t s);
-size_t cpa_smem_fp8(int op, const KemParams &P);
-size_t cpa_smem_int8(int op, const KemParams &P);
-size_t cpa_smem_cc(int op, const KemParams &P);
-size_t cpa_smem_sb(int op, const KemParams &P);
-}  // namespace tmvp
-
 using namespace tmvp;
 
 static thread_local int g_last_error = TMVP_OK;
@@ -65,6 +55,8 @@ struct tmvp_ctx {
   size_t ws_cap = 0;
   int *d_err = nullptr;   // device-side input-range flag
   uint64_t launches = 0;
+  cudaStream_t side = nullptr;          // second stream for independent stages
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   std::mutex mu;
   // optional per-stage timing: CUDA events recorded on the launching stream
   bool timing = false;
@@ -237,13 +229,9 @@ int run_cpa(tmvp_ctx *c, int form, int op, CpaArgs &a, cudaStream_t s) {
   a.err = c->d_err;
   int e;
   StageTimer tm(c, form_tag(resolve_form(form), op), s);
-  switch (resolve_form(form)) {
-    case kFp8TC: e = cpa_launch_fp8(op, a, s); break;
-    case kInt8TC: e = cpa_launch_int8(op, a, s); break;
-    case kCudaCore: e = cpa_launch_cc(op, a, s); break;
-    case kSchoolbook: e = cpa_launch_sb(op, a, s); break;
-    default: return TMVP_EINVAL;
-  }
+  int f = resolve_form(form);
+  if (f != kFp8TC && f != kInt8TC && f != kCudaCore && f != kSchoolbook) return TMVP_EINVAL;
+  e = cpa_launch(f, op, a, s);
   c->launches++;
   return e == 0 ? TMVP_OK : TMVP_EDEVICE;
 }
@@ -342,7 +330,10 @@ int tmvp_ctx_create(int device, size_t mem_budget, tmvp_ctx **out) {
   c->device = device;
   c->budget = mem_budget;
   Guard g(c);
-  if (cudaMalloc(&c->d_err, sizeof(int)) != cudaSuccess || cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) {
+  if (cudaMalloc(&c->d_err, sizeof(int)) != cudaSuccess || cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess) {
     delete c;
     return set_err(TMVP_EDEVICE);
   }
@@ -359,6 +350,9 @@ void tmvp_ctx_destroy(tmvp_ctx *c) {
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     if (c->ws) cudaFree(c->ws);
     if (c->d_err) cudaFree(c->d_err);
+    if (c->side) cudaStreamDestroy(c->side);
+    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+    if (c->join_ev) cudaEventDestroy(c->join_ev);
   }
   delete c;
 }
@@ -485,7 +479,7 @@ int tmvp_kem_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, u
   if ((r = run_cpa(c, form, kEncrypt, a, s))) return set_err(r);
   {
     StageTimer tm_(c, "final_key", s);
-    k_final_key<<<blocks_for(n, 128), 128, 0, s>>>(P, bct.dev, kr, nullptr, nullptr, bss.dev, (int)n);
+    k_final_key<<<blocks_for(n, 128), 128, 0, s>>>(P, bct.dev, nullptr, kr, nullptr, nullptr, bss.dev, (int)n);
   }
   c->launches++;
   if ((r = download(bct, s)) || (r = download(bss, s))) return set_err(r);
@@ -504,26 +498,25 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
   cudaStream_t s = (cudaStream_t)stream;
   Buf bss = classify(ss, n * 32, c->device), bct = classify(ct, n * P.ct_bytes, c->device),
       bsk = classify(sk, n * P.sk_bytes, c->device);
-  size_t need = up(n * P.gm_bytes) + up(n * P.gs_bytes) + 2 * up(n * 64) + up(n) +
+  size_t need = up(n * P.gm_bytes) + up(n * P.gs_bytes) + 2 * up(n * 64) + up(n) + up(n * 32) +
                 stage_bytes(bss) + stage_bytes(bct) + stage_bytes(bsk);
   if ((r = ensure_ws(c, need))) return set_err(r);
   Arena A{c->ws};
   uint8_t *a_stream = A.take(n * P.gm_bytes), *s_stream = A.take(n * P.gs_bytes);
-  uint8_t *mbuf = A.take(n * 64), *kr = A.take(n * 64), *fail = A.take(n);
+  uint8_t *mbuf = A.take(n * 64), *kr = A.take(n * 64), *fail = A.take(n), *hc = A.take(n * 32);
   stage_assign(bss, A);
   stage_assign(bct, A);
   stage_assign(bsk, A);
   if ((r = upload(bct, s)) || (r = upload(bsk, s))) return set_err(r);
-  // GenMatrix from the seed of the pk embedded in sk
-  ShakeJob j0{bsk.dev, (size_t)P.sk_bytes,
-              (size_t)P.indcpa_sk_bytes + (size_t)P.l * P.polycompbytes, a_stream,
-              (size_t)P.gm_bytes, P.gm_bytes, 0, nullptr, 0, 0};
-  ShakeJob none{};
+  // fork: GenMatrix and H(c) on the side stream, concurrent with decryption
+  TRY_CUDA(cudaEventRecord(c->fork_ev, s));
+  TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
   {
-    StageTimer tm_(c, "shake_jobs", s);
-    k_shake_jobs<<<blocks_for(n, 128), 128, 0, s>>>(j0, none, (int)n);
+    StageTimer tm_(c, "dec_front", c->side);
+    k_dec_front<<<blocks_for(2 * n, 128), 128, 0, c->side>>>(P, bsk.dev, bct.dev, a_stream, hc, (int)n);
   }
   c->launches++;
+  TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
   CpaArgs a{};
   a.P = P;
   a.n = (int)n;
@@ -538,6 +531,7 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
     k_dec_g<<<blocks_for(n, 128), 128, 0, s>>>(P, mbuf, kr, s_stream, (int)n);
   }
   c->launches++;
+  TRY_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));  // join
   CpaArgs b{};
   b.P = P;
   b.n = (int)n;
@@ -553,7 +547,7 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
   if ((r = run_cpa(c, form, kReenc, b, s))) return set_err(r);
   {
     StageTimer tm_(c, "final_key", s);
-    k_final_key<<<blocks_for(n, 128), 128, 0, s>>>(P, bct.dev, kr, fail, bsk.dev, bss.dev, (int)n);
+    k_final_key<<<blocks_for(n, 128), 128, 0, s>>>(P, bct.dev, hc, kr, fail, bsk.dev, bss.dev, (int)n);
   }
   c->launches++;
   if ((r = download(bss, s))) return set_err(r);

@@ -1,0 +1,380 @@
+#!/usr/bin/env python3
+"""Saber decapsulations per second at batch 65536, bit-exact.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: 65536 independent Saber (l=3) instances, each with its own key
+pair, decapsulating its own ciphertext (keys and ciphertexts are generated on
+the GPU from SplitMix64 seeds before timing; every decapsulated key is then
+checked against the encapsulated one, and a sample against the CPU oracle).
+
+One step = one tmvp_kem_dec_batch call over the whole batch with device-
+resident inputs (inputs are 222 MB, larger than the 129 MB L2, so no flush is
+needed between steps).  `value` is decaps/s of the FP8 tensor-core form;
+`forms` adds the INT8 tensor-core and CUDA-core TMVP forms timed the same
+way.  `e2e` is the same metric through the public C ABI with pinned HOST
+buffers (host-to-device copies of ct and sk and the copy of the keys back are
+inside the timed region).  `roofline` is the dominant kernel of the step,
+timed live with CUDA events on its own stream.  `cpu_baseline` is the CPU
+oracle timed on a sample over all host threads.
+
+--impl reference times the reference's CPU path for this workload (the CPU
+oracle port of the reference's serial code; the reference itself has no CPU
+implementation) on the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "asfand-tmvp_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Saber decaps/sec at batch 64K (tensor-core TMVP vs CUDA-core TMVP), bit-exact"
+UNIT = "decaps/s"
+BATCH = 65536
+SABER = 1
+CT_BYTES, SK_BYTES, PK_BYTES = 1088, 2304, 992
+# schoolbook-equivalent work per Saber decapsulation: 15 polynomial products
+# (3 decryption + 9 matrix-vector + 3 inner product), 2*256^2 ops each
+POLY_OPS = 2 * 256 * 256
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d["hbm_gbs"], d["bf16_tflops"], "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str | None):
+        self.rows, self.proc = [], None
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+        if gpu_id:
+            cmd += ["-i", gpu_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if not self.rows:
+            return None
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def cpu_decaps_rate(n: int, nthreads: int, seed: int = 99):
+    """Oracle decapsulations per second over all host threads on n instances."""
+    from oracle import pyoracle as O
+    import tmvpkem as T
+    O.build()
+    coins = T.splitmix_bytes(seed, n * 96).reshape(n, 96)
+    pk, sk = O.kem_keypair_batch(SABER, coins, nthreads)
+    ct, ss = O.kem_enc_batch(SABER, pk, T.splitmix_bytes(seed + 1, n * 32).reshape(n, 32), nthreads)
+    t0 = time.perf_counter()
+    ss2, fail = O.kem_dec_batch(SABER, ct, sk, nthreads)
+    dt = time.perf_counter() - t0
+    assert np.array_equal(ss, ss2) and not fail.any()
+    return n / dt, (ct, sk, ss)
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    from oracle import pyoracle as O
+    import tmvpkem as T
+    nthreads = os.cpu_count() or 1
+    sample = args.ref_sample
+    O.build()
+    coins = T.splitmix_bytes(7, sample * 96).reshape(sample, 96)
+    pk, sk = O.kem_keypair_batch(SABER, coins, nthreads)
+    ct, ss = O.kem_enc_batch(SABER, pk, T.splitmix_bytes(8, sample * 32).reshape(sample, 32), nthreads)
+    for _ in range(args.warmup):
+        O.kem_dec_batch(SABER, ct, sk, nthreads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        ss2, fail = O.kem_dec_batch(SABER, ct, sk, nthreads)
+        times.append(time.perf_counter() - t0)
+        assert np.array_equal(ss, ss2) and not fail.any()
+    step = statistics.mean(times)
+    value = sample / step
+    desc = (f"CPU oracle (C port of the reference's serial Keccak/CBD/pack code, schoolbook "
+            f"multiplication), {sample} of the {BATCH} decapsulations per step")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step * 1e3 * BATCH / sample,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
+            "data": "synthetic: SplitMix64-seeded keys and ciphertexts",
+            "config": {"workload": "Saber l=3 decapsulation, batch 65536, per-instance keys",
+                       "batch": BATCH, "sample_per_step": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import tmvpkem as T
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    T.build.build()
+    ctx = T.Context(local)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+    n = args.batch
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- inputs (untimed): per-instance keys and ciphertexts, on the GPU
+    seed = 1_000_003 * (rank + 1)
+    coins = torch.from_numpy(T.splitmix_bytes(seed, n * 96).reshape(n, 96)).to(dev)
+    ecoins = torch.from_numpy(T.splitmix_bytes(seed + 1, n * 32).reshape(n, 32)).to(dev)
+    pk = torch.empty((n, PK_BYTES), dtype=torch.uint8, device=dev)
+    sk = torch.empty((n, SK_BYTES), dtype=torch.uint8, device=dev)
+    ct = torch.empty((n, CT_BYTES), dtype=torch.uint8, device=dev)
+    ss_ref = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+    ss = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+    ctx.kem_keypair_ptr(SABER, n, pk, sk, coins, T.FORM_AUTO, sp)
+    ctx.kem_enc_ptr(SABER, n, ct, ss_ref, pk, ecoins, T.FORM_AUTO, sp)
+    torch.cuda.synchronize()
+
+    def timed(form, steps, stage_timing=False):
+        for _ in range(args.warmup):
+            ctx.kem_dec_ptr(SABER, n, ss, ct, sk, form, sp)
+        if stage_timing:
+            ctx.set_timing(True)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        l0 = ctx.launches
+        barrier()
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for k in range(steps):
+            ctx.kem_dec_ptr(SABER, n, ss, ct, sk, form, sp)
+            ev[k + 1].record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        launches = ctx.launches - l0
+        per = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
+        total = ev[0].elapsed_time(ev[steps])
+        stages = ctx.stage_stats() if stage_timing else {}
+        if stage_timing:
+            ctx.set_timing(False)
+        ok = bool(torch.equal(ss, ss_ref))
+        return total, per, launches, stages, ok
+
+    gpu_id = None
+    try:
+        gpu_id = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        pass
+    sampler = ClockSampler(gpu_id)
+    total_ms, per_ms, launches, stages, exact_main = timed(T.FORM_AUTO, args.steps, stage_timing=True)
+    clocks = sampler.stop()
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = ws * n * args.steps / (total_ms / 1e3)
+
+    # ---- other forms, same workload
+    form_rates, form_exact = {}, {}
+    kf = max(3, args.steps // 4)
+    others = [f for f in args.forms.split(",") if f and f != "none"]
+    for name in others:
+        form = {v: k for k, v in T.FORM_NAMES.items()}[name]
+        tm, _, _, _, ok = timed(form, kf)
+        form_rates[name] = n * kf / (tm / 1e3)
+        form_exact[name] = ok
+    form_rates["fp8_tc"] = value / ws
+
+    # ---- end to end through the C ABI with pinned host buffers
+    if args.no_e2e:
+        e2e_ms, e2e_exact, e2e_value = [float("nan")], True, None
+    else:
+        e2e_ms, e2e_exact, e2e_value = _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws)
+    # ---- bit-exactness against the CPU oracle on a sample
+    oracle_ok = None
+    if not args.no_oracle:
+        from oracle import pyoracle as O
+        O.build()
+        idx = np.random.default_rng(5).choice(n, 256, replace=False)
+        oss, fail = O.kem_dec_batch(SABER, ct.cpu().numpy()[idx], sk.cpu().numpy()[idx],
+                                    os.cpu_count() or 1)
+        oracle_ok = bool(np.array_equal(oss, ss.cpu().numpy()[idx]) and not fail.any())
+
+    # ---- roofline of the dominant kernel
+    hbm, bf16, peak_src = _peaks()
+    name, (cnt, ms) = max(stages.items(), key=lambda kv: kv[1][1])
+    avg_s = ms / cnt / 1e3
+    traffic = _ncu_traffic(name)
+    if name.startswith("cpa_reenc") or name.startswith("cpa_decrypt"):
+        polys = 12 if "reenc" in name else 3
+        flops = n * polys * POLY_OPS
+        ach = flops / avg_s / 1e12
+        roof = {"kernel": name, "bound": "tensor" if "_tc" in name else "int32", "achieved": ach,
+                "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16,
+                "peak_source": f"{peak_src} bf16 dense (schoolbook-equivalent integer ops)",
+                "traffic": traffic}
+    else:
+        per_inst = {"shake_jobs": 32 + 3744, "dec_g": 64 + 64 + 768, "final_key": 64 + 1 + 32 + 1088 + 32}
+        byts = n * per_inst.get(name, 0)
+        ach = byts / avg_s / 1e9
+        roof = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                "frac": ach / hbm, "peak_source": f"{peak_src} HBM copy", "traffic": traffic,
+                "note": "Keccak kernel: integer-pipe bound, HBM figure is the algorithmic bytes"}
+    roof["avg_launch_ms"] = avg_s * 1e3
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "e4m3 x e4m3 -> f32 exact integer sums; results u16 mod 2^13",
+        "data": "synthetic: 65536 SplitMix64-seeded key pairs and encapsulations per GPU",
+        "config": {"workload": "Saber l=3 decapsulation, batch 65536, per-instance keys",
+                   "batch": n, "param_set": "Saber", "form": "fp8_tc",
+                   "l2": "inputs (222 MB) larger than L2; no flush", "parallelism": f"replicas x{ws}"},
+        "forms": form_rates,
+        "tc_over_cuda_core": (value / ws / form_rates["cuda_core"]) if "cuda_core" in form_rates else None,
+        "latency_ms": {"p50": float(np.percentile(per_ms, 50)), "p99": float(np.percentile(per_ms, 99)),
+                       "batch": n},
+        "bit_exact": {"all_keys_match": exact_main and all(form_exact.values()) and e2e_exact,
+                      "checked": n, "oracle_sample": 256, "oracle_match": oracle_ok},
+        "roofline": roof,
+        "stages_ms_per_step": {k: v[1] / max(v[0], 1) for k, v in stages.items()},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * (CT_BYTES + SK_BYTES),
+                "d2h_bytes_per_step": n * 32, "ms_per_step": statistics.mean(e2e_ms)},
+        "oracle_sample_note": "256 random instances decapsulated by the CPU oracle and compared",
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu:
+        rate, _ = cpu_decaps_rate(args.cpu_sample, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": f"{args.cpu_sample} Saber decapsulations (oracle C port, "
+                                          f"schoolbook), all host threads"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws):
+    import torch
+    ct_h = ct.cpu().pin_memory()
+    sk_h = sk.cpu().pin_memory()
+    ss_h = torch.empty((n, 32), dtype=torch.uint8).pin_memory()
+    ke = max(3, args.steps // 2)
+    for _ in range(min(2, args.warmup)):
+        ctx.kem_dec_ptr(SABER, n, ss_h, ct_h, sk_h, T.FORM_AUTO, sp)
+    e2e_ms = []
+    for _ in range(ke):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.kem_dec_ptr(SABER, n, ss_h, ct_h, sk_h, T.FORM_AUTO, sp)
+        b.record(stream)
+        b.synchronize()
+        e2e_ms.append(a.elapsed_time(b))
+    e2e_exact = bool(torch.equal(ss_h, ss_ref.cpu()))
+    return e2e_ms, e2e_exact, ws * n / (statistics.mean(e2e_ms) / 1e3)
+
+
+def _ncu_traffic(kernel: str):
+    """DRAM bytes per launch for `kernel` from the committed ncu summary, scaled
+    to the benchmark batch (profiles/dram_traffic.txt: '<stage> <bytes per
+    instance>' lines)."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for ln in open(p):
+        parts = ln.split()
+        if len(parts) >= 2 and parts[0] == kernel:
+            try:
+                return float(parts[1]) * BATCH
+            except ValueError:
+                return None
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=BATCH)
+    ap.add_argument("--cpu-sample", type=int, default=16384)
+    ap.add_argument("--ref-sample", type=int, default=16384)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (e2e) leg")
+    ap.add_argument("--no-oracle", action="store_true", help="skip the oracle sample check")
+    ap.add_argument("--forms", default="int8_tc,cuda_core",
+                    help="other forms to time besides fp8_tc (comma list, or 'none')")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())
