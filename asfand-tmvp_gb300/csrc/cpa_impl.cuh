@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(CpaCfg<FORM, OP, L, Q>::NT) k_cpa(CpaArgs a) {
         int h = P.mu >> 1;
         v = __popc(x & ((1u << h) - 1u)) - __popc(x >> h);
       }
-      if (C::TC && (v > 8 || v < -8)) bad = true;
+      if (C::TC && (v > 7 || v < -7)) bad = true;
       sec[idx] = (int16_t)v;
     }
     if (bad && a.err) atomicOr(a.err, 1);

@@ -105,7 +105,7 @@ __device__ __forceinline__ void pack8(uint8_t *dst, const uint32_t (&V)[4], int 
 }
 
 template <int FORM, int OP, int L, int Q>
-__global__ void __launch_bounds__(128, 4) k_cpa_tc(CpaArgs a, TcLayout lo) {
+__global__ void __launch_bounds__(128, (Q >= 4 ? 3 : 4)) k_cpa_tc(CpaArgs a, TcLayout lo) {
   using C = TcCfg<FORM, OP, L, Q>;
   extern __shared__ __align__(16) uint8_t sm[];
   const KemParams &P = a.P;

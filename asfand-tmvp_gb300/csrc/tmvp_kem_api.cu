@@ -359,6 +359,7 @@ void tmvp_ctx_destroy(tmvp_ctx *c) {
 
 size_t tmvp_ctx_workspace_bytes(const tmvp_ctx *c) { return c ? c->ws_cap : 0; }
 
+
 int tmvp_ctx_set_timing(tmvp_ctx *c, int enable) {
   if (!c) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(c->mu);

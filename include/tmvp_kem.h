@@ -107,6 +107,9 @@ int tmvp_ctx_stage_stats(tmvp_ctx *ctx, int idx, char *name, size_t name_len,
                          uint64_t *launches, double *total_ms);
 
 /* Batched, derandomised KEM.  stream: a cudaStream_t (NULL = legacy default).
+ * A secret key whose coefficients are outside the tensor-core forms' range
+ * (|s| <= 7; real keys have |s| <= 5) makes the call return TMVP_EINVAL when
+ * the call synchronises (host buffers).
  * keypair coins per instance: seed_A(32) | seed_s(32) | z(32).
  * enc coins per instance: 32 bytes (hashed into the message, as saber_enc
  * does with its 32 random bytes, cuda_kernel.cu:116).
@@ -132,7 +135,9 @@ int tmvp_indcpa_dec_batch(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *
 
 /* MatrixVectorMul alone: out[i] = sum_j A[i][j] * s[j] mod 2^eq
  * (transpose: A[j][i]); A uint16 [n][l][l][256] (values < 2^eq), s int8
- * [n][l][256] with |s| <= 8, out uint16 [n][l][256].  l in 2..4, eq <= 13. */
+ * [n][l][256], out uint16 [n][l][256].  l in 2..4, eq <= 13.  The
+ * tensor-core forms take |s| <= 7 (CBD secrets have |s| <= 5) and return
+ * TMVP_EINVAL otherwise; the CUDA-core forms take any int8 secret. */
 int tmvp_matvec_batch(tmvp_ctx *ctx, size_t n, int l, int eq, int transpose, uint16_t *out,
                       const uint16_t *A, const int8_t *s, tmvp_form form, void *stream);
 

@@ -33,20 +33,31 @@ def test_matvec_random(kem, oracle, form, l, eq, transpose):
 
 @pytest.mark.parametrize("form", ALL_FORMS)
 def test_matvec_extremes(kem, oracle, form):
-    """Largest exact inputs: |s| = 8 everywhere and public values at the digit
-    boundaries, so every tensor-core accumulator reaches its bound."""
+    """Largest exact inputs: |s| = 7 everywhere (the tensor-core forms' limit)
+    and public values at the digit boundaries, so every accumulator reaches
+    its bound."""
     T, ctx = kem
     n, l, eq = 12, 4, 13
-    vals = np.array([0, 1, 15, 16, 17, 31, 32, 511, 512, 4095, 4096, 4097, 8176, 8191], np.uint16)
+    vals = np.array([0, 1, 7, 8, 15, 16, 17, 31, 32, 511, 512, 4095, 4096, 4097, 8176, 8191], np.uint16)
     rng = np.random.default_rng(5)
     A = vals[rng.integers(0, len(vals), (n, l, l, 256))]
-    s = np.where(rng.integers(0, 2, (n, l, 256)) == 1, 8, -8).astype(np.int8)
+    s = np.where(rng.integers(0, 2, (n, l, 256)) == 1, 7, -7).astype(np.int8)
     A[0] = 4096
-    s[0] = -8
+    s[0] = -7
     A[1] = 8191
-    s[1] = 8
+    s[1] = 7
     got = ctx.matvec(A, s, eq=eq, form=form)
     assert np.array_equal(got, oracle.matvec(A, s, eq=eq, nthreads=4))
+
+
+@pytest.mark.parametrize("form", [0, 4])
+def test_matvec_wide_secrets_cuda_core(kem, oracle, form):
+    """The CUDA-core forms take any int8 secret."""
+    T, ctx = kem
+    rng = np.random.default_rng(6)
+    A = rng.integers(0, 1 << 13, (8, 3, 3, 256), dtype=np.uint16)
+    s = rng.integers(-128, 128, (8, 3, 256)).astype(np.int8)
+    assert np.array_equal(ctx.matvec(A, s, eq=13, form=form), oracle.matvec(A, s, eq=13, nthreads=4))
 
 
 @pytest.mark.parametrize("form", ALL_FORMS)

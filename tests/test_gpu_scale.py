@@ -1,0 +1,73 @@
+"""Batch-scale properties on the GPU: 10^6 seeded Saber round trips are
+bit-exact, and the raw TMVP matvec at its benchmark size (16384 instances)
+agrees with the oracle on a sample and is linear in the secret."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_million_round_trips(kem, oracle):
+    import torch
+    T, ctx = kem
+    dev = torch.device("cuda", 0)
+    n, chunks = 65536, 16  # 16 * 65536 = 1,048,576 round trips
+    z = T.sizes(T.SABER)
+    pk = torch.empty((n, z.pk_bytes), dtype=torch.uint8, device=dev)
+    sk = torch.empty((n, z.sk_bytes), dtype=torch.uint8, device=dev)
+    ct = torch.empty((n, z.ct_bytes), dtype=torch.uint8, device=dev)
+    ss = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+    ss2 = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+    rng = np.random.default_rng(0)
+    total = 0
+    for c in range(chunks):
+        coins = torch.from_numpy(T.splitmix_bytes(7_000_000 + c, n * 96).reshape(n, 96)).to(dev)
+        ec = torch.from_numpy(T.splitmix_bytes(8_000_000 + c, n * 32).reshape(n, 32)).to(dev)
+        ctx.kem_keypair_ptr(T.SABER, n, pk, sk, coins)
+        ctx.kem_enc_ptr(T.SABER, n, ct, ss, pk, ec)
+        form = [T.FORM_FP8_TC, T.FORM_INT8_TC, T.FORM_CUDA_CORE][c % 3]
+        ctx.kem_dec_ptr(T.SABER, n, ss2, ct, sk, form)
+        torch.cuda.synchronize()
+        assert torch.equal(ss, ss2), f"chunk {c}: decapsulated keys differ"
+        total += n
+        # every stage of a random sample against the oracle
+        idx = rng.choice(n, 16, replace=False)
+        c_np = coins.cpu().numpy()[idx]
+        opk, osk = oracle.kem_keypair_batch(T.SABER, c_np, 4)
+        assert np.array_equal(pk.cpu().numpy()[idx], opk) and np.array_equal(sk.cpu().numpy()[idx], osk)
+        oct_, oss = oracle.kem_enc_batch(T.SABER, opk, ec.cpu().numpy()[idx], 4)
+        assert np.array_equal(ct.cpu().numpy()[idx], oct_) and np.array_equal(ss.cpu().numpy()[idx], oss)
+    assert total >= 1_000_000
+
+
+@pytest.mark.parametrize("form", [0, 1, 2])
+def test_matvec_benchmark_size(kem, oracle, form):
+    """16384 instances of a 3x3 matrix (uniform mod 2^13) times CBD(mu=8) secrets."""
+    import torch
+    T, ctx = kem
+    dev = torch.device("cuda", 0)
+    n, l = 16384, 3
+    rng = np.random.default_rng(11)
+    A = rng.integers(0, 1 << 13, (n, l, l, 256), dtype=np.uint16)
+    # CBD(mu=8): popcount difference of two nibbles
+    b = rng.integers(0, 256, (n, l, 256), dtype=np.uint8)
+    pc = np.vectorize(lambda x: bin(int(x)).count("1"), otypes=[np.int8])
+    s = (pc(b & 15) - pc(b >> 4)).astype(np.int8)
+    At = torch.from_numpy(A.view(np.int16)).to(dev)
+    st = torch.from_numpy(s).to(dev)
+    out = torch.empty((n, l, 256), dtype=torch.int16, device=dev)
+    ctx.matvec_ptr(n, l, 13, 0, out, At, st, form)
+    got = out.cpu().numpy().view(np.uint16)
+    idx = rng.choice(n, 64, replace=False)
+    want = oracle.matvec(A[idx], s[idx], eq=13, nthreads=4)
+    assert np.array_equal(got[idx], want)
+    # linearity in the secret: A(s1 + s2) = A s1 + A s2 (mod 2^13)
+    s1 = np.clip(s, -3, 3).astype(np.int8)
+    s2 = (s - s1).astype(np.int8)
+    o1 = torch.empty_like(out)
+    o2 = torch.empty_like(out)
+    ctx.matvec_ptr(n, l, 13, 0, o1, At, torch.from_numpy(s1).to(dev), form)
+    ctx.matvec_ptr(n, l, 13, 0, o2, At, torch.from_numpy(s2).to(dev), form)
+    summ = (o1.cpu().numpy().view(np.uint16).astype(np.uint32) +
+            o2.cpu().numpy().view(np.uint16).astype(np.uint32)) & 8191
+    assert np.array_equal(summ.astype(np.uint16), got)
