@@ -141,6 +141,25 @@ int tmvp_indcpa_dec_batch(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *
 int tmvp_matvec_batch(tmvp_ctx *ctx, size_t n, int l, int eq, int transpose, uint16_t *out,
                       const uint16_t *A, const int8_t *s, tmvp_form form, void *stream);
 
+/* Decapsulation that allocates nothing.  No counterpart in the reference.
+ * For callers that cannot call cudaMalloc: a host whose GPU memory is owned
+ * by its own pool allocator, a serving process that forbids allocation after
+ * start-up, or code recorded into a graph where allocation is not allowed.
+ * Instead of a context workspace it uses one fixed array in device global
+ * memory (7.4 MiB, sized for TMVP_NOALLOC_MAX_BATCH instances of the largest
+ * parameter set), which every GPU that loads the library holds until the
+ * process exits.  n <= TMVP_NOALLOC_MAX_BATCH
+ * (larger n returns TMVP_EINVAL and launches nothing); ss, ct and sk must be
+ * 16-byte-aligned device memory of the current GPU.  The first call on a
+ * device looks up the array's address with that device current: make it
+ * before any stream capture.  All calls share the array, which keeps the last
+ * call's contents, so calls that overlap on the GPU race; issue them in order
+ * on one stream.  The call is asynchronous on `stream` and calls no
+ * cudaMalloc, cudaFree or allocating library routine. */
+#define TMVP_NOALLOC_MAX_BATCH 1024
+int tmvp_kem_dec_batch_noalloc(tmvp_param_set set, size_t n, uint8_t *ss, const uint8_t *ct,
+                               const uint8_t *sk, tmvp_form form, void *stream);
+
 /* NIST-style single-instance API for the default parameter set (Saber unless
  * changed).  Randomness comes from the randombytes hook (default: the
  * operating system's getrandom).  Return 0 on success. */
