@@ -1,8 +1,8 @@
 // cpa_tc.cuh — operand staging and the mma.sync engine of the tensor-core
 // IND-CPA forms.
 //
-// Both forms multiply the negacyclic Toeplitz matrix of a small secret
-// (A operand, m16 x k32) by digit columns of the public polynomials (B
+// The mma.sync forms multiply the negacyclic Toeplitz matrix of a small
+// secret (A operand, m16 x k32) by digit columns of the public polynomials (B
 // operand, k32 x n8):
 //   FP8  (mma.sync m16n8k32 e4m3 x e4m3 -> f32): the public coefficient is
 //        split into unsigned radix-8 digits d (3 bits each); a column holds
@@ -14,10 +14,13 @@
 //   INT8 (mma.sync m16n8k32 s8 x u8 -> s32): two 8-bit limbs per coefficient.
 // The Toeplitz fragments are 4-byte windows of srev[k] = s_ext[510 - k],
 // read from four byte-shifted copies so that every window is an aligned word.
+// The tcgen05 form (cpa_umma.cuh) uses unsigned radix-16 digits 0..15, each
+// exact in e4m3, and no bias column.
 #pragma once
 #include <cstdint>
 
 #include "cpa_engine.cuh"
+#include "cpa_umma.cuh"
 #include "kem_common.cuh"
 
 namespace tmvp {
@@ -32,7 +35,7 @@ __device__ __forceinline__ void copy16(uint8_t *dst, const uint8_t *src, int nby
 // Digit columns of a w-bit public coefficient.
 template <int FORM>
 __host__ __device__ __forceinline__ int tc_digits(int w) {
-  return FORM == kFp8TC ? (w + 2) / 3 : 2;
+  return FORM == kFp8TC ? (w + 2) / 3 : (FORM == kFp8Tcgen05 ? (w + 3) / 4 : 2);
 }
 
 // Number of B columns for R public polys whose first RA have width wa and the
@@ -67,10 +70,16 @@ __device__ __forceinline__ void unpack8(const uint8_t *base, int byte0, int w, u
 
 // Digit column words for eight coefficients held as 16-bit lanes.
 // FP8: bytes 0x50 | ((x >> 3d) & 7).  INT8: limb d = (x >> 8d) & 0xff.
+// tcgen05 FP8: e4m3 of (x >> 4d) & 15.
 template <int FORM>
 __device__ __forceinline__ uint2 digit8(const uint32_t (&X)[4], int d) {
   uint32_t t[4];
-  if (FORM == kFp8TC) {
+  if (FORM == kFp8Tcgen05) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) t[i] = (X[i] >> (4 * d)) & 0x000F000Fu;
+    return make_uint2(e4m3_digits4(__byte_perm(t[0], t[1], 0x6420)),
+                      e4m3_digits4(__byte_perm(t[2], t[3], 0x6420)));
+  } else if (FORM == kFp8TC) {
 #pragma unroll
     for (int i = 0; i < 4; i++) t[i] = ((X[i] >> (3 * d)) & 0x00070007u) | 0x00500050u;
     return make_uint2(__byte_perm(t[0], t[1], 0x6420), __byte_perm(t[2], t[3], 0x6420));

@@ -71,7 +71,19 @@ inline bool make_params(int set, KemParams *p) {
 }
 
 // Polynomial-multiplication forms (same numbering as tmvp_form).
-enum Form : int { kCudaCore = 0, kInt8TC = 1, kFp8TC = 2, kAuto = 3, kSchoolbook = 4 };
+enum Form : int {
+  kCudaCore = 0,
+  kInt8TC = 1,
+  kFp8TC = 2,
+  kAuto = 3,
+  kSchoolbook = 4,
+  kFp8Tcgen05 = 5
+};
+
+// A form a kernel exists for (kAuto is resolved before launch).
+__host__ __device__ constexpr bool form_valid(int f) {
+  return f == kCudaCore || f == kInt8TC || f == kFp8TC || f == kSchoolbook || f == kFp8Tcgen05;
+}
 
 // Little-endian bit-stream field read from a byte array: bits
 // [bit, bit + w), w <= 16.  Reads up to 4 bytes starting at bit / 8; callers

@@ -102,8 +102,8 @@ extern "C" int tmvp_kem_dec_batch_noalloc(tmvp_param_set set, size_t n, uint8_t 
   if (!make_params(set, &P)) return TMVP_EINVAL;
   if (n == 0) return TMVP_OK;
   if (n > kMaxBatch) return TMVP_EINVAL;  // beyond the fixed scratch array
-  int f = form == TMVP_FORM_AUTO ? kFp8TC : (int)form;
-  if (f != kFp8TC && f != kInt8TC && f != kCudaCore && f != kSchoolbook) return TMVP_EINVAL;
+  int f = form == TMVP_FORM_AUTO ? kFp8Tcgen05 : (int)form;
+  if (!form_valid(f)) return TMVP_EINVAL;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return TMVP_ENOTSUP;
   if (!device_buffer(ss, dev) || !device_buffer(ct, dev) || !device_buffer(sk, dev))

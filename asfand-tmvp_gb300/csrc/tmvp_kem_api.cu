@@ -160,7 +160,7 @@ int download(const Buf &b, cudaStream_t s) {
 }
 
 int resolve_form(int form) {
-  if (form == kAuto) return kFp8TC;
+  if (form == kAuto) return kFp8Tcgen05;
   return form;
 }
 
@@ -216,12 +216,13 @@ void collect_stage_times(tmvp_ctx *c) {
 }
 
 const char *form_tag(int form, int op) {
-  static const char *names[4][5] = {
+  static const char *names[5][5] = {
       {"cpa_decrypt_cuda_core", "cpa_encrypt_cuda_core", "cpa_reenc_cuda_core", "cpa_keygen_cuda_core", "cpa_matvec_cuda_core"},
       {"cpa_decrypt_int8_tc", "cpa_encrypt_int8_tc", "cpa_reenc_int8_tc", "cpa_keygen_int8_tc", "cpa_matvec_int8_tc"},
       {"cpa_decrypt_fp8_tc", "cpa_encrypt_fp8_tc", "cpa_reenc_fp8_tc", "cpa_keygen_fp8_tc", "cpa_matvec_fp8_tc"},
-      {"cpa_decrypt_schoolbook", "cpa_encrypt_schoolbook", "cpa_reenc_schoolbook", "cpa_keygen_schoolbook", "cpa_matvec_schoolbook"}};
-  int f = form == kSchoolbook ? 3 : form;
+      {"cpa_decrypt_schoolbook", "cpa_encrypt_schoolbook", "cpa_reenc_schoolbook", "cpa_keygen_schoolbook", "cpa_matvec_schoolbook"},
+      {"cpa_decrypt_fp8_tcgen05", "cpa_encrypt_fp8_tcgen05", "cpa_reenc_fp8_tcgen05", "cpa_keygen_fp8_tcgen05", "cpa_matvec_fp8_tcgen05"}};
+  int f = form == kSchoolbook ? 3 : (form == kFp8Tcgen05 ? 4 : form);
   return names[f][op];
 }
 
@@ -230,7 +231,7 @@ int run_cpa(tmvp_ctx *c, int form, int op, CpaArgs &a, cudaStream_t s) {
   int e;
   StageTimer tm(c, form_tag(resolve_form(form), op), s);
   int f = resolve_form(form);
-  if (f != kFp8TC && f != kInt8TC && f != kCudaCore && f != kSchoolbook) return TMVP_EINVAL;
+  if (!form_valid(f)) return TMVP_EINVAL;
   e = cpa_launch(f, op, a, s);
   c->launches++;
   return e == 0 ? TMVP_OK : TMVP_EDEVICE;
@@ -243,7 +244,7 @@ int check_common(tmvp_ctx *c, int set, size_t n, int form, KemParams *P) {
   if (!make_params(set, P)) return TMVP_EINVAL;
   if (n > (size_t)(INT_MAX / 2)) return TMVP_EINVAL;
   int f = resolve_form(form);
-  if (f != kFp8TC && f != kInt8TC && f != kCudaCore && f != kSchoolbook) return TMVP_EINVAL;
+  if (!form_valid(f)) return TMVP_EINVAL;
   return TMVP_OK;
 }
 
@@ -258,7 +259,7 @@ int finish(tmvp_ctx *c, cudaStream_t s, bool host_sync) {
     if (h) {
       cudaMemsetAsync(c->d_err, 0, sizeof(int), s);
       cudaStreamSynchronize(s);
-      return TMVP_EINVAL;
+      return (h & 2) ? TMVP_ETIMEOUT : TMVP_EINVAL;
     }
   }
   return TMVP_OK;
@@ -358,6 +359,13 @@ void tmvp_ctx_destroy(tmvp_ctx *c) {
 }
 
 size_t tmvp_ctx_workspace_bytes(const tmvp_ctx *c) { return c ? c->ws_cap : 0; }
+
+int tmvp_ctx_reserve(tmvp_ctx *c, size_t bytes) {
+  if (!c) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  return set_err(ensure_ws(c, bytes));
+}
 
 
 int tmvp_ctx_set_timing(tmvp_ctx *c, int enable) {
@@ -689,7 +697,7 @@ int tmvp_matvec_batch(tmvp_ctx *c, size_t n, int l, int eq, int transpose, uint1
   if (n == 0) return set_err(TMVP_OK);
   if (!out || !A_ || !s_) return set_err(TMVP_EINVAL);
   int f = resolve_form(form);
-  if (f != kFp8TC && f != kInt8TC && f != kCudaCore && f != kSchoolbook) return set_err(TMVP_EINVAL);
+  if (!form_valid(f)) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(c->mu);
   Guard g(c);
   cudaStream_t st = (cudaStream_t)stream;

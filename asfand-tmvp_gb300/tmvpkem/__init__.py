@@ -18,9 +18,9 @@ from . import build as _build
 LIGHTSABER, SABER, FIRESABER, LIGHTSABLE, SABLE, FIRESABLE = range(6)
 SET_NAMES = {LIGHTSABER: "LightSaber", SABER: "Saber", FIRESABER: "FireSaber",
              LIGHTSABLE: "LightSable", SABLE: "Sable", FIRESABLE: "FireSable"}
-FORM_CUDA_CORE, FORM_INT8_TC, FORM_FP8_TC, FORM_AUTO, FORM_SCHOOLBOOK = range(5)
+FORM_CUDA_CORE, FORM_INT8_TC, FORM_FP8_TC, FORM_AUTO, FORM_SCHOOLBOOK, FORM_FP8_TCGEN05 = range(6)
 FORM_NAMES = {FORM_CUDA_CORE: "cuda_core", FORM_INT8_TC: "int8_tc", FORM_FP8_TC: "fp8_tc",
-              FORM_AUTO: "auto", FORM_SCHOOLBOOK: "schoolbook"}
+              FORM_AUTO: "auto", FORM_SCHOOLBOOK: "schoolbook", FORM_FP8_TCGEN05: "fp8_tcgen05"}
 
 OK, EINVAL, ENOMEM, EDEVICE, ETIMEOUT, ENOTSUP = 0, -1, -2, -3, -4, -5
 
@@ -107,11 +107,41 @@ def lib(build_if_missing: bool = False):
     L.SABLE_dec.argtypes = [P, P, P, P, I]
     for nm in ("saber_enc", "saber_dec", "SABLE_enc", "SABLE_dec"):
         getattr(L, nm).restype = None
+    L.tmvp_ctx_reserve.argtypes = [P, S]
+    L.tmvp_kem_dec_batch_noalloc.argtypes = [I, S, P, P, P, I, P]
+    L.tmvp_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]
+    L.tmvp_server_destroy.argtypes = [P]
+    L.tmvp_server_destroy.restype = None
+    L.tmvp_server_add_keys.argtypes = [P, I, S, P, P, P]
+    L.tmvp_server_submit.argtypes = [P, I, ctypes.c_uint32, P, P, ctypes.POINTER(ctypes.c_uint64)]
+    L.tmvp_server_wait.argtypes = [P, ctypes.c_uint64, I]
+    L.tmvp_server_drain.argtypes = [P, I]
+    L.tmvp_server_get_stats.argtypes = [P, ctypes.POINTER(ServerStats)]
+    L.tmvp_server_reset_stats.argtypes = [P]
+    L.tmvp_server_reset_stats.restype = None
+    L.tmvp_server_loadgen.argtypes = [P, ctypes.c_double, ctypes.c_double, ctypes.c_uint64, P, S,
+                                      ctypes.c_double, ctypes.POINTER(ctypes.c_uint64)]
     L.tmvp_ref_set_batch.argtypes = [I, S]
     L.tmvp_ref_batch.argtypes = [I]
     L.tmvp_ref_batch.restype = S
     _lib = L
     return L
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("mem_budget", ctypes.c_size_t), ("max_batch", ctypes.c_int),
+                ("slots", ctypes.c_int), ("form", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("batches", ctypes.c_uint64), ("mean_batch", ctypes.c_double),
+                ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double), ("max_us", ctypes.c_double),
+                ("elapsed_s", ctypes.c_double), ("throughput", ctypes.c_double), ("slots", ctypes.c_int),
+                ("failed", ctypes.c_uint64)]
+
+
+OP_ENCAPS, OP_DECAPS = 0, 1
 
 
 def sizes(set_id: int) -> Sizes:
@@ -281,6 +311,65 @@ class Context:
         out = np.zeros((n, l, 256), np.uint16)
         self.matvec_ptr(n, l, eq, transpose, out, A, s, form)
         return out
+
+
+class Server:
+    """The request-serving loop (tmvp_server): device-resident keys,
+    continuous batching over several in-flight batch slots."""
+
+    def __init__(self, device=0, mem_budget=0, max_batch=4096, slots=4, form=FORM_AUTO):
+        cfg = ServerConfig(device, mem_budget, max_batch, slots, form)
+        h = ctypes.c_void_p()
+        _check(lib().tmvp_server_create(ctypes.byref(cfg), ctypes.byref(h)), "tmvp_server_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().tmvp_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_keys(self, set_id, pk, sk) -> np.ndarray:
+        z = sizes(set_id)
+        pk = _u8(pk).reshape(-1, z.pk_bytes)
+        sk = _u8(sk).reshape(-1, z.sk_bytes)
+        ids = np.zeros(pk.shape[0], np.uint32)
+        _check(lib().tmvp_server_add_keys(self.h, set_id, pk.shape[0], _ptr(pk), _ptr(sk), _ptr(ids)),
+               "tmvp_server_add_keys")
+        return ids
+
+    def submit(self, op, key_id, inp: np.ndarray, out: np.ndarray) -> int:
+        """inp / out must stay alive until the request completes."""
+        t = ctypes.c_uint64()
+        _check(lib().tmvp_server_submit(self.h, op, int(key_id), _ptr(inp), _ptr(out), ctypes.byref(t)),
+               "tmvp_server_submit")
+        return t.value
+
+    def wait(self, ticket, timeout_ms=60000):
+        _check(lib().tmvp_server_wait(self.h, ticket, timeout_ms), "tmvp_server_wait")
+
+    def drain(self, timeout_ms=120000):
+        _check(lib().tmvp_server_drain(self.h, timeout_ms), "tmvp_server_drain")
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(lib().tmvp_server_get_stats(self.h, ctypes.byref(st)), "tmvp_server_get_stats")
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def reset_stats(self):
+        lib().tmvp_server_reset_stats(self.h)
+
+    def loadgen(self, rate, seconds, seed, key_ids, decaps_fraction=0.5) -> int:
+        ids = np.ascontiguousarray(key_ids, np.uint32)
+        n = ctypes.c_uint64()
+        _check(lib().tmvp_server_loadgen(self.h, rate, seconds, seed, _ptr(ids), ids.size,
+                                         decaps_fraction, ctypes.byref(n)), "tmvp_server_loadgen")
+        return n.value
 
 
 def splitmix_bytes(seed: int, n: int) -> np.ndarray:

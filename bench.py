@@ -40,7 +40,7 @@ for _p in (ROOT, os.path.join(ROOT, "asfand-tmvp_gb300")):
 
 import numpy as np  # noqa: E402
 
-METRIC = "Saber decaps/sec at batch 64K (tensor-core TMVP vs CUDA-core TMVP), bit-exact"
+METRIC = "Saber decaps/sec at batch 64K (INT8-TC vs CUDA-core), bit-exact; p50/p99 latency"
 UNIT = "decaps/s"
 BATCH = 65536
 SABER = 1
@@ -241,7 +241,7 @@ def run_ours(args):
         tm, _, _, _, ok = timed(form, kf)
         form_rates[name] = n * kf / (tm / 1e3)
         form_exact[name] = ok
-    form_rates["fp8_tc"] = value / ws
+    form_rates["auto"] = value / ws
 
     # ---- end to end through the C ABI with pinned host buffers
     if args.no_e2e:
@@ -272,7 +272,8 @@ def run_ours(args):
                 "peak_source": f"{peak_src} bf16 dense (schoolbook-equivalent integer ops)",
                 "traffic": traffic}
     else:
-        per_inst = {"shake_jobs": 32 + 3744, "dec_g": 64 + 64 + 768, "final_key": 64 + 1 + 32 + 1088 + 32}
+        per_inst = {"shake_jobs": 32 + 3744, "dec_front": 32 + 1088 + 3744 + 32,
+                    "dec_g": 64 + 64 + 768, "final_key": 64 + 1 + 32 + 1088 + 32}
         byts = n * per_inst.get(name, 0)
         ach = byts / avg_s / 1e9
         roof = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
@@ -284,10 +285,10 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "e4m3 x e4m3 -> f32 exact integer sums; results u16 mod 2^13",
+        "dtype": "e4m3 x e4m3 -> f32 (tcgen05), exact integer sums; results u16 mod 2^13",
         "data": "synthetic: 65536 SplitMix64-seeded key pairs and encapsulations per GPU",
         "config": {"workload": "Saber l=3 decapsulation, batch 65536, per-instance keys",
-                   "batch": n, "param_set": "Saber", "form": "fp8_tc",
+                   "batch": n, "param_set": "Saber", "form": "auto = fp8_tcgen05",
                    "l2": "inputs (222 MB) larger than L2; no flush", "parallelism": f"replicas x{ws}"},
         "forms": form_rates,
         "tc_over_cuda_core": (value / ws / form_rates["cuda_core"]) if "cuda_core" in form_rates else None,
@@ -303,6 +304,8 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    if not args.no_extra:
+        line["workloads"] = _workloads(ctx, T, dev, sp, stream, args)
     if rank == 0 and not args.no_cpu:
         rate, _ = cpu_decaps_rate(args.cpu_sample, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
@@ -337,6 +340,94 @@ def _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws):
     return e2e_ms, e2e_exact, ws * n / (statistics.mean(e2e_ms) / 1e3)
 
 
+def _event_ms(stream, fn, steps):
+    import torch
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(steps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def _workloads(ctx, T, dev, sp, stream, args):
+    """The other workloads of this path, timed the same way (device-resident
+    inputs, CUDA events): raw TMVP matrix-vector products, the Sable KEM at
+    batch 65536, and the serving loop under Poisson load."""
+    import torch
+    out = {}
+    forms = [("fp8_tc", T.FORM_FP8_TC), ("int8_tc", T.FORM_INT8_TC), ("cuda_core", T.FORM_CUDA_CORE)]
+    if hasattr(T, "FORM_FP8_TCGEN05"):
+        forms.insert(0, ("fp8_tcgen05", T.FORM_FP8_TCGEN05))
+    # raw matrix-vector: 16384 instances of a 3x3 matrix (uniform mod 2^13) times CBD(mu=8) secrets
+    n, l = 16384, 3
+    g = torch.Generator(device="cpu").manual_seed(1234)
+    A = torch.randint(0, 1 << 13, (n, l, l, 256), generator=g, dtype=torch.int32).to(torch.int16).to(dev)
+    r = torch.randint(0, 256, (n, l, 256), generator=g, dtype=torch.int32)
+    pc = torch.tensor([bin(i).count("1") for i in range(16)], dtype=torch.int32)
+    s8 = (pc[r & 15] - pc[r >> 4]).to(torch.int8).to(dev)
+    mv = {}
+    ref = None
+    for name, f in forms:
+        o = torch.empty((n, l, 256), dtype=torch.int16, device=dev)
+        fn = lambda o=o, f=f: ctx.matvec_ptr(n, l, 13, False, o, A, s8, f, sp)
+        for _ in range(3):
+            fn()
+        ms = _event_ms(stream, fn, 10)
+        if ref is None:
+            ref = o.clone()
+        mv[name] = {"instances_per_s": n / (ms / 1e3), "ms": ms, "matches_first_form": bool(torch.equal(o, ref))}
+    if "cuda_core" in mv:
+        for name in mv:
+            mv[name]["over_cuda_core"] = mv[name]["instances_per_s"] / mv["cuda_core"]["instances_per_s"]
+    out["matvec_16384_l3"] = mv
+    # Sable l=3 full KEM at batch 65536
+    SABLE = 4
+    z = T.sizes(SABLE)
+    nb = 65536
+    coins = torch.from_numpy(T.splitmix_bytes(77, nb * 96).reshape(nb, 96)).to(dev)
+    ecoins = torch.from_numpy(T.splitmix_bytes(78, nb * 32).reshape(nb, 32)).to(dev)
+    pk = torch.empty((nb, z.pk_bytes), dtype=torch.uint8, device=dev)
+    sk = torch.empty((nb, z.sk_bytes), dtype=torch.uint8, device=dev)
+    ct = torch.empty((nb, z.ct_bytes), dtype=torch.uint8, device=dev)
+    ss1 = torch.empty((nb, 32), dtype=torch.uint8, device=dev)
+    ss2 = torch.empty((nb, 32), dtype=torch.uint8, device=dev)
+    sab = {}
+    for name, f in forms:
+        kp = lambda f=f: ctx.kem_keypair_ptr(SABLE, nb, pk, sk, coins, f, sp)
+        en = lambda f=f: ctx.kem_enc_ptr(SABLE, nb, ct, ss1, pk, ecoins, f, sp)
+        de = lambda f=f: ctx.kem_dec_ptr(SABLE, nb, ss2, ct, sk, f, sp)
+        for fn in (kp, en, de):
+            fn()
+        t_kp, t_en, t_de = (_event_ms(stream, fn, 3) for fn in (kp, en, de))
+        sab[name] = {"keypairs_per_s": nb / (t_kp / 1e3), "encaps_per_s": nb / (t_en / 1e3),
+                     "decaps_per_s": nb / (t_de / 1e3),
+                     "round_trips_per_s": nb / ((t_kp + t_en + t_de) / 1e3),
+                     "bit_exact_round_trip": bool(torch.equal(ss1, ss2))}
+    out["sable_l3_kem_65536"] = sab
+    # serving loop: Poisson arrivals over LightSaber, Saber, FireSaber and Sable
+    rate, secs = 200_000.0, 2.0
+    srv = T.Server(device=dev.index or 0, max_batch=4096, slots=4, form=T.FORM_AUTO)
+    try:
+        ids = []
+        for k, sid in enumerate((0, 1, 2, 4)):
+            kpk, ksk = ctx.kem_keypair(sid, T.splitmix_bytes(500 + k, 256 * 96).reshape(256, 96))
+            ids.append(srv.add_keys(sid, kpk, ksk))
+        nreq = srv.loadgen(rate=rate, seconds=secs, seed=21, key_ids=np.concatenate(ids),
+                           decaps_fraction=0.5)
+        st = srv.stats()
+    finally:
+        srv.close()
+    out["serving"] = {"offered_req_per_s": rate, "seconds": secs, "requests": nreq,
+                      "throughput_req_per_s": st["throughput"], "p50_us": st["p50_us"],
+                      "p99_us": st["p99_us"], "max_us": st["max_us"], "mean_batch": st["mean_batch"],
+                      "batches": st["batches"], "slots": st["slots"], "failed": st["failed"],
+                      "mix": "encaps/decaps 50/50 over LightSaber, Saber, FireSaber, Sable; 256 keys each"}
+    return out
+
+
 def _ncu_traffic(kernel: str):
     """DRAM bytes per launch for `kernel` from the committed ncu summary, scaled
     to the benchmark batch (profiles/dram_traffic.txt: '<stage> <bytes per
@@ -366,8 +457,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (e2e) leg")
     ap.add_argument("--no-oracle", action="store_true", help="skip the oracle sample check")
-    ap.add_argument("--forms", default="int8_tc,cuda_core",
-                    help="other forms to time besides fp8_tc (comma list, or 'none')")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the matrix-vector, Sable and serving workloads")
+    ap.add_argument("--forms", default="fp8_tc,int8_tc,cuda_core",
+                    help="forms to time besides the headline (AUTO) form (comma list, or 'none')")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -49,19 +49,24 @@ typedef enum {
 
 /* Polynomial-multiplication form (the reference's `mode` argument,
  * TMVP-Saber/SABER-GPU/main.cu:25-33, cuda_kernel.cu:140-163):
- *   CUDA_CORE   TMVP on CUDA cores (reference mode 1)
- *   INT8_TC     TMVP on INT8 tensor cores: s8 secrets x u8 limbs, s32 accumulate
- *   FP8_TC      TMVP on FP8 tensor cores: e4m3 secrets x balanced radix-32
- *               digits, f32 accumulate; every partial sum is an integer below
- *               2^24, so the result is exact
- *   AUTO        the fastest exact tensor-core form on this GPU (FP8_TC)
- *   SCHOOLBOOK  plain negacyclic schoolbook on CUDA cores (reference mode 2) */
+ *   CUDA_CORE     TMVP on CUDA cores (reference mode 1)
+ *   INT8_TC       TMVP on INT8 tensor cores (mma.sync): s8 secrets x u8 limbs,
+ *                 s32 accumulate
+ *   FP8_TC        TMVP on FP8 tensor cores (mma.sync): e4m3 secrets x radix-8
+ *                 digits biased by 8, f32 accumulate; every partial sum is an
+ *                 integer below 2^24, so the result is exact
+ *   AUTO          the fastest exact tensor-core form on this GPU (FP8_TCGEN05)
+ *   SCHOOLBOOK    plain negacyclic schoolbook on CUDA cores (reference mode 2)
+ *   FP8_TCGEN05   TMVP on the 5th-generation tensor cores (tcgen05.mma,
+ *                 operands in shared memory, accumulator in tensor memory):
+ *                 e4m3 secrets x radix-16 digits, f32 accumulate, exact */
 typedef enum {
   TMVP_FORM_CUDA_CORE = 0,
   TMVP_FORM_INT8_TC = 1,
   TMVP_FORM_FP8_TC = 2,
   TMVP_FORM_AUTO = 3,
-  TMVP_FORM_SCHOOLBOOK = 4
+  TMVP_FORM_SCHOOLBOOK = 4,
+  TMVP_FORM_FP8_TCGEN05 = 5
 } tmvp_form;
 
 enum {
@@ -140,6 +145,64 @@ int tmvp_indcpa_dec_batch(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *
  * TMVP_EINVAL otherwise; the CUDA-core forms take any int8 secret. */
 int tmvp_matvec_batch(tmvp_ctx *ctx, size_t n, int l, int eq, int transpose, uint16_t *out,
                       const uint16_t *A, const int8_t *s, tmvp_form form, void *stream);
+
+/* Reserve `bytes` of device workspace up front (so that later calls do not
+ * allocate).  Fails with TMVP_ENOMEM above the context's budget. */
+int tmvp_ctx_reserve(tmvp_ctx *ctx, size_t bytes);
+
+/* ---------------------------------------------------------------------------
+ * Request-serving loop with device-resident keys and continuous batching.
+ * No counterpart in the reference (its host API runs one fixed batch per call).
+ *
+ * Requests (one KEM operation each) are queued per (parameter set, op).  A
+ * scheduler thread turns the queue with the oldest waiting request into a
+ * batch of up to max_batch requests whenever one of `slots` batch slots is
+ * free; each slot owns its workspace and CUDA stream, so up to `slots`
+ * batches run on the GPU at once while new requests keep arriving.  The slot
+ * count is the configured one reduced until all slots' device memory fits
+ * mem_budget (memory-based admission).  Keys live in device tables and are
+ * gathered per batch by index.
+ *   encaps: in = 32 random bytes,   out = ct || ss   (ct_bytes + 32 bytes)
+ *   decaps: in = ct (ct_bytes),     out = ss         (32 bytes)
+ * `in` and `out` must stay valid until the request completes.
+ * ------------------------------------------------------------------------- */
+typedef struct tmvp_server tmvp_server;
+typedef struct {
+  int device;
+  size_t mem_budget; /* device bytes for slots (0 = no cap)            */
+  int max_batch;     /* largest batch per launch, 1..65536 (0 = 4096)  */
+  int slots;         /* batches in flight (0 = 4)                      */
+  int form;          /* tmvp_form used for every batch                 */
+} tmvp_server_config;
+typedef struct {
+  uint64_t submitted, completed, batches;
+  double mean_batch;          /* requests per batch             */
+  double p50_us, p99_us, max_us; /* submit-to-completion latency */
+  double elapsed_s, throughput;  /* since the last reset         */
+  int slots;                     /* slots admitted by the budget */
+  uint64_t failed;               /* requests of batches whose launch failed
+                                    (their outputs are not written) */
+} tmvp_server_stats;
+enum { TMVP_OP_ENCAPS = 0, TMVP_OP_DECAPS = 1 };
+int tmvp_server_create(const tmvp_server_config *cfg, tmvp_server **out);
+void tmvp_server_destroy(tmvp_server *srv);
+/* Copies n key pairs of one parameter set into the device key table and
+ * returns their ids (key_ids[n]). */
+int tmvp_server_add_keys(tmvp_server *srv, tmvp_param_set set, size_t n, const uint8_t *pk,
+                         const uint8_t *sk, uint32_t *key_ids);
+int tmvp_server_submit(tmvp_server *srv, int op, uint32_t key_id, const uint8_t *in, uint8_t *out,
+                       uint64_t *ticket);
+/* 0 when the request has completed, TMVP_ETIMEOUT otherwise. */
+int tmvp_server_wait(tmvp_server *srv, uint64_t ticket, int timeout_ms);
+int tmvp_server_drain(tmvp_server *srv, int timeout_ms);
+int tmvp_server_get_stats(tmvp_server *srv, tmvp_server_stats *out);
+void tmvp_server_reset_stats(tmvp_server *srv);
+/* Load generator for benchmarking: Poisson arrivals at `rate` requests/s for
+ * `seconds`, keys drawn uniformly from key_ids, decapsulations with
+ * probability decaps_fraction (of a ciphertext made once per key), seeded. */
+int tmvp_server_loadgen(tmvp_server *srv, double rate, double seconds, uint64_t seed,
+                        const uint32_t *key_ids, size_t nkeys, double decaps_fraction,
+                        uint64_t *submitted);
 
 /* Decapsulation that allocates nothing.  No counterpart in the reference.
  * For callers that cannot call cudaMalloc: a host whose GPU memory is owned

@@ -8,7 +8,7 @@ from conftest import golden
 
 pytestmark = pytest.mark.gpu
 
-ALL_FORMS = [0, 1, 2, 4]  # cuda_core, int8_tc, fp8_tc, schoolbook
+ALL_FORMS = [0, 1, 2, 4, 5]  # cuda_core, int8_tc, fp8_tc, schoolbook, fp8_tcgen05
 SETS = range(6)
 
 
@@ -113,7 +113,7 @@ def test_reference_golden(kem, name, set_id, form):
     assert rej[0].tobytes() == g["rej_ss"].tobytes()
 
 
-@pytest.mark.parametrize("form", [0, 2])
+@pytest.mark.parametrize("form", [0, 2, 5])
 @pytest.mark.parametrize("set_id", [1, 4])
 def test_indcpa_parity(kem, oracle, set_id, form):
     T, ctx = kem
@@ -224,9 +224,10 @@ def test_out_of_range_secret_is_reported(kem):
     A = np.zeros((2, 3, 3, 256), np.uint16)
     s = np.zeros((2, 3, 256), np.int8)
     s[1, 0, 7] = 100
-    with pytest.raises(T.TmvpError) as e:
-        ctx.matvec(A, s, eq=13, form=T.FORM_FP8_TC)
-    assert e.value.code == T.EINVAL
+    for form in (T.FORM_FP8_TC, T.FORM_INT8_TC, T.FORM_FP8_TCGEN05):
+        with pytest.raises(T.TmvpError) as e:
+            ctx.matvec(A, s, eq=13, form=form)
+        assert e.value.code == T.EINVAL
     # the CUDA-core form computes it exactly
     out = ctx.matvec(A, s, eq=13, form=T.FORM_CUDA_CORE)
     assert not out.any()

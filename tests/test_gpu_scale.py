@@ -25,7 +25,7 @@ def test_million_round_trips(kem, oracle):
         ec = torch.from_numpy(T.splitmix_bytes(8_000_000 + c, n * 32).reshape(n, 32)).to(dev)
         ctx.kem_keypair_ptr(T.SABER, n, pk, sk, coins)
         ctx.kem_enc_ptr(T.SABER, n, ct, ss, pk, ec)
-        form = [T.FORM_FP8_TC, T.FORM_INT8_TC, T.FORM_CUDA_CORE][c % 3]
+        form = [T.FORM_FP8_TCGEN05, T.FORM_FP8_TC, T.FORM_INT8_TC, T.FORM_CUDA_CORE][c % 4]
         ctx.kem_dec_ptr(T.SABER, n, ss2, ct, sk, form)
         torch.cuda.synchronize()
         assert torch.equal(ss, ss2), f"chunk {c}: decapsulated keys differ"
@@ -40,7 +40,7 @@ def test_million_round_trips(kem, oracle):
     assert total >= 1_000_000
 
 
-@pytest.mark.parametrize("form", [0, 1, 2])
+@pytest.mark.parametrize("form", [0, 1, 2, 5])
 def test_matvec_benchmark_size(kem, oracle, form):
     """16384 instances of a 3x3 matrix (uniform mod 2^13) times CBD(mu=8) secrets."""
     import torch

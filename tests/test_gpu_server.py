@@ -1,0 +1,103 @@
+"""The request-serving loop: results are the same alone and in a concurrent
+mix of parameter sets and operations, and match the oracle; batches form and
+overlap under load; memory-based admission bounds the slots."""
+import threading
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SETS = (0, 1, 2, 4)  # LightSaber, Saber, FireSaber, Sable
+
+
+def _keys(T, ctx, set_id, n, seed):
+    return ctx.kem_keypair(set_id, T.splitmix_bytes(seed, n * 96).reshape(n, 96))
+
+
+def test_alone_and_in_the_mix(kem, oracle):
+    T, ctx = kem
+    srv = T.Server(max_batch=512, slots=3)
+    try:
+        keys, ids = {}, {}
+        for s in SETS:
+            pk, sk = _keys(T, ctx, s, 8, 100 + s)
+            keys[s] = (pk, sk)
+            ids[s] = srv.add_keys(s, pk, sk)
+        # one encapsulation and one decapsulation alone
+        s0 = 1
+        z = T.sizes(s0)
+        coins = T.splitmix_bytes(42, 32)
+        out_alone = np.zeros(z.ct_bytes + 32, np.uint8)
+        srv.wait(srv.submit(T.OP_ENCAPS, ids[s0][3], coins, out_alone))
+        oct_, oss = oracle.kem_enc(s0, keys[s0][0][3], coins)
+        assert out_alone[:z.ct_bytes].tobytes() == oct_ and out_alone[z.ct_bytes:].tobytes() == oss
+        ct = out_alone[:z.ct_bytes].copy()
+        dec_alone = np.zeros(32, np.uint8)
+        srv.wait(srv.submit(T.OP_DECAPS, ids[s0][3], ct, dec_alone))
+        assert dec_alone.tobytes() == oss
+        # the same two requests inside a mixed concurrent stream
+        rng = np.random.default_rng(7)
+        reqs = []
+        for i in range(3000):
+            s = SETS[rng.integers(0, len(SETS))]
+            k = int(rng.integers(0, 8))
+            zz = T.sizes(s)
+            if rng.random() < 0.5:
+                inp = T.splitmix_bytes(10_000 + i, 32)
+                reqs.append(("enc", s, k, inp, np.zeros(zz.ct_bytes + 32, np.uint8)))
+            else:
+                c, _ = ctx.kem_enc(s, keys[s][0][k], T.splitmix_bytes(20_000 + i, 32))
+                reqs.append(("dec", s, k, c[0], np.zeros(32, np.uint8)))
+        mid = len(reqs) // 2
+        reqs.insert(mid, ("enc", s0, 3, coins, np.zeros(z.ct_bytes + 32, np.uint8)))
+        reqs.insert(mid + 1, ("dec", s0, 3, ct, np.zeros(32, np.uint8)))
+        srv.reset_stats()
+
+        def producer(part):
+            for op, s, k, inp, out in part:
+                srv.submit(T.OP_ENCAPS if op == "enc" else T.OP_DECAPS, ids[s][k], inp, out)
+
+        ths = [threading.Thread(target=producer, args=(reqs[i::2],)) for i in range(2)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        srv.drain()
+        st = srv.stats()
+        assert st["completed"] == len(reqs) and st["failed"] == 0
+        assert st["batches"] < len(reqs)  # requests were batched together
+        # the two repeated requests give the same bytes as alone
+        assert np.array_equal(reqs[mid][4], out_alone)
+        assert np.array_equal(reqs[mid + 1][4], dec_alone)
+        # everything against the oracle
+        for op, s, k, inp, out in reqs:
+            zz = T.sizes(s)
+            if op == "enc":
+                c, kk = oracle.kem_enc(s, keys[s][0][k], inp)
+                assert out[:zz.ct_bytes].tobytes() == c and out[zz.ct_bytes:].tobytes() == kk
+            else:
+                kk, fail = oracle.kem_dec(s, inp, keys[s][1][k])
+                assert out.tobytes() == kk and fail == 0
+    finally:
+        srv.close()
+
+
+def test_memory_admission_and_loadgen(kem):
+    T, ctx = kem
+    # a budget that holds two slots of 256 requests, while four were asked for
+    one_slot = 256 * (1472 + 1504 + 3040 + 4 + 16 * 416 + 768 + 64 + 64 + 1 + 32) + 64 * 256
+    srv = T.Server(max_batch=256, slots=4, mem_budget=2 * one_slot + 1000)
+    try:
+        assert srv.stats()["slots"] == 2
+        ids = []
+        for s in SETS:
+            pk, sk = _keys(T, ctx, s, 16, 300 + s)
+            ids.append(srv.add_keys(s, pk, sk))
+        n = srv.loadgen(rate=20000.0, seconds=0.5, seed=9, key_ids=np.concatenate(ids),
+                        decaps_fraction=0.5)
+        st = srv.stats()
+        assert n > 5000 and st["completed"] == n and st["failed"] == 0
+        assert st["p99_us"] >= st["p50_us"] > 0
+    finally:
+        srv.close()
