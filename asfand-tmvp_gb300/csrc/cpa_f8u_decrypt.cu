@@ -1,8 +1,34 @@
-// cpa_f8u_decrypt.cu — instantiates the IND-CPA kernel for form kFp8Tcgen05
-// (tcgen05 tensor cores), op kDecrypt (template in cpa_impl.cuh / cpa_tc_kernel.cuh;
-// one translation unit per pair so that they compile in parallel).
+// cpa_f8u_decrypt.cu — op kDecrypt on the tcgen05 tensor cores, in one of two launch
+// shapes picked per (op, parameter set) by the autotuner: one CTA per
+// instance (cpa_tc_kernel.cuh), or the persistent pipelined kernel
+// (cpa_persist.cuh), which also runs mixed tables of groups.  One translation
+// unit per op so that they compile in parallel.
 #include "cpa_impl.cuh"
+#include "cpa_persist.cuh"
+
+#include <cstring>
 
 namespace tmvp {
-int cpa_launch_f8u_decrypt(const CpaArgs &a, cudaStream_t s) { return launch_op<kFp8Tcgen05, kDecrypt>(a, s); }
+int cpa_launch_f8u_decrypt(const CpaArgs &a, cudaStream_t s) {
+  const int mode = persist_ctas_per_sm(kDecrypt, a.P.set);
+  if (mode < 0) return launch_op<kFp8Tcgen05, kDecrypt>(a, s);  // one CTA per instance
+  return launch_persist<kDecrypt>(&a, 1, nullptr, s, mode);
+}
+int cpa_launch_mixed_decrypt(const CpaArgs *g, int ng, const MixTable *dev_tab, cudaStream_t s, int ctas_per_sm) {
+  if (ng < 1 || ng > kMaxGroups) return (int)cudaErrorInvalidValue;
+  return launch_persist<kDecrypt>(g, ng, dev_tab, s, ctas_per_sm);
+}
+
+size_t mix_table_bytes() { return sizeof(MixTable); }
+
+void mix_table_build(void *host_dst, const CpaArgs *g, int ng) {
+  MixTable *T = static_cast<MixTable *>(host_dst);
+  std::memset(T, 0, sizeof(MixTable));
+  T->first[0] = 0;
+  for (int i = 0; i < ng && i < kMaxGroups; i++) {
+    T->g[i] = g[i];
+    T->first[i + 1] = T->first[i] + g[i].n;
+  }
+}
+static_assert(kMaxGroups == kMixMaxGroups, "one group limit");
 }  // namespace tmvp

@@ -46,8 +46,26 @@ struct CpaArgs {
   int *err;           // set when a secret coefficient is outside the form's range
 };
 
-// Launch over a.n instances (one CTA each) on `stream`.  Returns a CUDA error
-// code (0 on success).
+// Launch over a.n instances on `stream`.  Returns a CUDA error code (0 on
+// success).
 int cpa_launch(int form, int op, const CpaArgs &a, void *stream);
+
+// tcgen05 form only: one persistent launch over `ngroups` (<= kMixMaxGroups)
+// groups of instances, each with its own parameter set and buffers.  groups:
+// host copies; dev_tab: the same groups as a device table (mix_table_build
+// into mix_table_bytes() of device memory; unused when ngroups == 1).
+// ctas_per_sm = 0 takes as many CTAs per SM as fit.
+constexpr int kMixMaxGroups = 64;
+struct MixTable;
+size_t mix_table_bytes();
+void mix_table_build(void *host_dst, const CpaArgs *groups, int ngroups);
+int cpa_launch_mixed(int op, const CpaArgs *groups, int ngroups, const MixTable *dev_tab, void *stream,
+                     int ctas_per_sm);
+
+// Launch shape of the tcgen05 kernels per (op, parameter set): -1 = one CTA
+// per instance; n >= 0 = the persistent kernel with n CTAs per SM (0 = as many
+// as fit).  Default -1; written by the autotuner.
+int persist_ctas_per_sm(int op, int set);
+void persist_set_ctas_per_sm(int op, int set, int ctas);
 
 }  // namespace tmvp

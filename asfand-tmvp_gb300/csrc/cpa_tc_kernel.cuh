@@ -143,7 +143,25 @@ __global__ void __launch_bounds__(128, (Q >= 4 ? 3 : 4)) k_cpa_tc(CpaArgs a, TcL
   uint32_t *sencw = reinterpret_cast<uint32_t *>(sm + lo.senc);
   {
     bool ok = true;
-    for (int w = tid; w < L * 64; w += C::NT) {
+    const bool packed13 = OP == kDecrypt && !P.sable;  // 13-bit two's complement (SABER pack.cu:53-84)
+    if (packed13) {
+      const uint32_t m = ((1u << P.eq) - 1u) * 0x10001u;
+      for (int g8 = tid; g8 < L * 32; g8 += C::NT) {
+        uint32_t X[4];
+        unpack8(sm + lo.raw_sk, g8 * P.eq, P.eq, X);
+        // in range when (v + 128) mod 2^eq < 256; the low byte is then the value
+        uint32_t bad = 0;
+#pragma unroll
+        for (int i = 0; i < 4; i++) bad |= ((X[i] + 0x00800080u) & m) & 0xFF00FF00u;
+        const uint32_t s0 = __byte_perm(X[0], X[1], 0x6420), s1 = __byte_perm(X[2], X[3], 0x6420);
+        ok = ok && bad == 0u && small4(s0) && small4(s1);
+        sec8w[2 * g8] = s0;
+        sec8w[2 * g8 + 1] = s1;
+        sencw[2 * g8] = enc4<FORM>(s0);
+        sencw[2 * g8 + 1] = enc4<FORM>(s1);
+      }
+    }
+    for (int w = packed13 ? L * 64 : tid; w < L * 64; w += C::NT) {
       uint32_t sb;  // four signed bytes
       if (OP == kMatvec) {
         sb = *reinterpret_cast<const uint32_t *>(a.mv_s + (size_t)inst * (L * 256) + 4 * w);
@@ -212,7 +230,7 @@ __global__ void __launch_bounds__(128, (Q >= 4 ? 3 : 4)) k_cpa_tc(CpaArgs a, TcL
     // zero the padding columns ncols..N-1 (16 bytes = one K chunk of a column)
     const int padc = NU - ncols;
     for (int idx = tid; idx < L * padc * 16; idx += C::NT) {
-      const int j = idx / (padc * 16), r = idx % (padc * 16), n = ncols + r / 16, ac = r % 16;
+      const int j = idx / (padc * 16), r = idx % (padc * 16), n = ncols + r % padc, ac = r / padc;
       *reinterpret_cast<uint4 *>(umma_b + j * 256 * NU + ac * 16 * NU + (n >> 3) * 128 + (n & 7) * 16) =
           make_uint4(0u, 0u, 0u, 0u);
     }
@@ -264,27 +282,32 @@ __global__ void __launch_bounds__(128, (Q >= 4 ? 3 : 4)) k_cpa_tc(CpaArgs a, TcL
     tc_fence_after();
     const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(sm + lo.bar + 8);
     if (tid == 0) {
+      // descriptors differ only in the start address field (16-byte units)
       constexpr uint32_t idesc = umma_idesc_e4m3(NU);
-      const uint32_t h0 = smem_u32(umma_h), b0 = smem_u32(umma_b);
-#pragma unroll 1
+      const uint64_t ad0 = umma_desc(smem_u32(umma_h), 256, 128);
+      const uint64_t bd0 = umma_desc(smem_u32(umma_b), 16 * NU, 128);
+#pragma unroll
       for (int j = 0; j < L; j++) {
 #pragma unroll
         for (int ks = 0; ks < 8; ks++) {
-          const uint64_t bd = umma_desc(b0 + j * 256 * NU + 2 * ks * 16 * NU, 16 * NU, 128);
+          const uint64_t bd = bd0 + (uint64_t)((j * 256 * NU + 2 * ks * 16 * NU) >> 4);
 #pragma unroll
           for (int hh = 0; hh < 2; hh++) {
-            const uint64_t ad = umma_desc(h0 + j * kHankelBytes + (16 * hh + 4 * ks) * 128, 256, 128);
+            const uint64_t ad = ad0 + (uint64_t)((j * kHankelBytes + (16 * hh + 4 * ks) * 128) >> 4);
             umma_f8(tmem + hh * NU, ad, bd, idesc, (j | ks) != 0);
           }
         }
       }
       umma_commit(mbar);
     }
-    const bool done = mbar_wait_bounded(mbar, 0);
+    // one warp polls; the others wait in the barrier
+    const int warp = tid >> 5, lane = tid & 31;
+    bool done = true;
+    if (warp == 0) done = mbar_wait_bounded(mbar, 0);
+    done = __syncthreads_and(done) != 0;
     tc_fence_after();
     int *acc = reinterpret_cast<int *>(sm + lo.eng);
-    const int warp = tid >> 5, lane = tid & 31;
-    if (__all_sync(0xffffffffu, done)) {
+    if (done) {
 #pragma unroll
       for (int hh = 0; hh < 2; hh++) {
 #pragma unroll
@@ -296,7 +319,7 @@ __global__ void __launch_bounds__(128, (Q >= 4 ? 3 : 4)) k_cpa_tc(CpaArgs a, TcL
           for (int c = 0; c < 16; c++) acc[(cc + c) * 256 + row] = __float2int_rn(__uint_as_float(r[c]));
         }
       }
-    } else if (lane == 0 && a.err) {
+    } else if (tid == 0 && a.err) {
       atomicOr(a.err, 2);  // the tensor core did not signal completion in time
     }
     tc_fence_before();

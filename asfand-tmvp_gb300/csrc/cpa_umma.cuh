@@ -184,18 +184,27 @@ __device__ __forceinline__ void stage_ext(uint32_t *ext, const uint32_t *S, int 
 
 // The Hankel core matrices of every j < L (H: kHankelBytes per polynomial):
 // row i of core m is s_ext[8m + i .. 8m + i + 15], so row x = 8m + i sits at
-// byte 16x.
+// byte 16x.  Rows x = 4q + sh (q = 0..123) with the same byte shift sh are
+// windows of consecutive words, so a thread makes a run of rows from a
+// sliding window of ext words: one word load and four byte permutes per row.
 __device__ __forceinline__ void stage_hankel(uint8_t *H, const uint32_t *ext, int L, int tid,
                                              int nthreads) {
-  for (int idx = tid; idx < L * kHankelCores * 8; idx += nthreads) {
-    const int j = idx / (kHankelCores * 8), x = idx % (kHankelCores * 8);
-    const uint32_t *e = ext + 128 * j + (x >> 2);
-    const int sh = x & 3;
-    const uint32_t sel = (uint32_t)(sh | ((sh + 1) << 4) | ((sh + 2) << 8) | ((sh + 3) << 12));
-    const uint32_t e0 = e[0], e1 = e[1], e2 = e[2], e3 = e[3], e4 = e[4];
-    *reinterpret_cast<uint4 *>(H + (size_t)j * kHankelBytes + 16 * x) =
-        make_uint4(__byte_perm(e0, e1, sel), __byte_perm(e1, e2, sel), __byte_perm(e2, e3, sel),
-                   __byte_perm(e3, e4, sel));
+  const int groups = nthreads >> 2;            // threads per shift class
+  const int run = (124 + groups - 1) / groups;  // rows per thread and polynomial
+  const int sh = tid & 3, q0 = (tid >> 2) * run;
+  const uint32_t sel = (uint32_t)(sh | ((sh + 1) << 4) | ((sh + 2) << 8) | ((sh + 3) << 12));
+  for (int j = 0; j < L; j++) {
+    const uint32_t *e = ext + 128 * j;
+    uint8_t *hj = H + (size_t)j * kHankelBytes;
+    if (q0 >= 124) continue;
+    uint32_t w0 = e[q0], w1 = e[q0 + 1], w2 = e[q0 + 2], w3 = e[q0 + 3];
+    for (int q = q0; q < q0 + run && q < 124; q++) {
+      const uint32_t w4 = e[q + 4];
+      *reinterpret_cast<uint4 *>(hj + 16 * (4 * q + sh)) =
+          make_uint4(__byte_perm(w0, w1, sel), __byte_perm(w1, w2, sel), __byte_perm(w2, w3, sel),
+                     __byte_perm(w3, w4, sel));
+      w0 = w1; w1 = w2; w2 = w3; w3 = w4;
+    }
   }
 }
 

@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <utility>
@@ -864,3 +865,349 @@ void SABLE_dec(uint8_t *h_c, uint8_t *h_pk, uint8_t *h_sk, uint8_t *h_k, int mod
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Launch shapes, the autotuner, mixed-parameter decapsulation and its graphs
+// ---------------------------------------------------------------------------
+namespace {
+
+// Workspace of one mixed decapsulation pass over `gr` (per-group regions).
+size_t mixed_ws_bytes(size_t ng, const tmvp_dec_group *gr) {
+  size_t need = 0;
+  for (size_t g = 0; g < ng; g++) {
+    KemParams P;
+    make_params(gr[g].set, &P);
+    const size_t n = gr[g].n;
+    need += up(n * P.gm_bytes) + up(n * P.gs_bytes) + 2 * up(n * 64) + up(n) + up(n * 32);
+  }
+  return need;
+}
+
+int mixed_check(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr) {
+  if (!c || !gr || ng == 0 || ng > (size_t)kMixMaxGroups) return TMVP_EINVAL;
+  for (size_t g = 0; g < ng; g++) {
+    KemParams P;
+    if (!make_params(gr[g].set, &P) || gr[g].n == 0 || gr[g].n > (size_t)(INT_MAX / 4)) return TMVP_EINVAL;
+    const void *bufs[3] = {gr[g].ss, gr[g].ct, gr[g].sk};
+    for (const void *p : bufs)
+      if (!p || ((uintptr_t)p & 15) || !is_device_ptr(p, c->device)) return TMVP_EINVAL;
+  }
+  return TMVP_OK;
+}
+
+// Enqueues one mixed decapsulation pass on s: per-group Keccak stages on the
+// side stream and s, and one persistent tcgen05 launch per CPA step over all
+// groups.  ws: mixed_ws_bytes of device memory; tabs: two device group tables
+// (decryption, re-encryption).  Makes no allocation and no host
+// synchronisation, so it can be captured into a graph.
+int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws, uint8_t *tabs,
+                  std::vector<uint8_t> &host_tabs, bool upload_tabs, cudaStream_t s) {
+  std::vector<CpaArgs> ga(ng), gb(ng);
+  std::vector<KemParams> P(ng);
+  Arena A{ws};
+  std::vector<uint8_t *> a_stream(ng), s_stream(ng), mbuf(ng), kr(ng), fail(ng), hc(ng);
+  for (size_t g = 0; g < ng; g++) {
+    make_params(gr[g].set, &P[g]);
+    const size_t n = gr[g].n;
+    a_stream[g] = A.take(n * P[g].gm_bytes);
+    s_stream[g] = A.take(n * P[g].gs_bytes);
+    mbuf[g] = A.take(n * 64);
+    kr[g] = A.take(n * 64);
+    fail[g] = A.take(n);
+    hc[g] = A.take(n * 32);
+  }
+  TRY_CUDA(cudaEventRecord(c->fork_ev, s));
+  TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+  for (size_t g = 0; g < ng; g++) {
+    k_dec_front<<<blocks_for(2 * gr[g].n, 128), 128, 0, c->side>>>(P[g], gr[g].sk, gr[g].ct, a_stream[g], hc[g],
+                                                                    (int)gr[g].n);
+    c->launches++;
+  }
+  TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
+  int shape_dec = 0, shape_re = 0;
+  for (size_t g = 0; g < ng; g++) {
+    CpaArgs &a = ga[g];
+    a = CpaArgs{};
+    a.P = P[g];
+    a.n = (int)gr[g].n;
+    a.ct = gr[g].ct;
+    a.sk = gr[g].sk;
+    a.m_out = mbuf[g];
+    a.m_out_stride = 64;
+    a.copy_hpk = 1;
+    a.err = c->d_err;
+    CpaArgs &b = gb[g];
+    b = CpaArgs{};
+    b.P = P[g];
+    b.n = (int)gr[g].n;
+    b.a_stream = a_stream[g];
+    b.s_stream = s_stream[g];
+    b.pk = gr[g].sk;
+    b.pk_stride = P[g].sk_bytes;
+    b.pk_off = P[g].indcpa_sk_bytes;
+    b.msg = mbuf[g];
+    b.msg_stride = 64;
+    b.ct = gr[g].ct;
+    b.fail = fail[g];
+    b.err = c->d_err;
+    shape_dec = std::max(shape_dec, persist_ctas_per_sm(kDecrypt, P[g].set));
+    shape_re = std::max(shape_re, persist_ctas_per_sm(kReenc, P[g].set));
+  }
+  const size_t tb = mix_table_bytes();
+  host_tabs.assign(2 * tb, 0);
+  mix_table_build(host_tabs.data(), ga.data(), (int)ng);
+  mix_table_build(host_tabs.data() + tb, gb.data(), (int)ng);
+  // (pageable source: the call returns once the bytes are staged)
+  if (upload_tabs) TRY_CUDA(cudaMemcpyAsync(tabs, host_tabs.data(), 2 * tb, cudaMemcpyHostToDevice, s));
+  const MixTable *tdec = reinterpret_cast<const MixTable *>(tabs);
+  const MixTable *tre = reinterpret_cast<const MixTable *>(tabs + tb);
+  if (cpa_launch_mixed(kDecrypt, ga.data(), (int)ng, tdec, s, shape_dec) != 0) return TMVP_EDEVICE;
+  c->launches++;
+  for (size_t g = 0; g < ng; g++) {
+    k_dec_g<<<blocks_for(gr[g].n, 128), 128, 0, s>>>(P[g], mbuf[g], kr[g], s_stream[g], (int)gr[g].n);
+    c->launches++;
+  }
+  TRY_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));  // join
+  if (cpa_launch_mixed(kReenc, gb.data(), (int)ng, tre, s, shape_re) != 0) return TMVP_EDEVICE;
+  c->launches++;
+  for (size_t g = 0; g < ng; g++) {
+    k_final_key<<<blocks_for(gr[g].n, 128), 128, 0, s>>>(P[g], gr[g].ct, hc[g], kr[g], fail[g], gr[g].sk, gr[g].ss,
+                                                         (int)gr[g].n);
+    c->launches++;
+  }
+  TRY_CUDA(cudaGetLastError());
+  return TMVP_OK;
+}
+
+}  // namespace
+
+struct tmvp_mixed_plan {
+  tmvp_ctx *c = nullptr;
+  uint8_t *ws = nullptr, *tabs = nullptr;
+  std::vector<uint8_t> host_tabs;  // pageable: copied into the graph's memcpy node at capture
+  cudaStream_t cs = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" {
+
+int tmvp_tune_set(int step, tmvp_param_set set, int shape) {
+  KemParams P;
+  if (step < 0 || step > 4 || !make_params(set, &P) || shape < -1 || shape > 64) return set_err(TMVP_EINVAL);
+  persist_set_ctas_per_sm(step, set, shape);
+  return set_err(TMVP_OK);
+}
+
+int tmvp_tune_get(int step, tmvp_param_set set) { return persist_ctas_per_sm(step, set); }
+
+int tmvp_ctx_sync_status(tmvp_ctx *c, void *stream) {
+  if (!c) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  return set_err(finish(c, (cudaStream_t)stream, true));
+}
+
+int tmvp_kem_dec_mixed(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, void *stream) {
+  int r = mixed_check(c, ng, gr);
+  if (r) return set_err(r);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  const size_t tb = up(mix_table_bytes());
+  if ((r = ensure_ws(c, mixed_ws_bytes(ng, gr) + 2 * tb))) return set_err(r);
+  std::vector<uint8_t> host_tabs;
+  uint8_t *tabs = c->ws + mixed_ws_bytes(ng, gr);
+  if ((r = mixed_enqueue(c, ng, gr, c->ws, tabs, host_tabs, true, (cudaStream_t)stream))) return set_err(r);
+  return set_err(TMVP_OK);
+}
+
+int tmvp_mixed_plan_create(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, tmvp_mixed_plan **out) {
+  if (!out) return set_err(TMVP_EINVAL);
+  *out = nullptr;
+  int r = mixed_check(c, ng, gr);
+  if (r) return set_err(r);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  tmvp_mixed_plan *p = new tmvp_mixed_plan();
+  p->c = c;
+  auto fail = [&](int code) {
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->cs) cudaStreamDestroy(p->cs);
+    if (p->ws) cudaFree(p->ws);
+    if (p->tabs) cudaFree(p->tabs);
+    delete p;
+    cudaGetLastError();
+    return set_err(code);
+  };
+  // the plan owns its workspace: the graph keeps these addresses
+  if (cudaMalloc(&p->ws, std::max<size_t>(mixed_ws_bytes(ng, gr), 256)) != cudaSuccess ||
+      cudaMalloc(&p->tabs, 2 * up(mix_table_bytes())) != cudaSuccess)
+    return fail(TMVP_ENOMEM);
+  if (cudaStreamCreateWithFlags(&p->cs, cudaStreamNonBlocking) != cudaSuccess) return fail(TMVP_EDEVICE);
+  // the group tables are fixed for the plan: the capture records no copy of
+  // them; they are written once, below, after the capture built them
+  if (cudaStreamBeginCapture(p->cs, cudaStreamCaptureModeRelaxed) != cudaSuccess) return fail(TMVP_EDEVICE);
+  r = mixed_enqueue(c, ng, gr, p->ws, p->tabs, p->host_tabs, false, p->cs);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(p->cs, &graph);
+  p->graph = graph;
+  if (r) return fail(r);
+  if (e != cudaSuccess || !graph) return fail(TMVP_EDEVICE);
+  if (cudaMemcpy(p->tabs, p->host_tabs.data(), p->host_tabs.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(TMVP_EDEVICE);
+  if (cudaGraphInstantiate(&p->exec, p->graph, 0) != cudaSuccess) return fail(TMVP_EDEVICE);
+  *out = p;
+  return set_err(TMVP_OK);
+}
+
+int tmvp_mixed_plan_launch(tmvp_mixed_plan *p, void *stream) {
+  if (!p) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(p->c->mu);
+  Guard g(p->c);
+  TRY_CUDA(cudaGraphLaunch(p->exec, (cudaStream_t)stream));
+  p->c->launches++;
+  return set_err(TMVP_OK);
+}
+
+void tmvp_mixed_plan_destroy(tmvp_mixed_plan *p) {
+  if (!p) return;
+  {
+    Guard g(p->c);
+    cudaDeviceSynchronize();
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->cs) cudaStreamDestroy(p->cs);
+    if (p->ws) cudaFree(p->ws);
+    if (p->tabs) cudaFree(p->tabs);
+  }
+  delete p;
+}
+
+}  // extern "C"
+
+namespace {
+
+uint64_t tune_splitmix(uint64_t &x) {
+  uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+struct DevBufs {
+  std::vector<void *> ptrs;
+  ~DevBufs() {
+    for (void *p : ptrs) cudaFree(p);
+  }
+  uint8_t *get(size_t bytes) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
+    ptrs.push_back(p);
+    return static_cast<uint8_t *>(p);
+  }
+};
+
+}  // namespace
+
+extern "C" int tmvp_autotune(tmvp_ctx *c, tmvp_param_set set, size_t n, int *shapes) {
+  KemParams P;
+  if (!c || !make_params(set, &P)) return set_err(TMVP_EINVAL);
+  n = std::min<size_t>(std::max<size_t>(n, 1024), 65536);
+  Guard g(c);
+  DevBufs B;
+  uint8_t *pk = B.get(n * P.pk_bytes), *sk = B.get(n * P.sk_bytes), *ct = B.get(n * P.ct_bytes);
+  uint8_t *ss = B.get(n * 32), *ss2 = B.get(n * 32), *coins = B.get(n * 96), *ecoins = B.get(n * 32);
+  uint8_t *mvA = B.get(n * P.l * P.l * 512), *mvs = B.get(n * P.l * 256), *mvo = B.get(n * P.l * 512);
+  if (!pk || !sk || !ct || !ss || !ss2 || !coins || !ecoins || !mvA || !mvs || !mvo) return set_err(TMVP_ENOMEM);
+  {
+    uint64_t st = 0x5eed0000ull + (uint64_t)set;
+    std::vector<uint8_t> h(n * 96);
+    for (auto &b : h) b = (uint8_t)tune_splitmix(st);
+    TRY_CUDA(cudaMemcpy(coins, h.data(), n * 96, cudaMemcpyHostToDevice));
+    TRY_CUDA(cudaMemcpy(ecoins, h.data() + n * 64, n * 32, cudaMemcpyHostToDevice));
+    std::vector<uint16_t> A((size_t)n * P.l * P.l * 256);
+    for (auto &v : A) v = (uint16_t)(tune_splitmix(st) & ((1u << P.eq) - 1u));
+    std::vector<int8_t> sv((size_t)n * P.l * 256);
+    for (auto &v : sv) v = (int8_t)((int)(tune_splitmix(st) % 9) - 4);
+    TRY_CUDA(cudaMemcpy(mvA, A.data(), A.size() * 2, cudaMemcpyHostToDevice));
+    TRY_CUDA(cudaMemcpy(mvs, sv.data(), sv.size(), cudaMemcpyHostToDevice));
+  }
+  cudaStream_t st = nullptr;
+  TRY_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamDestroy(s); }
+  } sg{st};
+  int r;
+  if ((r = tmvp_kem_keypair_batch(c, set, n, pk, sk, coins, TMVP_FORM_FP8_TCGEN05, st)) ||
+      (r = tmvp_kem_enc_batch(c, set, n, ct, ss, pk, ecoins, TMVP_FORM_FP8_TCGEN05, st)))
+    return set_err(r);
+  TRY_CUDA(cudaStreamSynchronize(st));
+  std::vector<uint8_t> want(n * 32), got(n * 32);
+  TRY_CUDA(cudaMemcpy(want.data(), ss, n * 32, cudaMemcpyDeviceToHost));
+
+  cudaEvent_t e0, e1;
+  TRY_CUDA(cudaEventCreate(&e0));
+  TRY_CUDA(cudaEventCreate(&e1));
+  struct EvGuard {
+    cudaEvent_t a, b;
+    ~EvGuard() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } eg{e0, e1};
+  // median-free but warm: one untimed call, then three timed
+  auto timed = [&](const std::function<int()> &fn, float &ms) -> int {
+    int rr = fn();
+    if (rr) return rr;
+    cudaEventRecord(e0, st);
+    for (int i = 0; i < 3 && !rr; i++) rr = fn();
+    cudaEventRecord(e1, st);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return TMVP_EDEVICE;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return rr;
+  };
+  const int cand[] = {-1, 0, 1, 2};
+  const int steps[] = {kDecrypt, kReenc, kEncrypt, kKeygen, kMatvec};
+  for (int step : steps) {
+    int best = persist_ctas_per_sm(step, set);
+    float best_ms = 1e30f;
+    for (int shape : cand) {
+      persist_set_ctas_per_sm(step, set, shape);
+      float ms = 0;
+      std::function<int()> fn;
+      if (step == kDecrypt || step == kReenc)
+        fn = [&] { return tmvp_kem_dec_batch(c, set, n, ss2, ct, sk, TMVP_FORM_FP8_TCGEN05, st); };
+      else if (step == kEncrypt)
+        fn = [&] { return tmvp_kem_enc_batch(c, set, n, ct, ss2, pk, ecoins, TMVP_FORM_FP8_TCGEN05, st); };
+      else if (step == kKeygen)
+        fn = [&] { return tmvp_kem_keypair_batch(c, set, n, pk, sk, coins, TMVP_FORM_FP8_TCGEN05, st); };
+      else
+        fn = [&] {
+          return tmvp_matvec_batch(c, n, P.l, P.eq, 0, reinterpret_cast<uint16_t *>(mvo),
+                                   reinterpret_cast<const uint16_t *>(mvA), reinterpret_cast<const int8_t *>(mvs),
+                                   TMVP_FORM_FP8_TCGEN05, st);
+        };
+      if ((r = timed(fn, ms))) {
+        persist_set_ctas_per_sm(step, set, best);
+        return set_err(r);
+      }
+      if (step != kMatvec) {
+        // every shape must give the same keys
+        TRY_CUDA(cudaMemcpy(got.data(), ss2, n * 32, cudaMemcpyDeviceToHost));
+        if (got != want) {
+          persist_set_ctas_per_sm(step, set, best);
+          return set_err(TMVP_EDEVICE);
+        }
+      }
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = shape;
+      }
+    }
+    persist_set_ctas_per_sm(step, set, best);
+    if (shapes) shapes[step] = best;
+  }
+  return set_err(TMVP_OK);
+}

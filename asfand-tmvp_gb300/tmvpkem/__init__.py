@@ -121,11 +121,71 @@ def lib(build_if_missing: bool = False):
     L.tmvp_server_reset_stats.restype = None
     L.tmvp_server_loadgen.argtypes = [P, ctypes.c_double, ctypes.c_double, ctypes.c_uint64, P, S,
                                       ctypes.c_double, ctypes.POINTER(ctypes.c_uint64)]
+    L.tmvp_tune_set.argtypes = [I, I, I]
+    L.tmvp_tune_get.argtypes = [I, I]
+    L.tmvp_autotune.argtypes = [P, I, S, ctypes.POINTER(ctypes.c_int)]
+    L.tmvp_ctx_sync_status.argtypes = [P, P]
+    L.tmvp_kem_dec_mixed.argtypes = [P, S, ctypes.POINTER(DecGroup), P]
+    L.tmvp_mixed_plan_create.argtypes = [P, S, ctypes.POINTER(DecGroup), ctypes.POINTER(P)]
+    L.tmvp_mixed_plan_launch.argtypes = [P, P]
+    L.tmvp_mixed_plan_destroy.argtypes = [P]
+    L.tmvp_mixed_plan_destroy.restype = None
     L.tmvp_ref_set_batch.argtypes = [I, S]
     L.tmvp_ref_batch.argtypes = [I]
     L.tmvp_ref_batch.restype = S
     _lib = L
     return L
+
+
+class DecGroup(ctypes.Structure):
+    _fields_ = [("set", ctypes.c_int), ("n", ctypes.c_size_t), ("ss", ctypes.c_void_p),
+                ("ct", ctypes.c_void_p), ("sk", ctypes.c_void_p)]
+
+
+STEP_DECRYPT, STEP_ENCRYPT, STEP_REENC, STEP_KEYGEN, STEP_MATVEC = range(5)
+
+
+def tune_set(step: int, set_id: int, shape: int):
+    """Launch shape of a tcgen05 IND-CPA step: -1 one CTA per instance, n >= 0
+    the persistent kernel with n CTAs per SM (0 = as many as fit)."""
+    _check(lib().tmvp_tune_set(step, set_id, shape), "tmvp_tune_set")
+
+
+def tune_get(step: int, set_id: int) -> int:
+    return lib().tmvp_tune_get(step, set_id)
+
+
+def _groups(groups):
+    arr = (DecGroup * len(groups))()
+    for i, (set_id, ss, ct, sk) in enumerate(groups):
+        arr[i] = DecGroup(set_id, ss.shape[0], _ptr(ss), _ptr(ct), _ptr(sk))
+    return arr
+
+
+class MixedPlan:
+    """A mixed-parameter decapsulation pass captured into a CUDA graph for
+    fixed device buffers (tmvp_mixed_plan)."""
+
+    def __init__(self, ctx, groups):
+        self._keep = groups
+        h = ctypes.c_void_p()
+        arr = _groups(groups)
+        _check(lib().tmvp_mixed_plan_create(ctx.h, len(groups), arr, ctypes.byref(h)), "tmvp_mixed_plan_create")
+        self.h = h
+
+    def launch(self, stream=None):
+        _check(lib().tmvp_mixed_plan_launch(self.h, stream), "tmvp_mixed_plan_launch")
+
+    def close(self):
+        if self.h:
+            lib().tmvp_mixed_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class ServerConfig(ctypes.Structure):
@@ -243,6 +303,19 @@ class Context:
     def matvec_ptr(self, n, l, eq, transpose, out, A, s, form=FORM_AUTO, stream=None):
         _check(lib().tmvp_matvec_batch(self.h, n, l, eq, int(transpose), _ptr(out), _ptr(A),
                                        _ptr(s), form, stream), "tmvp_matvec_batch")
+
+    def kem_dec_mixed(self, groups, stream=None):
+        """groups: [(set_id, ss, ct, sk)] of device tensors; one pass."""
+        arr = _groups(groups)
+        _check(lib().tmvp_kem_dec_mixed(self.h, len(groups), arr, stream), "tmvp_kem_dec_mixed")
+
+    def sync_status(self, stream=None):
+        _check(lib().tmvp_ctx_sync_status(self.h, stream), "tmvp_ctx_sync_status")
+
+    def autotune(self, set_id, n=16384) -> list:
+        shapes = (ctypes.c_int * 5)()
+        _check(lib().tmvp_autotune(self.h, set_id, n, shapes), "tmvp_autotune")
+        return list(shapes)
 
     # --- numpy conveniences (host buffers) ---------------------------------
     def kem_keypair(self, set_id, coins, form=FORM_AUTO):

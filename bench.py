@@ -193,6 +193,9 @@ def run_ours(args):
     ctx.kem_enc_ptr(SABER, n, ct, ss_ref, pk, ecoins, T.FORM_AUTO, sp)
     torch.cuda.synchronize()
 
+    # launch shapes for this workload, picked by the library's autotuner
+    tuned = {} if args.no_tune else {"saber": ctx.autotune(SABER, n)}
+
     def timed(form, steps, stage_timing=False):
         for _ in range(args.warmup):
             ctx.kem_dec_ptr(SABER, n, ss, ct, sk, form, sp)
@@ -291,6 +294,7 @@ def run_ours(args):
                    "batch": n, "param_set": "Saber", "form": "auto = fp8_tcgen05",
                    "l2": "inputs (222 MB) larger than L2; no flush", "parallelism": f"replicas x{ws}"},
         "forms": form_rates,
+        "launch_shapes": tuned,
         "tc_over_cuda_core": (value / ws / form_rates["cuda_core"]) if "cuda_core" in form_rates else None,
         "latency_ms": {"p50": float(np.percentile(per_ms, 50)), "p99": float(np.percentile(per_ms, 99)),
                        "batch": n},
@@ -407,6 +411,43 @@ def _workloads(ctx, T, dev, sp, stream, args):
                      "round_trips_per_s": nb / ((t_kp + t_en + t_de) / 1e3),
                      "bit_exact_round_trip": bool(torch.equal(ss1, ss2))}
     out["sable_l3_kem_65536"] = sab
+    # mixed batch: requests of LightSaber, Saber, FireSaber and Sable interleaved, each with a
+    # count drawn uniformly from 1..8192, decapsulated by one CUDA-graph replay
+    rng = np.random.default_rng(4242)
+    sets = [0, 1, 2, 4]
+    reqs = [(sets[i % 4], int(rng.integers(1, 8193))) for i in range(24)]
+    made, outs = [], []
+    for i, (sid, cnt) in enumerate(reqs):
+        z = T.sizes(sid)
+        cc = torch.from_numpy(T.splitmix_bytes(9000 + i, cnt * 96).reshape(cnt, 96)).to(dev)
+        ee = torch.from_numpy(T.splitmix_bytes(9500 + i, cnt * 32).reshape(cnt, 32)).to(dev)
+        pk_i = torch.empty((cnt, z.pk_bytes), dtype=torch.uint8, device=dev)
+        sk_i = torch.empty((cnt, z.sk_bytes), dtype=torch.uint8, device=dev)
+        ct_i = torch.empty((cnt, z.ct_bytes), dtype=torch.uint8, device=dev)
+        ss_i = torch.empty((cnt, 32), dtype=torch.uint8, device=dev)
+        ctx.kem_keypair_ptr(sid, cnt, pk_i, sk_i, cc, T.FORM_AUTO, sp)
+        ctx.kem_enc_ptr(sid, cnt, ct_i, ss_i, pk_i, ee, T.FORM_AUTO, sp)
+        made.append((sid, cnt, sk_i, ct_i, ss_i))
+        outs.append(torch.zeros_like(ss_i))
+    total = sum(c for _, c in reqs)
+    plan = T.MixedPlan(ctx, [(sid, outs[i], ct_i, sk_i) for i, (sid, _, sk_i, ct_i, _) in enumerate(made)])
+    try:
+        ms_graph = _event_ms(stream, lambda: plan.launch(sp), 5)
+    finally:
+        plan.close()
+    exact = all(torch.equal(outs[i], made[i][4]) for i in range(len(made)))
+
+    sep_out = [torch.empty_like(o) for o in outs]
+
+    def per_request():
+        for i, (sid, cnt, sk_i, ct_i, _) in enumerate(made):
+            ctx.kem_dec_ptr(sid, cnt, sep_out[i], ct_i, sk_i, T.FORM_AUTO, sp)
+    ms_sep = _event_ms(stream, per_request, 3)
+    out["mixed_graph"] = {"requests": len(reqs), "instances": total, "sets": "LightSaber, Saber, FireSaber, Sable",
+                          "decaps_per_s": total / (ms_graph / 1e3), "ms": ms_graph,
+                          "per_request_calls_decaps_per_s": total / (ms_sep / 1e3),
+                          "bit_exact": bool(exact),
+                          "launch": "one CUDA graph: per-request Keccak stages, one persistent tcgen05 launch per CPA step"}
     # serving loop: Poisson arrivals over LightSaber, Saber, FireSaber and Sable
     rate, secs = 200_000.0, 2.0
     srv = T.Server(device=dev.index or 0, max_batch=4096, slots=4, form=T.FORM_AUTO)
@@ -457,6 +498,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (e2e) leg")
     ap.add_argument("--no-oracle", action="store_true", help="skip the oracle sample check")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the matrix-vector, Sable and serving workloads")
     ap.add_argument("--forms", default="fp8_tc,int8_tc,cuda_core",

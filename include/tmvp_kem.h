@@ -204,6 +204,62 @@ int tmvp_server_loadgen(tmvp_server *srv, double rate, double seconds, uint64_t 
                         const uint32_t *key_ids, size_t nkeys, double decaps_fraction,
                         uint64_t *submitted);
 
+/* ---------------------------------------------------------------------------
+ * Launch shapes and the autotuner (FP8_TCGEN05 form).  No counterpart in the
+ * reference, whose kernels have fixed launch shapes (cuda_kernel.cu:140-163).
+ *
+ * Every IND-CPA step runs either as one CTA per instance (shape -1) or as the
+ * persistent, pipelined kernel with `shape` CTAs per SM (0 = as many as fit);
+ * the choice is kept per (step, parameter set), process-wide.
+ * tmvp_autotune times every shape of every step for `set` on n synthetic
+ * instances (key pairs and ciphertexts made with this library; every shape
+ * must decapsulate to the same keys), keeps the fastest and, if `shapes` is
+ * not NULL, writes them to shapes[5] (indexed by step).
+ * ------------------------------------------------------------------------- */
+enum {
+  TMVP_STEP_DECRYPT = 0,
+  TMVP_STEP_ENCRYPT = 1,
+  TMVP_STEP_REENC = 2,
+  TMVP_STEP_KEYGEN = 3,
+  TMVP_STEP_MATVEC = 4
+};
+int tmvp_tune_set(int step, tmvp_param_set set, int shape);
+int tmvp_tune_get(int step, tmvp_param_set set);
+int tmvp_autotune(tmvp_ctx *ctx, tmvp_param_set set, size_t n, int *shapes);
+
+/* Waits for `stream`, then reads and clears the context's device status:
+ * TMVP_EINVAL if a secret was outside the tensor-core range, TMVP_ETIMEOUT if
+ * a bounded device wait gave up, TMVP_OK otherwise.  For work launched without
+ * a host synchronisation (device buffers, graphs). */
+int tmvp_ctx_sync_status(tmvp_ctx *ctx, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Mixed-parameter decapsulation.  No counterpart in the reference (one
+ * parameter set per build, params.h:4).
+ *
+ * Up to 64 groups, each with its own parameter set (any of the six) and its
+ * own device buffers (16-byte aligned, this context's GPU), decapsulate in one
+ * pass: every IND-CPA step is ONE persistent tcgen05 launch over all groups;
+ * the Keccak stages run per group on two streams.  tmvp_mixed_plan_create
+ * captures the pass for fixed buffers into a CUDA graph (the plan owns its
+ * workspace); tmvp_mixed_plan_launch replays it, so the caller refills the
+ * ciphertext / key buffers and relaunches.  Asynchronous on `stream`; use
+ * tmvp_ctx_sync_status for the device status.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  tmvp_param_set set;
+  size_t n;
+  uint8_t *ss;        /* [n][32]       */
+  const uint8_t *ct;  /* [n][ct_bytes] */
+  const uint8_t *sk;  /* [n][sk_bytes] */
+} tmvp_dec_group;
+int tmvp_kem_dec_mixed(tmvp_ctx *ctx, size_t ngroups, const tmvp_dec_group *groups, void *stream);
+typedef struct tmvp_mixed_plan tmvp_mixed_plan;
+int tmvp_mixed_plan_create(tmvp_ctx *ctx, size_t ngroups, const tmvp_dec_group *groups,
+                           tmvp_mixed_plan **out);
+int tmvp_mixed_plan_launch(tmvp_mixed_plan *plan, void *stream);
+void tmvp_mixed_plan_destroy(tmvp_mixed_plan *plan);
+
 /* Decapsulation that allocates nothing.  No counterpart in the reference.
  * For callers that cannot call cudaMalloc: a host whose GPU memory is owned
  * by its own pool allocator, a serving process that forbids allocation after
