@@ -1,0 +1,466 @@
+// cpa5i.cuh — the tcgen05 IND-CPA kernel specialised per parameter set: one
+// CTA of 128 threads per instance, with every width, count and offset a
+// compile-time constant.
+//
+// Per instance:
+//   1. the packed inputs arrive by TMA bulk copies (cp.async.bulk) issued by
+//      one thread, counted on an mbarrier;
+//   2. secrets (CBD or unpacked), radix-16 e4m3 digit columns with K
+//      reversed, s_ext and the Hankel core matrices (cpa_umma.cuh);
+//   3. one thread issues the 16 l tcgen05.mma (M = 128, N = 16 / 32, K = 32)
+//      into tensor memory and commits them to an mbarrier;
+//   4. accumulators -> int32 columns (tcgen05.ld) -> the rounding / packing /
+//      compare / decode epilogue, eight coefficients at a time.
+// Same results as the runtime-shaped kernels (cpa_tc_kernel.cuh,
+// cpa_persist.cuh); the arithmetic per instance is the same.
+#pragma once
+#include <cstdint>
+
+#include "cpa_persist.cuh"
+
+namespace tmvp {
+
+// l, log2 q, log2 p, log2 T, mu, Sable (same table as make_params)
+constexpr int kSetTab[6][6] = {{2, 13, 10, 3, 10, 0}, {3, 13, 10, 4, 8, 0}, {4, 13, 10, 6, 6, 0},
+                               {2, 11, 9, 3, 2, 1},   {3, 11, 9, 5, 2, 1},  {4, 11, 10, 3, 2, 1}};
+
+template <int SET>
+struct SetC {
+  static constexpr int L = kSetTab[SET][0], EQ = kSetTab[SET][1], EP = kSetTab[SET][2], ET = kSetTab[SET][3];
+  static constexpr int MU = kSetTab[SET][4], SABLE = kSetTab[SET][5];
+  static constexpr int POLYBYTES = EQ * 32, POLYCOMP = EP * 32, SCALE = ET * 32, COIN = MU * 32;
+  static constexpr int PK = L * POLYCOMP + 32, INDCPA_SK = SABLE ? L * 64 : L * POLYBYTES;
+  static constexpr int SK = INDCPA_SK + PK + 64, CT = L * POLYCOMP + SCALE;
+  static constexpr int GM = L * L * POLYBYTES, GS = L * COIN;
+  static constexpr int H1 = 1 << (EQ - EP - 1);
+  static constexpr int H2 = (1 << (EP - 2)) - (1 << (EP - ET - 1)) + (1 << (EQ - EP - 1));
+};
+
+template <int OP, int SET>
+struct ShapeC {
+  using C = SetC<SET>;
+  static constexpr int L = C::L;
+  static constexpr int R = OP == kDecrypt ? 1 : (OP == kKeygen ? L : L + 1);
+  static constexpr int RA = OP == kDecrypt ? 0 : L;
+  static constexpr int WA = C::EQ, WB = C::EP;
+  static constexpr int DA = (WA + 3) / 4, DB = (WB + 3) / 4;
+  static constexpr int NCOLS = RA * DA + (R - RA) * DB;
+  static constexpr int NU = NCOLS <= 16 ? 16 : 32;
+  static constexpr int TMEM_COLS = NU <= 16 ? 32 : 64;
+  static constexpr int col_base(int p) { return p < RA ? p * DA : RA * DA + (p - RA) * DB; }
+  static constexpr int digits(int p) { return p < RA ? DA : DB; }
+};
+
+constexpr int al16c(int x) { return (x + 15) & ~15; }
+
+// Shared-memory layout of one CTA (byte offsets; -1 = absent).
+template <int OP, int SET>
+struct LayoutC {
+  using C = SetC<SET>;
+  using S = ShapeC<OP, SET>;
+  static constexpr bool HAS_AS = OP == kEncrypt || OP == kReenc || OP == kKeygen;
+  static constexpr bool HAS_B = OP == kEncrypt || OP == kReenc;
+  static constexpr bool HAS_CT = OP == kReenc || OP == kDecrypt;
+  static constexpr bool HAS_SK = OP == kDecrypt;
+  static constexpr int A = 0;
+  static constexpr int SS = HAS_AS ? al16c(A + C::GM + 16) : A;
+  static constexpr int B = HAS_AS ? al16c(SS + C::GS + 16) : SS;
+  static constexpr int MSG = HAS_B ? al16c(B + C::L * C::POLYCOMP + 16) : B;
+  static constexpr int CTO = HAS_B ? al16c(MSG + 32 + 16) : MSG;
+  static constexpr int SKO = HAS_CT ? al16c(CTO + C::CT + 16) : CTO;
+  static constexpr int SEC8 = HAS_SK ? al16c(SKO + C::INDCPA_SK + 16) : SKO;
+  static constexpr int SENC = al16c(SEC8 + C::L * 256);
+  static constexpr int ENG = al16c(SENC + C::L * 256);
+  static constexpr int ENG_BYTES = (C::L * (kHankelBytes + 256 * S::NU + 512) > S::NU * 1024)
+                                       ? C::L * (kHankelBytes + 256 * S::NU + 512)
+                                       : S::NU * 1024;
+  static constexpr int OUT = al16c(ENG + ENG_BYTES);
+  static constexpr int OUT_BYTES = OP == kEncrypt ? C::CT + 16
+                                   : (OP == kKeygen ? C::L * C::POLYCOMP + C::INDCPA_SK + 16 : 0);
+  static constexpr int BAR = al16c(OUT + OUT_BYTES);  // mbarriers in, mma; TMEM base
+  static constexpr int TOTAL = BAR + 32;
+  static constexpr int IN_BYTES = (HAS_AS ? C::GM + C::GS : 0) + (HAS_B ? C::L * C::POLYCOMP + 32 : 0) +
+                                  (HAS_CT ? C::CT : 0) + (HAS_SK ? C::INDCPA_SK : 0);
+};
+
+// Eight W-bit little-endian fields from byte `byte0` (16 bytes of slack after
+// the stream), as four words of two 16-bit lanes.
+template <int W>
+__device__ __forceinline__ void unpack8c(const uint8_t *base, int byte0, uint32_t (&X)[4]) {
+  const uint32_t *wp = reinterpret_cast<const uint32_t *>(base + (byte0 & ~3));
+  const int sh = 8 * (byte0 & 3);
+  uint32_t q[5];
+#pragma unroll
+  for (int i = 0; i < 5; i++) q[i] = wp[i];
+  uint32_t a[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) a[i] = __funnelshift_r(q[i], q[i + 1], sh);
+  constexpr uint32_t m = (1u << W) - 1u;
+#pragma unroll
+  for (int k = 0; k < 8; k += 2) {
+    const int b0 = k * W, b1 = (k + 1) * W;
+    const uint32_t v0 = __funnelshift_r(a[b0 >> 5], a[(b0 >> 5) + 1 < 4 ? (b0 >> 5) + 1 : 3], b0 & 31) & m;
+    const uint32_t v1 = __funnelshift_r(a[b1 >> 5], a[(b1 >> 5) + 1 < 4 ? (b1 >> 5) + 1 : 3], b1 & 31) & m;
+    X[k >> 1] = __byte_perm(v0, v1, 0x5410);
+  }
+}
+
+template <int OP, int SET>
+__global__ void __launch_bounds__(128, 4) k_cpa5i(CpaArgs a) {
+  using C = SetC<SET>;
+  using S = ShapeC<OP, SET>;
+  using LO = LayoutC<OP, SET>;
+  constexpr int L = C::L, NU = S::NU, NT = 128;
+  extern __shared__ __align__(16) uint8_t sm[];
+  const unsigned inst = blockIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t mbar_in = smem_u32(sm + LO::BAR), mbar_mma = mbar_in + 8;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + LO::BAR + 16);
+
+  // 0. tensor memory, barriers, and the input copies (one thread)
+  if (warp == 0) tmem_alloc(smem_u32(tmem_slot), S::TMEM_COLS);
+  if (tid == 0) {
+    mbar_init(mbar_in, 1);
+    mbar_init(mbar_mma, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    const uint32_t d = smem_u32(sm);
+    mbar_expect_tx(mbar_in, LO::IN_BYTES);
+    if (LO::HAS_AS) {
+      bulk_g2s(d + LO::A, a.a_stream + (size_t)inst * C::GM, C::GM, mbar_in);
+      bulk_g2s(d + LO::SS, a.s_stream + (size_t)inst * C::GS, C::GS, mbar_in);
+    }
+    if (LO::HAS_B) {
+      bulk_g2s(d + LO::B, a.pk + (size_t)inst * a.pk_stride + a.pk_off, C::L * C::POLYCOMP, mbar_in);
+      bulk_g2s(d + LO::MSG, a.msg + (size_t)inst * a.msg_stride, 32, mbar_in);
+    }
+    if (LO::HAS_CT) bulk_g2s(d + LO::CTO, a.ct + (size_t)inst * C::CT, C::CT, mbar_in);
+    if (LO::HAS_SK) bulk_g2s(d + LO::SKO, a.sk + (size_t)inst * C::SK, C::INDCPA_SK, mbar_in);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(tmem_slot);
+  bool ready = true;
+  if (warp == 0) ready = mbar_wait_bounded(mbar_in, 0);
+  ready = __syncthreads_and(ready) != 0;
+
+  uint32_t *sec8w = reinterpret_cast<uint32_t *>(sm + LO::SEC8);
+  uint32_t *sencw = reinterpret_cast<uint32_t *>(sm + LO::SENC);
+  uint8_t *H = sm + LO::ENG, *Bm = H + L * kHankelBytes;
+  uint32_t *ext = reinterpret_cast<uint32_t *>(Bm + L * 256 * NU);
+  int *acc = reinterpret_cast<int *>(sm + LO::ENG);
+  bool ok = true, done = false;
+  if (ready) {
+    // 1. secrets
+    if (OP == kDecrypt && !C::SABLE) {
+      // 13-bit two's complement (SABER pack.cu:53-84), eight coefficients at a time
+      constexpr uint32_t m = ((1u << C::EQ) - 1u) * 0x10001u;
+      for (int g8 = tid; g8 < L * 32; g8 += NT) {
+        uint32_t X[4];
+        unpack8c<C::EQ>(sm + LO::SKO, g8 * C::EQ, X);
+        uint32_t bad = 0;
+#pragma unroll
+        for (int i = 0; i < 4; i++) bad |= ((X[i] + 0x00800080u) & m) & 0xFF00FF00u;
+        const uint32_t s0 = __byte_perm(X[0], X[1], 0x6420), s1 = __byte_perm(X[2], X[3], 0x6420);
+        ok = ok && bad == 0u && small4(s0) && small4(s1);
+        sec8w[2 * g8] = s0;
+        sec8w[2 * g8 + 1] = s1;
+        sencw[2 * g8] = enc4<kFp8Tcgen05>(s0);
+        sencw[2 * g8 + 1] = enc4<kFp8Tcgen05>(s1);
+      }
+    } else {
+      for (int w = tid; w < L * 64; w += NT) {
+        uint32_t sb;
+        if (OP == kDecrypt) {
+          // 2-bit two's complement (SABLE pack.cu:371-376): one byte = 4 coefficients
+          const uint32_t x = sm[LO::SKO + w];
+          const uint32_t spread = (x & 3u) | ((x & 0xcu) << 6) | ((x & 0x30u) << 12) | ((x & 0xc0u) << 18);
+          sb = spread | (((spread >> 1) & 0x01010101u) * 0xfcu);
+        } else if (C::MU == 8) {
+          // CBD mu = 8 (SABER poly.cu:864-887)
+          const uint32_t x = *reinterpret_cast<const uint32_t *>(sm + LO::SS + 4 * w);
+          uint32_t n = x - ((x >> 1) & 0x55555555u);
+          n = (n & 0x33333333u) + ((n >> 2) & 0x33333333u);
+          sb = __vsub4(n & 0x0f0f0f0fu, (n >> 4) & 0x0f0f0f0fu);
+        } else if (C::MU == 2) {
+          // CBD mu = 2 (SABLE fips202.cu:625-651)
+          const uint32_t x = sm[LO::SS + w];
+          const uint32_t spread = (x & 3u) | ((x & 0xcu) << 6) | ((x & 0x30u) << 12) | ((x & 0xc0u) << 18);
+          sb = __vsub4(spread & 0x01010101u, (spread >> 1) & 0x01010101u);
+        } else {
+          // CBD mu = 6, 10: fields of mu bits, popcount halves
+          uint32_t r = 0;
+#pragma unroll
+          for (int b = 0; b < 4; b++) {
+            const uint32_t x = get_bits(sm + LO::SS, (4 * w + b) * C::MU, C::MU);
+            const int v = __popc(x & ((1u << (C::MU / 2)) - 1u)) - __popc(x >> (C::MU / 2));
+            r |= ((uint32_t)v & 0xffu) << (8 * b);
+          }
+          sb = r;
+        }
+        ok = ok && small4(sb);
+        sec8w[w] = sb;
+        sencw[w] = enc4<kFp8Tcgen05>(sb);
+      }
+    }
+    // 2. digit columns (K reversed, core-matrix order), then the zero columns
+    for (int idx = tid; idx < S::R * L * 32; idx += NT) {
+      const int grp = idx & 31, j = (idx >> 5) % L, p = idx / (32 * L);
+      uint32_t X[4];
+      if (OP == kDecrypt) {
+        unpack8c<S::WB>(sm + LO::CTO, (32 * j + grp) * S::WB, X);
+      } else if (p < S::RA) {
+        const int ij = (OP == kKeygen) ? (j * L + p) : (p * L + j);
+        unpack8c<S::WA>(sm + LO::A, (32 * ij + grp) * S::WA, X);
+      } else {
+        unpack8c<S::WB>(sm + LO::B, (32 * j + grp) * S::WB, X);
+      }
+      const int kq = 31 - grp;  // coefficients 8grp..8grp+7 are rows k' = 8kq+7..8kq
+      uint8_t *base = Bm + j * 256 * NU + (kq >> 1) * 16 * NU + 8 * (kq & 1);
+      const int cb = p < S::RA ? p * S::DA : S::RA * S::DA + (p - S::RA) * S::DB;
+      const int D = p < S::RA ? S::DA : S::DB;
+#pragma unroll
+      for (int d = 0; d < (S::DA > S::DB ? S::DA : S::DB); d++) {
+        if (d < D) {
+          const int n = cb + d;
+          const uint2 v = digit8<kFp8Tcgen05>(X, d);
+          *reinterpret_cast<uint2 *>(base + (n >> 3) * 128 + (n & 7) * 16) =
+              make_uint2(__byte_perm(v.y, 0, 0x0123), __byte_perm(v.x, 0, 0x0123));
+        }
+      }
+    }
+    constexpr int PADC = NU - S::NCOLS;
+    for (int idx = tid; idx < L * PADC * 16; idx += NT) {
+      const int j = idx / (PADC * 16), r = idx % (PADC * 16), n = S::NCOLS + r % PADC, ac = r / PADC;
+      *reinterpret_cast<uint4 *>(Bm + j * 256 * NU + ac * 16 * NU + (n >> 3) * 128 + (n & 7) * 16) =
+          make_uint4(0u, 0u, 0u, 0u);
+    }
+  }
+  __syncthreads();  // secret words complete before s_ext reads them
+  if (ready) stage_ext(ext, sencw, L, tid, NT, [](uint32_t v) { return v ^ 0x80808080u; });
+  __syncthreads();
+  if (ready) stage_hankel(H, ext, L, tid, NT);
+  fence_async_smem();  // generic-proxy writes -> visible to the tensor core
+  ok = __syncthreads_and(ok) != 0;
+  if (!ok && tid == 0 && a.err) atomicOr(a.err, 1);
+
+  // 3. the MMAs (one thread); descriptors differ only in the start address
+  if (ready && tid == 0) {
+    constexpr uint32_t idesc = umma_idesc_e4m3(NU);
+    const uint64_t ad0 = umma_desc(smem_u32(H), 256, 128);
+    const uint64_t bd0 = umma_desc(smem_u32(Bm), 16 * NU, 128);
+#pragma unroll
+    for (int j = 0; j < L; j++) {
+#pragma unroll
+      for (int ks = 0; ks < 8; ks++) {
+        const uint64_t bd = bd0 + (uint64_t)((j * 256 * NU + 2 * ks * 16 * NU) >> 4);
+#pragma unroll
+        for (int hh = 0; hh < 2; hh++) {
+          const uint64_t ad = ad0 + (uint64_t)((j * kHankelBytes + (16 * hh + 4 * ks) * 128) >> 4);
+          umma_f8(tmem + hh * NU, ad, bd, idesc, (j | ks) != 0);
+        }
+      }
+    }
+    umma_commit(mbar_mma);
+  }
+  // 4. accumulators -> int32 columns (one warp polls, the others wait in the barrier)
+  if (ready) {
+    bool fin = true;
+    if (warp == 0) fin = mbar_wait_bounded(mbar_mma, 0);
+    done = __syncthreads_and(fin) != 0;
+  }
+  tc_fence_after();
+  if (done) {
+#pragma unroll
+    for (int hh = 0; hh < 2; hh++) {
+#pragma unroll
+      for (int cc = 0; cc < NU; cc += 16) {
+        uint32_t r[16];
+        tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + hh * NU + cc, r);
+        const int row = 128 * hh + 32 * warp + lane;
+#pragma unroll
+        for (int c = 0; c < 16; c++)
+          if (cc + c < S::NCOLS) acc[(cc + c) * 256 + row] = __float2int_rn(__uint_as_float(r[c]));
+      }
+    }
+  } else {
+    // an input copy or the tensor core did not complete in time: report, and
+    // give what is still in flight a second bounded wait before releasing
+    if (tid == 0 && a.err) atomicOr(a.err, 2);
+    if (warp == 0) {
+      if (!ready) mbar_wait_bounded(mbar_in, 0);
+      else mbar_wait_bounded(mbar_mma, 0);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, S::TMEM_COLS);
+  if (!done) return;
+
+  // 5. epilogues on groups of eight coefficients
+  auto combine8 = [&](int p, int grp, uint32_t (&V)[4]) {
+    const int cb = p < S::RA ? p * S::DA : S::RA * S::DA + (p - S::RA) * S::DB;
+    const int D = p < S::RA ? S::DA : S::DB;
+    const int4 *base = reinterpret_cast<const int4 *>(acc + 8 * grp);
+    uint32_t v[8];
+    {
+      const int4 x0 = base[cb * 64], x1 = base[cb * 64 + 1];
+      v[0] = x0.x; v[1] = x0.y; v[2] = x0.z; v[3] = x0.w;
+      v[4] = x1.x; v[5] = x1.y; v[6] = x1.z; v[7] = x1.w;
+    }
+#pragma unroll
+    for (int d = 1; d < (S::DA > S::DB ? S::DA : S::DB); d++) {
+      if (d < D) {
+        const uint32_t wgt = 1u << (4 * d);
+        const int4 x0 = base[(cb + d) * 64], x1 = base[(cb + d) * 64 + 1];
+        v[0] += wgt * (uint32_t)x0.x; v[1] += wgt * (uint32_t)x0.y;
+        v[2] += wgt * (uint32_t)x0.z; v[3] += wgt * (uint32_t)x0.w;
+        v[4] += wgt * (uint32_t)x1.x; v[5] += wgt * (uint32_t)x1.y;
+        v[6] += wgt * (uint32_t)x1.z; v[7] += wgt * (uint32_t)x1.w;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) V[i] = (v[2 * i] & 0xffffu) | (v[2 * i + 1] << 16);
+  };
+  constexpr uint32_t qmask = (1u << C::EQ) - 1u, pmask = (1u << C::EP) - 1u;
+  // round(x) = ((x + h1) mod q) >> (eq - ep) on two 16-bit lanes
+  auto round_lanes = [&](uint32_t x) -> uint32_t {
+    const uint32_t lo16 = (((x & 0xffffu) + C::H1) & qmask) >> (C::EQ - C::EP);
+    const uint32_t hi16 = (((x >> 16) + C::H1) & qmask) >> (C::EQ - C::EP);
+    return lo16 | (hi16 << 16);
+  };
+  // c_m = ((x + h1 - (m << (ep-1))) mod p) >> (ep - et) on two 16-bit lanes
+  auto encode_lanes = [&](uint32_t x, uint32_t mlo, uint32_t mhi) -> uint32_t {
+    const uint32_t lo16 = (((x & 0xffffu) + C::H1 - (mlo << (C::EP - 1))) & pmask) >> (C::EP - C::ET);
+    const uint32_t hi16 = (((x >> 16) + C::H1 - (mhi << (C::EP - 1))) & pmask) >> (C::EP - C::ET);
+    return lo16 | (hi16 << 16);
+  };
+
+  if (OP == kDecrypt) {
+    // m'_k = ((v + h2 - (c_m << (ep-et))) mod p) >> (ep-1), one byte per group
+    if (tid < 32) {
+      uint32_t V[4], CM[4];
+      combine8(0, tid, V);
+      unpack8c<C::ET>(sm + LO::CTO + L * C::POLYCOMP, tid * C::ET, CM);
+      uint32_t byte = 0;
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const uint32_t v = (k & 1) ? (V[k >> 1] >> 16) : (V[k >> 1] & 0xffffu);
+        const uint32_t cm = (k & 1) ? (CM[k >> 1] >> 16) : (CM[k >> 1] & 0xffffu);
+        const uint32_t t = (v + C::H2 - (cm << (C::EP - C::ET))) & pmask;
+        byte |= ((t >> (C::EP - 1)) & 1u) << k;
+      }
+      uint8_t *mo = a.m_out + (size_t)inst * a.m_out_stride;
+      mo[tid] = (uint8_t)byte;
+      if (a.copy_hpk) mo[32 + tid] = a.sk[(size_t)inst * C::SK + C::SK - 64 + tid];
+    }
+  } else if (OP == kEncrypt || OP == kReenc) {
+    const uint8_t *msg = sm + LO::MSG;
+    int diff = 0;
+    for (int idx = tid; idx < S::R * 32; idx += NT) {
+      const int p = idx >> 5, grp = idx & 31;
+      uint32_t V[4], W[4];
+      combine8(p, grp, V);
+      if (p < L) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) W[i] = round_lanes(V[i]);
+        const int byte0 = (32 * p + grp) * C::EP;
+        if (OP == kReenc) {
+          uint32_t Cv[4];
+          unpack8c<C::EP>(sm + LO::CTO, byte0, Cv);
+          diff |= (Cv[0] ^ W[0]) | (Cv[1] ^ W[1]) | (Cv[2] ^ W[2]) | (Cv[3] ^ W[3]);
+        } else {
+          pack8(sm + LO::OUT + byte0, W, C::EP);
+        }
+      } else {
+        const uint32_t mb = msg[grp];
+#pragma unroll
+        for (int i = 0; i < 4; i++) W[i] = encode_lanes(V[i], (mb >> (2 * i)) & 1u, (mb >> (2 * i + 1)) & 1u);
+        const int byte0 = L * C::POLYCOMP + grp * C::ET;
+        if (OP == kReenc) {
+          uint32_t Cv[4];
+          unpack8c<C::ET>(sm + LO::CTO, byte0, Cv);
+          diff |= (Cv[0] ^ W[0]) | (Cv[1] ^ W[1]) | (Cv[2] ^ W[2]) | (Cv[3] ^ W[3]);
+        } else {
+          pack8(sm + LO::OUT + byte0, W, C::ET);
+        }
+      }
+    }
+    if (OP == kReenc) {
+      const int any = __syncthreads_or(diff != 0);
+      if (tid == 0) a.fail[inst] = (uint8_t)(any != 0);
+    } else {
+      __syncthreads();
+      copy16(a.ct_out + (size_t)inst * C::CT, sm + LO::OUT, C::CT);
+    }
+  } else if (OP == kKeygen) {
+    constexpr int bbytes = L * C::POLYCOMP;
+    uint8_t *outb = sm + LO::OUT;
+    for (int idx = tid; idx < L * 32; idx += NT) {
+      const int p = idx >> 5, grp = idx & 31;
+      uint32_t V[4], W[4];
+      combine8(p, grp, V);
+#pragma unroll
+      for (int i = 0; i < 4; i++) W[i] = round_lanes(V[i]);
+      pack8(outb + (32 * p + grp) * C::EP, W, C::EP);
+    }
+    // secret key: 13-bit two's complement (Saber) or 2-bit (Sable) of sec8
+    constexpr int sw = C::SABLE ? 2 : C::EQ;
+    const int8_t *s8 = reinterpret_cast<const int8_t *>(sm + LO::SEC8);
+    for (int grp = tid; grp < L * 32; grp += NT) {
+      uint32_t Sv[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+        Sv[i] = ((uint32_t)(int)s8[8 * grp + 2 * i] & 0xffffu) | ((uint32_t)(int)s8[8 * grp + 2 * i + 1] << 16);
+      pack8(outb + bbytes + grp * sw, Sv, sw);
+    }
+    __syncthreads();
+    uint8_t *pko = a.pk_out + (size_t)inst * C::PK;
+    uint8_t *sko = a.sk_out + (size_t)inst * a.sk_stride;
+    for (int i = tid; i < bbytes; i += NT) {
+      pko[i] = outb[i];
+      sko[C::INDCPA_SK + i] = outb[i];
+    }
+    if (tid < 32) sko[C::INDCPA_SK + bbytes + tid] = pko[bbytes + tid];  // seed_A
+    for (int i = tid; i < C::INDCPA_SK; i += NT) sko[i] = outb[bbytes + i];
+  }
+}
+
+template <int OP, int SET>
+inline int launch_cpa5i(const CpaArgs &a, cudaStream_t s) {
+  using LO = LayoutC<OP, SET>;
+  using S = ShapeC<OP, SET>;
+  auto fn = k_cpa5i<OP, SET>;
+  int smem = LO::TOTAL;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return (int)e;
+  // at most 512 / TMEM_COLS resident CTAs per SM, so every CTA's tensor
+  // memory allocation succeeds at once: pad the shared memory until no more fit
+  const int cap = 512 / S::TMEM_COLS;
+  for (int it = 0; it < 64; it++) {
+    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
+      return (int)e;
+    int nb = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, smem)) != cudaSuccess) return (int)e;
+    if (nb <= cap) break;
+    smem += 2048;
+  }
+  fn<<<a.n, 128, smem, s>>>(a);
+  return (int)cudaGetLastError();
+}
+
+// Dispatch over the six parameter sets (matvec is not set-shaped).
+template <int OP>
+inline int launch_cpa5i_set(const CpaArgs &a, cudaStream_t s) {
+  switch (a.P.set) {
+    case 0: return launch_cpa5i<OP, 0>(a, s);
+    case 1: return launch_cpa5i<OP, 1>(a, s);
+    case 2: return launch_cpa5i<OP, 2>(a, s);
+    case 3: return launch_cpa5i<OP, 3>(a, s);
+    case 4: return launch_cpa5i<OP, 4>(a, s);
+    case 5: return launch_cpa5i<OP, 5>(a, s);
+  }
+  return (int)cudaErrorInvalidValue;
+}
+
+}  // namespace tmvp

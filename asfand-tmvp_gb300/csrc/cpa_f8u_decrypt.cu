@@ -1,9 +1,9 @@
 // cpa_f8u_decrypt.cu — op kDecrypt on the tcgen05 tensor cores, in one of two launch
 // shapes picked per (op, parameter set) by the autotuner: one CTA per
-// instance (cpa_tc_kernel.cuh), or the persistent pipelined kernel
+// instance (cpa5i.cuh, specialised per parameter set), or the persistent pipelined kernel
 // (cpa_persist.cuh), which also runs mixed tables of groups.  One translation
 // unit per op so that they compile in parallel.
-#include "cpa_impl.cuh"
+#include "cpa5i.cuh"
 #include "cpa_persist.cuh"
 
 #include <cstring>
@@ -11,7 +11,7 @@
 namespace tmvp {
 int cpa_launch_f8u_decrypt(const CpaArgs &a, cudaStream_t s) {
   const int mode = persist_ctas_per_sm(kDecrypt, a.P.set);
-  if (mode < 0) return launch_op<kFp8Tcgen05, kDecrypt>(a, s);  // one CTA per instance
+  if (mode < 0) return launch_cpa5i_set<kDecrypt>(a, s);  // one CTA per instance
   return launch_persist<kDecrypt>(&a, 1, nullptr, s, mode);
 }
 int cpa_launch_mixed_decrypt(const CpaArgs *g, int ng, const MixTable *dev_tab, cudaStream_t s, int ctas_per_sm) {
