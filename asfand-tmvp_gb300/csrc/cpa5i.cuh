@@ -53,7 +53,15 @@ struct ShapeC {
 
 constexpr int al16c(int x) { return (x + 15) & ~15; }
 
-// Shared-memory layout of one CTA (byte offsets; -1 = absent).
+// Shared-memory layout of one CTA (byte offsets).  The operand region ENG
+// holds the Hankel core matrices H (l x kHankelBytes), the digit columns B and
+// s_ext; the packed GenMatrix / GenSecret / b streams and the packed secret
+// key are only read before H is written, so they land inside H.  Digit
+// columns: K chunk a of column group c at a * LBO_B + c * 128, with
+// LBO_B = 16 N + 16 (the 16-byte pad spreads the chunks of one column over
+// the banks).  When at most 8 columns are used (decryption), only group 0 is
+// stored and the MMA's group 1 reads a shared zero block through the stride
+// byte offset.
 template <int OP, int SET>
 struct LayoutC {
   using C = SetC<SET>;
@@ -62,25 +70,34 @@ struct LayoutC {
   static constexpr bool HAS_B = OP == kEncrypt || OP == kReenc;
   static constexpr bool HAS_CT = OP == kReenc || OP == kDecrypt;
   static constexpr bool HAS_SK = OP == kDecrypt;
-  static constexpr int A = 0;
+  static constexpr bool NARROW = S::NCOLS <= 8;
+  static constexpr int GROUPS = NARROW ? 1 : S::NU / 8;         // stored column groups
+  static constexpr int LBO_B = GROUPS * 128 + 16;
+  static constexpr int BJ = 16 * LBO_B;                          // digit columns of one j
+  static constexpr int ENG = 0;
+  static constexpr int H = ENG;
+  static constexpr int A = H;                                    // streams inside H
   static constexpr int SS = HAS_AS ? al16c(A + C::GM + 16) : A;
   static constexpr int B = HAS_AS ? al16c(SS + C::GS + 16) : SS;
-  static constexpr int MSG = HAS_B ? al16c(B + C::L * C::POLYCOMP + 16) : B;
-  static constexpr int CTO = HAS_B ? al16c(MSG + 32 + 16) : MSG;
-  static constexpr int SKO = HAS_CT ? al16c(CTO + C::CT + 16) : CTO;
-  static constexpr int SEC8 = HAS_SK ? al16c(SKO + C::INDCPA_SK + 16) : SKO;
-  static constexpr int SENC = al16c(SEC8 + C::L * 256);
-  static constexpr int ENG = al16c(SENC + C::L * 256);
-  static constexpr int ENG_BYTES = (C::L * (kHankelBytes + 256 * S::NU + 512) > S::NU * 1024)
-                                       ? C::L * (kHankelBytes + 256 * S::NU + 512)
-                                       : S::NU * 1024;
-  static constexpr int OUT = al16c(ENG + ENG_BYTES);
+  static constexpr int SKO = H;
+  static constexpr int BM = H + C::L * kHankelBytes;
+  static constexpr int ZERO = BM + C::L * BJ;                    // zero block (NARROW)
+  static constexpr int EXT = ZERO + (NARROW ? LBO_B + 128 : 0);
+  static constexpr int ENG_END_OPS = EXT + C::L * 512;
+  static constexpr int ENG_BYTES = ENG_END_OPS > S::NCOLS * 1024 ? ENG_END_OPS : S::NCOLS * 1024;
+  static constexpr int CTO = al16c(ENG + ENG_BYTES);
+  static constexpr int MSG = HAS_CT ? al16c(CTO + C::CT + 16) : CTO;
+  static constexpr int SENC = HAS_B ? al16c(MSG + 32 + 16) : MSG;
+  static constexpr int SEC8 = al16c(SENC + C::L * 256);
+  static constexpr int OUT = OP == kKeygen ? al16c(SEC8 + C::L * 256) : SEC8;
   static constexpr int OUT_BYTES = OP == kEncrypt ? C::CT + 16
                                    : (OP == kKeygen ? C::L * C::POLYCOMP + C::INDCPA_SK + 16 : 0);
   static constexpr int BAR = al16c(OUT + OUT_BYTES);  // mbarriers in, mma; TMEM base
   static constexpr int TOTAL = BAR + 32;
   static constexpr int IN_BYTES = (HAS_AS ? C::GM + C::GS : 0) + (HAS_B ? C::L * C::POLYCOMP + 32 : 0) +
                                   (HAS_CT ? C::CT : 0) + (HAS_SK ? C::INDCPA_SK : 0);
+  static_assert(!HAS_AS || B + (HAS_B ? C::L * C::POLYCOMP + 16 : 0) <= BM, "streams fit inside H");
+  static_assert(!HAS_SK || C::INDCPA_SK + 16 <= C::L * kHankelBytes, "secret key fits inside H");
 };
 
 // Eight W-bit little-endian fields from byte `byte0` (16 bytes of slack after
@@ -146,8 +163,8 @@ __global__ void __launch_bounds__(128, 4) k_cpa5i(CpaArgs a) {
 
   uint32_t *sec8w = reinterpret_cast<uint32_t *>(sm + LO::SEC8);
   uint32_t *sencw = reinterpret_cast<uint32_t *>(sm + LO::SENC);
-  uint8_t *H = sm + LO::ENG, *Bm = H + L * kHankelBytes;
-  uint32_t *ext = reinterpret_cast<uint32_t *>(Bm + L * 256 * NU);
+  uint8_t *H = sm + LO::H, *Bm = sm + LO::BM;
+  uint32_t *ext = reinterpret_cast<uint32_t *>(sm + LO::EXT);
   int *acc = reinterpret_cast<int *>(sm + LO::ENG);
   bool ok = true, done = false;
   if (ready) {
@@ -163,8 +180,6 @@ __global__ void __launch_bounds__(128, 4) k_cpa5i(CpaArgs a) {
         for (int i = 0; i < 4; i++) bad |= ((X[i] + 0x00800080u) & m) & 0xFF00FF00u;
         const uint32_t s0 = __byte_perm(X[0], X[1], 0x6420), s1 = __byte_perm(X[2], X[3], 0x6420);
         ok = ok && bad == 0u && small4(s0) && small4(s1);
-        sec8w[2 * g8] = s0;
-        sec8w[2 * g8 + 1] = s1;
         sencw[2 * g8] = enc4<kFp8Tcgen05>(s0);
         sencw[2 * g8 + 1] = enc4<kFp8Tcgen05>(s1);
       }
@@ -199,7 +214,7 @@ __global__ void __launch_bounds__(128, 4) k_cpa5i(CpaArgs a) {
           sb = r;
         }
         ok = ok && small4(sb);
-        sec8w[w] = sb;
+        if (OP == kKeygen) sec8w[w] = sb;
         sencw[w] = enc4<kFp8Tcgen05>(sb);
       }
     }
@@ -216,7 +231,7 @@ __global__ void __launch_bounds__(128, 4) k_cpa5i(CpaArgs a) {
         unpack8c<S::WB>(sm + LO::B, (32 * j + grp) * S::WB, X);
       }
       const int kq = 31 - grp;  // coefficients 8grp..8grp+7 are rows k' = 8kq+7..8kq
-      uint8_t *base = Bm + j * 256 * NU + (kq >> 1) * 16 * NU + 8 * (kq & 1);
+      uint8_t *base = Bm + j * LO::BJ + (kq >> 1) * LO::LBO_B + 8 * (kq & 1);
       const int cb = p < S::RA ? p * S::DA : S::RA * S::DA + (p - S::RA) * S::DB;
       const int D = p < S::RA ? S::DA : S::DB;
 #pragma unroll
@@ -229,12 +244,15 @@ __global__ void __launch_bounds__(128, 4) k_cpa5i(CpaArgs a) {
         }
       }
     }
-    constexpr int PADC = NU - S::NCOLS;
+    constexpr int PADC = LO::GROUPS * 8 - S::NCOLS;  // zero columns of the stored groups
     for (int idx = tid; idx < L * PADC * 16; idx += NT) {
       const int j = idx / (PADC * 16), r = idx % (PADC * 16), n = S::NCOLS + r % PADC, ac = r / PADC;
-      *reinterpret_cast<uint4 *>(Bm + j * 256 * NU + ac * 16 * NU + (n >> 3) * 128 + (n & 7) * 16) =
+      *reinterpret_cast<uint4 *>(Bm + j * LO::BJ + ac * LO::LBO_B + (n >> 3) * 128 + (n & 7) * 16) =
           make_uint4(0u, 0u, 0u, 0u);
     }
+    if (LO::NARROW)
+      for (int i = tid; i < (LO::LBO_B + 128) / 16; i += NT)
+        reinterpret_cast<uint4 *>(sm + LO::ZERO)[i] = make_uint4(0u, 0u, 0u, 0u);
   }
   __syncthreads();  // secret words complete before s_ext reads them
   if (ready) stage_ext(ext, sencw, L, tid, NT, [](uint32_t v) { return v ^ 0x80808080u; });
@@ -248,12 +266,14 @@ __global__ void __launch_bounds__(128, 4) k_cpa5i(CpaArgs a) {
   if (ready && tid == 0) {
     constexpr uint32_t idesc = umma_idesc_e4m3(NU);
     const uint64_t ad0 = umma_desc(smem_u32(H), 256, 128);
-    const uint64_t bd0 = umma_desc(smem_u32(Bm), 16 * NU, 128);
+    const uint32_t b0 = smem_u32(Bm), z0 = smem_u32(sm + LO::ZERO);
 #pragma unroll
     for (int j = 0; j < L; j++) {
 #pragma unroll
       for (int ks = 0; ks < 8; ks++) {
-        const uint64_t bd = bd0 + (uint64_t)((j * 256 * NU + 2 * ks * 16 * NU) >> 4);
+        const uint32_t bs = b0 + j * LO::BJ + 2 * ks * LO::LBO_B;
+        // group 1 of a narrow B is the zero block, one stride byte offset away
+        const uint64_t bd = umma_desc(bs, LO::LBO_B, LO::NARROW ? z0 - bs : 128);
 #pragma unroll
         for (int hh = 0; hh < 2; hh++) {
           const uint64_t ad = ad0 + (uint64_t)((j * kHankelBytes + (16 * hh + 4 * ks) * 128) >> 4);

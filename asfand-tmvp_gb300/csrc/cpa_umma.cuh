@@ -35,7 +35,7 @@
 namespace tmvp {
 
 constexpr int kHankelCores = 62;                  // distinct core matrices of H_j
-constexpr int kHankelBytes = 8192;                // per secret polynomial (7936 used)
+constexpr int kHankelBytes = kHankelCores * 128;  // per secret polynomial (7936 bytes)
 constexpr int kUmmaM = 128;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -185,25 +185,31 @@ __device__ __forceinline__ void stage_ext(uint32_t *ext, const uint32_t *S, int 
 // The Hankel core matrices of every j < L (H: kHankelBytes per polynomial):
 // row i of core m is s_ext[8m + i .. 8m + i + 15], so row x = 8m + i sits at
 // byte 16x.  Rows x = 4q + sh (q = 0..123) with the same byte shift sh are
-// windows of consecutive words, so a thread makes a run of rows from a
-// sliding window of ext words: one word load and four byte permutes per row.
+// windows of consecutive words.  Thread group g (four threads, sh = 0..3)
+// makes the rows q = 2u + (g & 1) for a run of u, from a window of ext words
+// that slides by two words per row; the eight threads of two neighbouring
+// groups store eight consecutive rows (128 contiguous bytes) at a time.
 __device__ __forceinline__ void stage_hankel(uint8_t *H, const uint32_t *ext, int L, int tid,
                                              int nthreads) {
-  const int groups = nthreads >> 2;            // threads per shift class
-  const int run = (124 + groups - 1) / groups;  // rows per thread and polynomial
-  const int sh = tid & 3, q0 = (tid >> 2) * run;
+  const int pairs = nthreads >> 3;             // group pairs
+  const int run = (62 + pairs - 1) / pairs;     // rows per thread and polynomial
+  const int sh = tid & 3, par = (tid >> 2) & 1, u0 = (tid >> 3) * run;
   const uint32_t sel = (uint32_t)(sh | ((sh + 1) << 4) | ((sh + 2) << 8) | ((sh + 3) << 12));
+  if (u0 >= 62) return;
   for (int j = 0; j < L; j++) {
     const uint32_t *e = ext + 128 * j;
     uint8_t *hj = H + (size_t)j * kHankelBytes;
-    if (q0 >= 124) continue;
-    uint32_t w0 = e[q0], w1 = e[q0 + 1], w2 = e[q0 + 2], w3 = e[q0 + 3];
-    for (int q = q0; q < q0 + run && q < 124; q++) {
-      const uint32_t w4 = e[q + 4];
+    int q = 2 * u0 + par;
+    uint32_t w0 = e[q], w1 = e[q + 1], w2 = e[q + 2], w3 = e[q + 3], w4 = e[q + 4];
+    for (int u = u0; u < u0 + run && u < 62; u++, q += 2) {
       *reinterpret_cast<uint4 *>(hj + 16 * (4 * q + sh)) =
           make_uint4(__byte_perm(w0, w1, sel), __byte_perm(w1, w2, sel), __byte_perm(w2, w3, sel),
                      __byte_perm(w3, w4, sel));
-      w0 = w1; w1 = w2; w2 = w3; w3 = w4;
+      if (u + 1 < u0 + run && u + 1 < 62) {
+        w0 = w2; w1 = w3; w2 = w4;
+        w3 = e[q + 5];
+        w4 = e[q + 6];
+      }
     }
   }
 }
