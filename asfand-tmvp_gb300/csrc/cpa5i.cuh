@@ -122,14 +122,13 @@ __device__ __forceinline__ void unpack8c(const uint8_t *base, int byte0, uint32_
   }
 }
 
+// One instance (CTA of 128 threads; sm: its dynamic shared memory).
 template <int OP, int SET>
-__global__ void __launch_bounds__(128, 4) k_cpa5i(CpaArgs a) {
+__device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst, uint8_t *sm) {
   using C = SetC<SET>;
   using S = ShapeC<OP, SET>;
   using LO = LayoutC<OP, SET>;
   constexpr int L = C::L, NU = S::NU, NT = 128;
-  extern __shared__ __align__(16) uint8_t sm[];
-  const unsigned inst = blockIdx.x;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t mbar_in = smem_u32(sm + LO::BAR), mbar_mma = mbar_in + 8;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + LO::BAR + 16);
@@ -444,6 +443,91 @@ __global__ void __launch_bounds__(128, 4) k_cpa5i(CpaArgs a) {
     if (tid < 32) sko[C::INDCPA_SK + bbytes + tid] = pko[bbytes + tid];  // seed_A
     for (int i = tid; i < C::INDCPA_SK; i += NT) sko[i] = outb[bbytes + i];
   }
+}
+
+template <int OP, int SET>
+__global__ void __launch_bounds__(128, 4) k_cpa5i(CpaArgs a) {
+  extern __shared__ __align__(16) uint8_t sm[];
+  cpa5i_body<OP, SET>(a, blockIdx.x, sm);
+}
+
+// Mixed launch: CTA gi runs instance gi of the group table R (one CTA per
+// instance over all groups, whatever their parameter sets).
+template <int OP>
+__global__ void __launch_bounds__(128, 4) k_cpa5m(const __grid_constant__ MixRef R) {
+  extern __shared__ __align__(16) uint8_t sm[];
+  const int gi = blockIdx.x;
+  const int g = find_group(R, gi);
+  const CpaArgs &a = group_args(R, g);
+  const unsigned inst = (unsigned)(gi - group_first(R, g));
+  switch (a.P.set) {
+    case 0: cpa5i_body<OP, 0>(a, inst, sm); break;
+    case 1: cpa5i_body<OP, 1>(a, inst, sm); break;
+    case 2: cpa5i_body<OP, 2>(a, inst, sm); break;
+    case 3: cpa5i_body<OP, 3>(a, inst, sm); break;
+    case 4: cpa5i_body<OP, 4>(a, inst, sm); break;
+    case 5: cpa5i_body<OP, 5>(a, inst, sm); break;
+  }
+}
+
+template <int OP>
+inline void layout5_of(int set, int &total, int &cols) {
+  switch (set) {
+#define TMVP_L5(S)                                 \
+  case S:                                          \
+    total = LayoutC<OP, S>::TOTAL;                 \
+    cols = ShapeC<OP, S>::TMEM_COLS;               \
+    break;
+    TMVP_L5(0) TMVP_L5(1) TMVP_L5(2) TMVP_L5(3) TMVP_L5(4) TMVP_L5(5)
+#undef TMVP_L5
+    default: total = 0; cols = 32;
+  }
+}
+
+// Pads `smem` until at most 512 / cols CTAs of fn fit on an SM, so that every
+// resident CTA's tensor-memory allocation succeeds at once.
+template <class F>
+inline int cap_tmem_residency(F fn, int &smem, int cols) {
+  const int cap = 512 / cols;
+  cudaError_t e;
+  for (int it = 0; it < 64; it++) {
+    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
+      return (int)e;
+    int nb = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, smem)) != cudaSuccess) return (int)e;
+    if (nb <= cap) return 0;
+    smem += 2048;
+  }
+  return 0;
+}
+
+template <int OP>
+inline int launch_cpa5m(const CpaArgs *groups, int ng, const MixTable *dev_tab, cudaStream_t s) {
+  MixRef R{};
+  R.ngroups = ng;
+  R.total = 0;
+  int smem = 0, cols = 32;
+  for (int g = 0; g < ng; g++) {
+    R.total += groups[g].n;
+    int t, c;
+    layout5_of<OP>(groups[g].P.set, t, c);
+    smem = std::max(smem, t);
+    cols = std::max(cols, c);
+  }
+  if (R.total <= 0) return 0;
+  if (ng == 1) {
+    R.one = groups[0];
+  } else {
+    if (!dev_tab) return (int)cudaErrorInvalidValue;
+    R.tab = dev_tab;
+  }
+  auto fn = k_cpa5m<OP>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return (int)e;
+  int rc = cap_tmem_residency(fn, smem, cols);
+  if (rc) return rc;
+  fn<<<R.total, 128, smem, s>>>(R);
+  return (int)cudaGetLastError();
 }
 
 template <int OP, int SET>

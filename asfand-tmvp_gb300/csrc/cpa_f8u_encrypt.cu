@@ -14,6 +14,7 @@ int cpa_launch_f8u_encrypt(const CpaArgs &a, cudaStream_t s) {
 }
 int cpa_launch_mixed_encrypt(const CpaArgs *g, int ng, const MixTable *dev_tab, cudaStream_t s, int ctas_per_sm) {
   if (ng < 1 || ng > kMaxGroups) return (int)cudaErrorInvalidValue;
+  if (ctas_per_sm < 0) return launch_cpa5m<kEncrypt>(g, ng, dev_tab, s);  // one CTA per instance
   return launch_persist<kEncrypt>(g, ng, dev_tab, s, ctas_per_sm);
 }
 }  // namespace tmvp

@@ -14,6 +14,6 @@ int cpa_launch_f8u_matvec(const CpaArgs &a, cudaStream_t s) {
 }
 int cpa_launch_mixed_matvec(const CpaArgs *g, int ng, const MixTable *dev_tab, cudaStream_t s, int ctas_per_sm) {
   if (ng < 1 || ng > kMaxGroups) return (int)cudaErrorInvalidValue;
-  return launch_persist<kMatvec>(g, ng, dev_tab, s, ctas_per_sm);
+  return launch_persist<kMatvec>(g, ng, dev_tab, s, ctas_per_sm < 0 ? 0 : ctas_per_sm);
 }
 }  // namespace tmvp

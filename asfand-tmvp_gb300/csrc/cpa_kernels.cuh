@@ -54,7 +54,8 @@ int cpa_launch(int form, int op, const CpaArgs &a, void *stream);
 // groups of instances, each with its own parameter set and buffers.  groups:
 // host copies; dev_tab: the same groups as a device table (mix_table_build
 // into mix_table_bytes() of device memory; unused when ngroups == 1).
-// ctas_per_sm = 0 takes as many CTAs per SM as fit.
+// ctas_per_sm >= 0: the persistent kernel with that many CTAs per SM (0 = as
+// many as fit); -1: one CTA per instance over all groups (not for matvec).
 constexpr int kMixMaxGroups = 64;
 struct MixTable;
 size_t mix_table_bytes();

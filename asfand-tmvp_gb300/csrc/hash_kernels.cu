@@ -77,10 +77,8 @@ __global__ void __launch_bounds__(128) k_enc_front(KemParams P, const uint8_t *p
 
 // Decapsulation step after decryption (saber_dec, cuda_kernel.cu:378-385):
 // kr = G(m' || H(pk)) and the GenSecret stream SHAKE-128(kr[32:64]).
-__global__ void __launch_bounds__(128) k_dec_g(KemParams P, const uint8_t *mbuf, uint8_t *kr,
-                                                uint8_t *s_stream, int n) {
-  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (size_t)n) return;
+__device__ __forceinline__ void dec_g_one(const KemParams &P, const uint8_t *mbuf, uint8_t *kr,
+                                          uint8_t *s_stream, size_t t) {
   uint64_t buf[8], g[8];
   load_words(buf, mbuf + t * 64, 8);
   sha3_512_64(g, buf);
@@ -91,37 +89,52 @@ __global__ void __launch_bounds__(128) k_dec_g(KemParams P, const uint8_t *mbuf,
   shake128_32(reinterpret_cast<uint64_t *>(s_stream + t * P.gs_bytes), P.gs_bytes, seed);
 }
 
-// Decapsulation front, independent of the decryption: threads i < n expand
-// GenMatrix from the seed of the pk embedded in sk; threads n..2n-1 hash the
-// ciphertext, H(c) (saber_dec, cuda_kernel.cu:383-384 and :447).
+__global__ void __launch_bounds__(128) k_dec_g(KemParams P, const uint8_t *mbuf, uint8_t *kr,
+                                                uint8_t *s_stream, int n) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (size_t)n) dec_g_one(P, mbuf, kr, s_stream, t);
+}
+
+// GenMatrix of instance t from the seed of the pk embedded in sk.
+__device__ __forceinline__ void dec_genmatrix_one(const KemParams &P, const uint8_t *sk, uint8_t *a_stream,
+                                                  size_t t) {
+  uint64_t seed[4];
+  load_words(seed, sk + t * P.sk_bytes + P.indcpa_sk_bytes + (size_t)P.l * P.polycompbytes, 4);
+  shake128_32(reinterpret_cast<uint64_t *>(a_stream + t * P.gm_bytes), P.gm_bytes, seed);
+}
+
+// H(c) of instance i.
+__device__ __forceinline__ void dec_hash_ct_one(const KemParams &P, const uint8_t *ct, uint8_t *hc, size_t i) {
+  uint64_t h[4];
+  sha3_256_words(h, reinterpret_cast<const uint64_t *>(ct + i * P.ct_bytes), P.ct_bytes);
+  uint64_t *o = reinterpret_cast<uint64_t *>(hc + i * 32);
+#pragma unroll
+  for (int w = 0; w < 4; w++) o[w] = h[w];
+}
+
+// Decapsulation front, independent of the decryption: GenMatrix from the seed
+// of the pk embedded in sk, and the ciphertext hash H(c) (saber_dec,
+// cuda_kernel.cu:383-384 and :447).  part 0: threads i < n expand GenMatrix,
+// threads n..2n-1 hash; part 1: GenMatrix only; part 2: H(c) only (n threads).
 __global__ void __launch_bounds__(128) k_dec_front(KemParams P, const uint8_t *sk,
                                                     const uint8_t *ct, uint8_t *a_stream,
-                                                    uint8_t *hc, int n) {
+                                                    uint8_t *hc, int n, int part) {
   size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < (size_t)n) {
-    uint64_t seed[4];
-    load_words(seed, sk + t * P.sk_bytes + P.indcpa_sk_bytes + (size_t)P.l * P.polycompbytes, 4);
-    shake128_32(reinterpret_cast<uint64_t *>(a_stream + t * P.gm_bytes), P.gm_bytes, seed);
-  } else if (t < 2 * (size_t)n) {
-    size_t i = t - n;
-    uint64_t h[4];
-    sha3_256_words(h, reinterpret_cast<const uint64_t *>(ct + i * P.ct_bytes), P.ct_bytes);
-    uint64_t *o = reinterpret_cast<uint64_t *>(hc + i * 32);
-#pragma unroll
-    for (int w = 0; w < 4; w++) o[w] = h[w];
-  }
+  if (part == 1 && t >= (size_t)n) return;
+  if (part == 2) t += (size_t)n;
+  if (t < (size_t)n)
+    dec_genmatrix_one(P, sk, a_stream, t);
+  else if (t < 2 * (size_t)n)
+    dec_hash_ct_one(P, ct, hc, t - n);
 }
 
 // Final key derivation.  Encapsulation (cuda_kernel.cu:185-186):
 // K = H(kr[0:32] || H(c)); hc, when given, holds H(c) already.  Decapsulation (cuda_kernel.cu:445-450, with the
 // FO selection done as specified): K = H((fail ? z : kr[0:32]) || H(c)), the
 // selection made with a mask so that it does not branch on `fail`.
-__global__ void __launch_bounds__(128) k_final_key(KemParams P, const uint8_t *ct,
-                                                    const uint8_t *hc, const uint8_t *kr,
-                                                    const uint8_t *fail, const uint8_t *sk,
-                                                    uint8_t *ss, int n) {
-  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (size_t)n) return;
+__device__ __forceinline__ void final_key_one(const KemParams &P, const uint8_t *ct, const uint8_t *hc,
+                                              const uint8_t *kr, const uint8_t *fail, const uint8_t *sk,
+                                              uint8_t *ss, size_t t) {
   uint64_t buf[8], k[4];
   load_words(buf, kr + t * 64, 4);
   if (fail) {
@@ -139,6 +152,49 @@ __global__ void __launch_bounds__(128) k_final_key(KemParams P, const uint8_t *c
   uint64_t *o = reinterpret_cast<uint64_t *>(ss + t * 32);
 #pragma unroll
   for (int w = 0; w < 4; w++) o[w] = k[w];
+}
+
+__global__ void __launch_bounds__(128) k_final_key(KemParams P, const uint8_t *ct,
+                                                    const uint8_t *hc, const uint8_t *kr,
+                                                    const uint8_t *fail, const uint8_t *sk,
+                                                    uint8_t *ss, int n) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (size_t)n) final_key_one(P, ct, hc, kr, fail, sk, ss, t);
+}
+
+// ---- mixed-parameter decapsulation: one launch per stage over a group table
+
+__device__ __forceinline__ int hash_group(const HashGroup *T, int ng, int gi) {
+  int lo = 0, hi = ng - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (gi >= T[mid].first) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(128) k_mix_front(const HashGroup *T, int ng, int total, int part) {
+  const int gi = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (gi >= total) return;
+  const HashGroup &G = T[hash_group(T, ng, gi)];
+  const size_t i = (size_t)(gi - G.first);
+  if (part == 1) dec_genmatrix_one(G.P, G.sk, G.a_stream, i);
+  else dec_hash_ct_one(G.P, G.ct, G.hc, i);
+}
+
+__global__ void __launch_bounds__(128) k_mix_g(const HashGroup *T, int ng, int total) {
+  const int gi = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (gi >= total) return;
+  const HashGroup &G = T[hash_group(T, ng, gi)];
+  dec_g_one(G.P, G.mbuf, G.kr, G.s_stream, (size_t)(gi - G.first));
+}
+
+__global__ void __launch_bounds__(128) k_mix_final(const HashGroup *T, int ng, int total) {
+  const int gi = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (gi >= total) return;
+  const HashGroup &G = T[hash_group(T, ng, gi)];
+  final_key_one(G.P, G.ct, G.hc, G.kr, G.fail, G.sk, G.ss, (size_t)(gi - G.first));
 }
 
 // Key-generation tail: sk[SK-64 : SK-32] = H(pk), sk[SK-32 : SK] = z.

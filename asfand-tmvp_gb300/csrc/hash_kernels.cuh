@@ -29,9 +29,22 @@ __global__ void k_dec_g(KemParams P, const uint8_t *mbuf, uint8_t *kr, uint8_t *
 __global__ void k_final_key(KemParams P, const uint8_t *ct, const uint8_t *hc, const uint8_t *kr,
                             const uint8_t *fail, const uint8_t *sk, uint8_t *ss, int n);
 __global__ void k_dec_front(KemParams P, const uint8_t *sk, const uint8_t *ct, uint8_t *a_stream,
-                            uint8_t *hc, int n);
+                            uint8_t *hc, int n, int part);
 __global__ void k_kp_final(KemParams P, const uint8_t *pk, uint8_t *sk, const uint8_t *coins,
                            int n);
 __global__ void k_sha3_256_batch(const uint8_t *in, int inbytes, uint8_t *out, int n);
+
+// Mixed-parameter decapsulation: group g covers global instances
+// [first, first + n) with its own parameters and buffers (device table).
+struct HashGroup {
+  KemParams P;
+  int first, n;
+  const uint8_t *sk, *ct;
+  uint8_t *a_stream, *s_stream, *mbuf, *kr, *fail, *hc, *ss;
+};
+// part 1: GenMatrix; part 2: H(c)
+__global__ void k_mix_front(const HashGroup *T, int ng, int total, int part);
+__global__ void k_mix_g(const HashGroup *T, int ng, int total);
+__global__ void k_mix_final(const HashGroup *T, int ng, int total);
 
 }  // namespace tmvp

@@ -7,9 +7,9 @@
 //             -> k_cpa<kKeygen> -> k_kp_final (H(pk), z)
 //   encaps  : k_enc_front (H(coins), H(pk), G, GenSecret; GenMatrix)
 //             -> k_cpa<kEncrypt> -> k_final_key
-//   decaps  : k_dec_front (GenMatrix; H(c)) on a side stream, concurrent with
-//             k_cpa<kDecrypt> -> k_dec_g; then k_cpa<kReenc> -> k_final_key
-//             (implicit rejection)
+//   decaps  : k_dec_front (GenMatrix, then H(c)) on a side stream, concurrent
+//             with k_cpa<kDecrypt> -> k_dec_g; k_cpa<kReenc> waits only for
+//             GenMatrix, k_final_key (implicit rejection) also for H(c)
 // They replace the launch sequences of saber_enc / saber_dec
 // (TMVP-Saber/SABER-GPU/src/cuda_kernel.cu:25-479) and SABLE_enc / SABLE_dec
 // (TMVP_SABLE/src/SABLE_indcpa.cu:24-610).
@@ -57,7 +57,10 @@ struct tmvp_ctx {
   int *d_err = nullptr;   // device-side input-range flag
   uint64_t launches = 0;
   cudaStream_t side = nullptr;          // second stream for independent stages
-  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr, hc_ev = nullptr;
+  size_t host_chunk = 16384;                       // chunk of host-input decapsulation (0: none)
+  cudaStream_t copy[2] = {};                       // host-to-device copies of chunked calls
+  cudaEvent_t ev_loaded[2][2] = {}, ev_free[2] = {};  // per input slot (and copy stream)
   std::mutex mu;
   // optional per-stage timing: CUDA events recorded on the launching stream
   bool timing = false;
@@ -278,6 +281,87 @@ struct Guard {
   }
 };
 
+// Host-resident decapsulation inputs are copied and processed in chunks (the
+// context's host_chunk instances, default below), so that the copy of one
+// chunk overlaps the kernels of the previous one.
+constexpr size_t kHostChunk = 16384;
+
+// Intermediate buffers of one decapsulation pass over n instances.
+struct DecScratch {
+  uint8_t *a_stream, *s_stream, *mbuf, *kr, *fail, *hc;
+};
+
+size_t dec_ws_bytes(const KemParams &P, size_t n) {
+  return up(n * P.gm_bytes) + up(n * P.gs_bytes) + 2 * up(n * 64) + up(n) + up(n * 32);
+}
+
+DecScratch dec_scratch(const KemParams &P, size_t n, Arena &A) {
+  DecScratch w;
+  w.a_stream = A.take(n * P.gm_bytes);
+  w.s_stream = A.take(n * P.gs_bytes);
+  w.mbuf = A.take(n * 64);
+  w.kr = A.take(n * 64);
+  w.fail = A.take(n);
+  w.hc = A.take(n * 32);
+  return w;
+}
+
+// Decapsulation of n instances in device memory (16-byte aligned):
+// GenMatrix, then H(c), on the side stream, concurrent with the decryption and
+// G on s; the re-encryption waits for GenMatrix, the final key for H(c).
+int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const uint8_t *ct,
+                 const uint8_t *sk, int form, cudaStream_t s, const DecScratch &w) {
+  int r;
+  TRY_CUDA(cudaEventRecord(c->fork_ev, s));
+  TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+  {
+    StageTimer tm_(c, "dec_front", c->side);
+    k_dec_front<<<blocks_for(n, 128), 128, 0, c->side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 1);
+  }
+  TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
+  {
+    StageTimer tm_(c, "dec_hash_ct", c->side);
+    k_dec_front<<<blocks_for(n, 128), 128, 0, c->side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
+  }
+  c->launches += 2;
+  TRY_CUDA(cudaEventRecord(c->hc_ev, c->side));
+  CpaArgs a{};
+  a.P = P;
+  a.n = (int)n;
+  a.ct = ct;
+  a.sk = sk;
+  a.m_out = w.mbuf;
+  a.m_out_stride = 64;
+  a.copy_hpk = 1;
+  if ((r = run_cpa(c, form, kDecrypt, a, s))) return r;
+  {
+    StageTimer tm_(c, "dec_g", s);
+    k_dec_g<<<blocks_for(n, 128), 128, 0, s>>>(P, w.mbuf, w.kr, w.s_stream, (int)n);
+  }
+  c->launches++;
+  TRY_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));  // join: GenMatrix
+  CpaArgs b{};
+  b.P = P;
+  b.n = (int)n;
+  b.a_stream = w.a_stream;
+  b.s_stream = w.s_stream;
+  b.pk = sk;
+  b.pk_stride = P.sk_bytes;
+  b.pk_off = P.indcpa_sk_bytes;
+  b.msg = w.mbuf;
+  b.msg_stride = 64;
+  b.ct = ct;
+  b.fail = w.fail;
+  if ((r = run_cpa(c, form, kReenc, b, s))) return r;
+  TRY_CUDA(cudaStreamWaitEvent(s, c->hc_ev, 0));  // join: H(c)
+  {
+    StageTimer tm_(c, "final_key", s);
+    k_final_key<<<blocks_for(n, 128), 128, 0, s>>>(P, ct, w.hc, w.kr, w.fail, sk, ss, (int)n);
+  }
+  c->launches++;
+  return TMVP_OK;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -335,7 +419,16 @@ int tmvp_ctx_create(int device, size_t mem_budget, tmvp_ctx **out) {
   if (cudaMalloc(&c->d_err, sizeof(int)) != cudaSuccess || cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->hc_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->copy[0], cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->copy[1], cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_loaded[0][0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_loaded[0][1], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_loaded[1][0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_loaded[1][1], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_free[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_free[1], cudaEventDisableTiming) != cudaSuccess) {
     delete c;
     return set_err(TMVP_EDEVICE);
   }
@@ -355,11 +448,25 @@ void tmvp_ctx_destroy(tmvp_ctx *c) {
     if (c->side) cudaStreamDestroy(c->side);
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->join_ev) cudaEventDestroy(c->join_ev);
+    if (c->hc_ev) cudaEventDestroy(c->hc_ev);
+    for (int i = 0; i < 2; i++) {
+      if (c->copy[i]) cudaStreamDestroy(c->copy[i]);
+      for (int k = 0; k < 2; k++)
+        if (c->ev_loaded[i][k]) cudaEventDestroy(c->ev_loaded[i][k]);
+      if (c->ev_free[i]) cudaEventDestroy(c->ev_free[i]);
+    }
   }
   delete c;
 }
 
 size_t tmvp_ctx_workspace_bytes(const tmvp_ctx *c) { return c ? c->ws_cap : 0; }
+
+int tmvp_ctx_set_host_chunk(tmvp_ctx *c, size_t n) {
+  if (!c || (n != 0 && n < 1024)) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->host_chunk = n;
+  return set_err(TMVP_OK);
+}
 
 int tmvp_ctx_reserve(tmvp_ctx *c, size_t bytes) {
   if (!c) return set_err(TMVP_EINVAL);
@@ -508,58 +615,50 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
   cudaStream_t s = (cudaStream_t)stream;
   Buf bss = classify(ss, n * 32, c->device), bct = classify(ct, n * P.ct_bytes, c->device),
       bsk = classify(sk, n * P.sk_bytes, c->device);
-  size_t need = up(n * P.gm_bytes) + up(n * P.gs_bytes) + 2 * up(n * 64) + up(n) + up(n * 32) +
-                stage_bytes(bss) + stage_bytes(bct) + stage_bytes(bsk);
+  if ((bct.host || bsk.host) && c->host_chunk && n > c->host_chunk) {
+    // host inputs: chunks whose copies overlap the previous chunk's kernels
+    const size_t cn = c->host_chunk;
+    const size_t inb = up(cn * P.ct_bytes) + up(cn * P.sk_bytes);
+    size_t need = dec_ws_bytes(P, cn) + 2 * inb + (bss.host ? up(cn * 32) : 0);
+    if ((r = ensure_ws(c, need))) return set_err(r);
+    Arena A{c->ws};
+    DecScratch w = dec_scratch(P, cn, A);
+    uint8_t *slot_in[2] = {A.take(inb), A.take(inb)};
+    uint8_t *ss_stage = bss.host ? A.take(cn * 32) : nullptr;
+    for (size_t off = 0, k = 0; off < n; off += cn, k++) {
+      const size_t m = std::min(cn, n - off);
+      const int sl = (int)(k & 1);
+      uint8_t *ct_k = bct.host ? slot_in[sl] : bct.dev + off * P.ct_bytes;
+      uint8_t *sk_k = bsk.host ? slot_in[sl] + up(cn * P.ct_bytes) : bsk.dev + off * P.sk_bytes;
+      // the copies of chunk k wait until chunk k-2's kernels have read this
+      // slot; ct and sk go on two copy streams (two copy engines)
+      for (int q = 0; q < 2; q++) {
+        if (k >= 2) TRY_CUDA(cudaStreamWaitEvent(c->copy[q], c->ev_free[sl], 0));
+        const Buf &b = q == 0 ? bct : bsk;
+        const size_t rec = q == 0 ? P.ct_bytes : P.sk_bytes;
+        if (b.host)
+          TRY_CUDA(cudaMemcpyAsync(q == 0 ? ct_k : sk_k, (const uint8_t *)b.user + off * rec, m * rec,
+                                   cudaMemcpyDefault, c->copy[q]));
+        TRY_CUDA(cudaEventRecord(c->ev_loaded[sl][q], c->copy[q]));
+        TRY_CUDA(cudaStreamWaitEvent(s, c->ev_loaded[sl][q], 0));
+      }
+      uint8_t *ss_k = bss.host ? ss_stage : bss.dev + off * 32;
+      if ((r = dec_pipeline(c, P, m, ss_k, ct_k, sk_k, form, s, w))) return set_err(r);
+      TRY_CUDA(cudaEventRecord(c->ev_free[sl], s));
+      if (bss.host)
+        TRY_CUDA(cudaMemcpyAsync((uint8_t *)bss.user + off * 32, ss_stage, m * 32, cudaMemcpyDefault, s));
+    }
+    return set_err(finish(c, s, bss.host));
+  }
+  size_t need = dec_ws_bytes(P, n) + stage_bytes(bss) + stage_bytes(bct) + stage_bytes(bsk);
   if ((r = ensure_ws(c, need))) return set_err(r);
   Arena A{c->ws};
-  uint8_t *a_stream = A.take(n * P.gm_bytes), *s_stream = A.take(n * P.gs_bytes);
-  uint8_t *mbuf = A.take(n * 64), *kr = A.take(n * 64), *fail = A.take(n), *hc = A.take(n * 32);
+  DecScratch w = dec_scratch(P, n, A);
   stage_assign(bss, A);
   stage_assign(bct, A);
   stage_assign(bsk, A);
   if ((r = upload(bct, s)) || (r = upload(bsk, s))) return set_err(r);
-  // fork: GenMatrix and H(c) on the side stream, concurrent with decryption
-  TRY_CUDA(cudaEventRecord(c->fork_ev, s));
-  TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
-  {
-    StageTimer tm_(c, "dec_front", c->side);
-    k_dec_front<<<blocks_for(2 * n, 128), 128, 0, c->side>>>(P, bsk.dev, bct.dev, a_stream, hc, (int)n);
-  }
-  c->launches++;
-  TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
-  CpaArgs a{};
-  a.P = P;
-  a.n = (int)n;
-  a.ct = bct.dev;
-  a.sk = bsk.dev;
-  a.m_out = mbuf;
-  a.m_out_stride = 64;
-  a.copy_hpk = 1;
-  if ((r = run_cpa(c, form, kDecrypt, a, s))) return set_err(r);
-  {
-    StageTimer tm_(c, "dec_g", s);
-    k_dec_g<<<blocks_for(n, 128), 128, 0, s>>>(P, mbuf, kr, s_stream, (int)n);
-  }
-  c->launches++;
-  TRY_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));  // join
-  CpaArgs b{};
-  b.P = P;
-  b.n = (int)n;
-  b.a_stream = a_stream;
-  b.s_stream = s_stream;
-  b.pk = bsk.dev;
-  b.pk_stride = P.sk_bytes;
-  b.pk_off = P.indcpa_sk_bytes;
-  b.msg = mbuf;
-  b.msg_stride = 64;
-  b.ct = bct.dev;
-  b.fail = fail;
-  if ((r = run_cpa(c, form, kReenc, b, s))) return set_err(r);
-  {
-    StageTimer tm_(c, "final_key", s);
-    k_final_key<<<blocks_for(n, 128), 128, 0, s>>>(P, bct.dev, hc, kr, fail, bsk.dev, bss.dev, (int)n);
-  }
-  c->launches++;
+  if ((r = dec_pipeline(c, P, n, bss.dev, bct.dev, bsk.dev, form, s, w))) return set_err(r);
   if ((r = download(bss, s))) return set_err(r);
   return set_err(finish(c, s, bss.host));
 }
@@ -885,7 +984,10 @@ size_t mixed_ws_bytes(size_t ng, const tmvp_dec_group *gr) {
 
 int mixed_check(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr) {
   if (!c || !gr || ng == 0 || ng > (size_t)kMixMaxGroups) return TMVP_EINVAL;
+  size_t total = 0;
   for (size_t g = 0; g < ng; g++) {
+    total += gr[g].n;
+    if (total > ((size_t)1 << 30)) return TMVP_EINVAL;
     KemParams P;
     if (!make_params(gr[g].set, &P) || gr[g].n == 0 || gr[g].n > (size_t)(INT_MAX / 4)) return TMVP_EINVAL;
     const void *bufs[3] = {gr[g].ss, gr[g].ct, gr[g].sk};
@@ -895,86 +997,100 @@ int mixed_check(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr) {
   return TMVP_OK;
 }
 
-// Enqueues one mixed decapsulation pass on s: per-group Keccak stages on the
-// side stream and s, and one persistent tcgen05 launch per CPA step over all
-// groups.  ws: mixed_ws_bytes of device memory; tabs: two device group tables
-// (decryption, re-encryption).  Makes no allocation and no host
-// synchronisation, so it can be captured into a graph.
+// Device bytes of the group tables of one pass: two CPA tables (decryption,
+// re-encryption) and the Keccak-stage table.
+size_t mixed_tab_bytes(size_t ng) {
+  return 2 * up(mix_table_bytes()) + up(ng * sizeof(HashGroup));
+}
+
+// Enqueues one mixed decapsulation pass on s: every stage is one launch over
+// all groups (GenMatrix, then H(c), on the side stream; decryption, G,
+// re-encryption and the final key on s).  ws: mixed_ws_bytes of device
+// memory; tabs: mixed_tab_bytes of device memory for the group tables, which
+// are built into host_tabs and, if upload_tabs, copied on s.  Makes no
+// allocation and no host synchronisation, so it can be captured into a graph.
 int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws, uint8_t *tabs,
                   std::vector<uint8_t> &host_tabs, bool upload_tabs, cudaStream_t s) {
   std::vector<CpaArgs> ga(ng), gb(ng);
-  std::vector<KemParams> P(ng);
+  std::vector<HashGroup> hg(ng);
   Arena A{ws};
-  std::vector<uint8_t *> a_stream(ng), s_stream(ng), mbuf(ng), kr(ng), fail(ng), hc(ng);
-  for (size_t g = 0; g < ng; g++) {
-    make_params(gr[g].set, &P[g]);
-    const size_t n = gr[g].n;
-    a_stream[g] = A.take(n * P[g].gm_bytes);
-    s_stream[g] = A.take(n * P[g].gs_bytes);
-    mbuf[g] = A.take(n * 64);
-    kr[g] = A.take(n * 64);
-    fail[g] = A.take(n);
-    hc[g] = A.take(n * 32);
-  }
-  TRY_CUDA(cudaEventRecord(c->fork_ev, s));
-  TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
-  for (size_t g = 0; g < ng; g++) {
-    k_dec_front<<<blocks_for(2 * gr[g].n, 128), 128, 0, c->side>>>(P[g], gr[g].sk, gr[g].ct, a_stream[g], hc[g],
-                                                                    (int)gr[g].n);
-    c->launches++;
-  }
-  TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
+  int total = 0;
+  bool persist_dec = true, persist_re = true;
   int shape_dec = 0, shape_re = 0;
   for (size_t g = 0; g < ng; g++) {
+    KemParams P;
+    make_params(gr[g].set, &P);
+    const size_t n = gr[g].n;
+    HashGroup &h = hg[g];
+    h.P = P;
+    h.first = total;
+    h.n = (int)n;
+    h.sk = gr[g].sk;
+    h.ct = gr[g].ct;
+    h.ss = gr[g].ss;
+    h.a_stream = A.take(n * P.gm_bytes);
+    h.s_stream = A.take(n * P.gs_bytes);
+    h.mbuf = A.take(n * 64);
+    h.kr = A.take(n * 64);
+    h.fail = A.take(n);
+    h.hc = A.take(n * 32);
+    total += (int)n;
     CpaArgs &a = ga[g];
     a = CpaArgs{};
-    a.P = P[g];
-    a.n = (int)gr[g].n;
+    a.P = P;
+    a.n = (int)n;
     a.ct = gr[g].ct;
     a.sk = gr[g].sk;
-    a.m_out = mbuf[g];
+    a.m_out = h.mbuf;
     a.m_out_stride = 64;
     a.copy_hpk = 1;
     a.err = c->d_err;
     CpaArgs &b = gb[g];
     b = CpaArgs{};
-    b.P = P[g];
-    b.n = (int)gr[g].n;
-    b.a_stream = a_stream[g];
-    b.s_stream = s_stream[g];
+    b.P = P;
+    b.n = (int)n;
+    b.a_stream = h.a_stream;
+    b.s_stream = h.s_stream;
     b.pk = gr[g].sk;
-    b.pk_stride = P[g].sk_bytes;
-    b.pk_off = P[g].indcpa_sk_bytes;
-    b.msg = mbuf[g];
+    b.pk_stride = P.sk_bytes;
+    b.pk_off = P.indcpa_sk_bytes;
+    b.msg = h.mbuf;
     b.msg_stride = 64;
     b.ct = gr[g].ct;
-    b.fail = fail[g];
+    b.fail = h.fail;
     b.err = c->d_err;
-    shape_dec = std::max(shape_dec, persist_ctas_per_sm(kDecrypt, P[g].set));
-    shape_re = std::max(shape_re, persist_ctas_per_sm(kReenc, P[g].set));
+    // the persistent kernel only where the autotuner chose it for every set
+    const int sd = persist_ctas_per_sm(kDecrypt, P.set), sr = persist_ctas_per_sm(kReenc, P.set);
+    persist_dec = persist_dec && sd >= 0;
+    persist_re = persist_re && sr >= 0;
+    shape_dec = std::max(shape_dec, sd);
+    shape_re = std::max(shape_re, sr);
   }
-  const size_t tb = mix_table_bytes();
-  host_tabs.assign(2 * tb, 0);
+  const size_t tb = up(mix_table_bytes());
+  host_tabs.assign(mixed_tab_bytes(ng), 0);
   mix_table_build(host_tabs.data(), ga.data(), (int)ng);
   mix_table_build(host_tabs.data() + tb, gb.data(), (int)ng);
+  std::memcpy(host_tabs.data() + 2 * tb, hg.data(), ng * sizeof(HashGroup));
   // (pageable source: the call returns once the bytes are staged)
-  if (upload_tabs) TRY_CUDA(cudaMemcpyAsync(tabs, host_tabs.data(), 2 * tb, cudaMemcpyHostToDevice, s));
+  if (upload_tabs) TRY_CUDA(cudaMemcpyAsync(tabs, host_tabs.data(), host_tabs.size(), cudaMemcpyHostToDevice, s));
   const MixTable *tdec = reinterpret_cast<const MixTable *>(tabs);
   const MixTable *tre = reinterpret_cast<const MixTable *>(tabs + tb);
-  if (cpa_launch_mixed(kDecrypt, ga.data(), (int)ng, tdec, s, shape_dec) != 0) return TMVP_EDEVICE;
-  c->launches++;
-  for (size_t g = 0; g < ng; g++) {
-    k_dec_g<<<blocks_for(gr[g].n, 128), 128, 0, s>>>(P[g], mbuf[g], kr[g], s_stream[g], (int)gr[g].n);
-    c->launches++;
-  }
-  TRY_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));  // join
-  if (cpa_launch_mixed(kReenc, gb.data(), (int)ng, tre, s, shape_re) != 0) return TMVP_EDEVICE;
-  c->launches++;
-  for (size_t g = 0; g < ng; g++) {
-    k_final_key<<<blocks_for(gr[g].n, 128), 128, 0, s>>>(P[g], gr[g].ct, hc[g], kr[g], fail[g], gr[g].sk, gr[g].ss,
-                                                         (int)gr[g].n);
-    c->launches++;
-  }
+  const HashGroup *th = reinterpret_cast<const HashGroup *>(tabs + 2 * tb);
+  const unsigned nb = blocks_for((size_t)total, 128);
+  TRY_CUDA(cudaEventRecord(c->fork_ev, s));
+  TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+  k_mix_front<<<nb, 128, 0, c->side>>>(th, (int)ng, total, 1);
+  TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
+  k_mix_front<<<nb, 128, 0, c->side>>>(th, (int)ng, total, 2);
+  TRY_CUDA(cudaEventRecord(c->hc_ev, c->side));
+  if (cpa_launch_mixed(kDecrypt, ga.data(), (int)ng, tdec, s, persist_dec ? shape_dec : -1) != 0)
+    return TMVP_EDEVICE;
+  k_mix_g<<<nb, 128, 0, s>>>(th, (int)ng, total);
+  TRY_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));  // GenMatrix
+  if (cpa_launch_mixed(kReenc, gb.data(), (int)ng, tre, s, persist_re ? shape_re : -1) != 0) return TMVP_EDEVICE;
+  TRY_CUDA(cudaStreamWaitEvent(s, c->hc_ev, 0));  // H(c)
+  k_mix_final<<<nb, 128, 0, s>>>(th, (int)ng, total);
+  c->launches += 6;
   TRY_CUDA(cudaGetLastError());
   return TMVP_OK;
 }
@@ -1013,8 +1129,7 @@ int tmvp_kem_dec_mixed(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, void *s
   if (r) return set_err(r);
   std::lock_guard<std::mutex> lk(c->mu);
   Guard g(c);
-  const size_t tb = up(mix_table_bytes());
-  if ((r = ensure_ws(c, mixed_ws_bytes(ng, gr) + 2 * tb))) return set_err(r);
+  if ((r = ensure_ws(c, mixed_ws_bytes(ng, gr) + mixed_tab_bytes(ng)))) return set_err(r);
   std::vector<uint8_t> host_tabs;
   uint8_t *tabs = c->ws + mixed_ws_bytes(ng, gr);
   if ((r = mixed_enqueue(c, ng, gr, c->ws, tabs, host_tabs, true, (cudaStream_t)stream))) return set_err(r);
@@ -1042,7 +1157,7 @@ int tmvp_mixed_plan_create(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, tmv
   };
   // the plan owns its workspace: the graph keeps these addresses
   if (cudaMalloc(&p->ws, std::max<size_t>(mixed_ws_bytes(ng, gr), 256)) != cudaSuccess ||
-      cudaMalloc(&p->tabs, 2 * up(mix_table_bytes())) != cudaSuccess)
+      cudaMalloc(&p->tabs, mixed_tab_bytes(ng)) != cudaSuccess)
     return fail(TMVP_ENOMEM);
   if (cudaStreamCreateWithFlags(&p->cs, cudaStreamNonBlocking) != cudaSuccess) return fail(TMVP_EDEVICE);
   // the group tables are fixed for the plan: the capture records no copy of

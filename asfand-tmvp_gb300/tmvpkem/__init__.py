@@ -108,6 +108,7 @@ def lib(build_if_missing: bool = False):
     for nm in ("saber_enc", "saber_dec", "SABLE_enc", "SABLE_dec"):
         getattr(L, nm).restype = None
     L.tmvp_ctx_reserve.argtypes = [P, S]
+    L.tmvp_ctx_set_host_chunk.argtypes = [P, S]
     L.tmvp_kem_dec_batch_noalloc.argtypes = [I, S, P, P, P, I, P]
     L.tmvp_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]
     L.tmvp_server_destroy.argtypes = [P]
@@ -308,6 +309,9 @@ class Context:
         """groups: [(set_id, ss, ct, sk)] of device tensors; one pass."""
         arr = _groups(groups)
         _check(lib().tmvp_kem_dec_mixed(self.h, len(groups), arr, stream), "tmvp_kem_dec_mixed")
+
+    def set_host_chunk(self, n: int):
+        _check(lib().tmvp_ctx_set_host_chunk(self.h, n), "tmvp_ctx_set_host_chunk")
 
     def sync_status(self, stream=None):
         _check(lib().tmvp_ctx_sync_status(self.h, stream), "tmvp_ctx_sync_status")

@@ -248,9 +248,9 @@ def run_ours(args):
 
     # ---- end to end through the C ABI with pinned host buffers
     if args.no_e2e:
-        e2e_ms, e2e_exact, e2e_value = [float("nan")], True, None
+        e2e_ms, e2e_exact, e2e_value, e2e_chunk = [float("nan")], True, None, None
     else:
-        e2e_ms, e2e_exact, e2e_value = _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws)
+        e2e_ms, e2e_exact, e2e_value, e2e_chunk = _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws)
     # ---- bit-exactness against the CPU oracle on a sample
     oracle_ok = None
     if not args.no_oracle:
@@ -275,7 +275,7 @@ def run_ours(args):
                 "peak_source": f"{peak_src} bf16 dense (schoolbook-equivalent integer ops)",
                 "traffic": traffic}
     else:
-        per_inst = {"shake_jobs": 32 + 3744, "dec_front": 32 + 1088 + 3744 + 32,
+        per_inst = {"shake_jobs": 32 + 3744, "dec_front": 32 + 3744, "dec_hash_ct": 1088 + 32,
                     "dec_g": 64 + 64 + 768, "final_key": 64 + 1 + 32 + 1088 + 32}
         byts = n * per_inst.get(name, 0)
         ach = byts / avg_s / 1e9
@@ -303,7 +303,8 @@ def run_ours(args):
         "roofline": roof,
         "stages_ms_per_step": {k: v[1] / max(v[0], 1) for k, v in stages.items()},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * (CT_BYTES + SK_BYTES),
-                "d2h_bytes_per_step": n * 32, "ms_per_step": statistics.mean(e2e_ms)},
+                "d2h_bytes_per_step": n * 32, "ms_per_step": statistics.mean(e2e_ms),
+                "host_chunk": e2e_chunk},
         "oracle_sample_note": "256 random instances decapsulated by the CPU oracle and compared",
         "gpu_launches": launches,
         "clocks": clocks,
@@ -330,18 +331,26 @@ def _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws):
     sk_h = sk.cpu().pin_memory()
     ss_h = torch.empty((n, 32), dtype=torch.uint8).pin_memory()
     ke = max(3, args.steps // 2)
-    for _ in range(min(2, args.warmup)):
-        ctx.kem_dec_ptr(SABER, n, ss_h, ct_h, sk_h, T.FORM_AUTO, sp)
-    e2e_ms = []
-    for _ in range(ke):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        ctx.kem_dec_ptr(SABER, n, ss_h, ct_h, sk_h, T.FORM_AUTO, sp)
-        b.record(stream)
-        b.synchronize()
-        e2e_ms.append(a.elapsed_time(b))
-    e2e_exact = bool(torch.equal(ss_h, ss_ref.cpu()))
-    return e2e_ms, e2e_exact, ws * n / (statistics.mean(e2e_ms) / 1e3)
+    best = None
+    # the copy/compute chunk of the host-buffer path: the library's knob, set per run
+    for chunk in (8192, 16384, 32768, 0):
+        ctx.set_host_chunk(chunk)
+        for _ in range(min(2, args.warmup)):
+            ctx.kem_dec_ptr(SABER, n, ss_h, ct_h, sk_h, T.FORM_AUTO, sp)
+        e2e_ms = []
+        for _ in range(ke):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.kem_dec_ptr(SABER, n, ss_h, ct_h, sk_h, T.FORM_AUTO, sp)
+            b.record(stream)
+            b.synchronize()
+            e2e_ms.append(a.elapsed_time(b))
+        e2e_exact = bool(torch.equal(ss_h, ss_ref.cpu()))
+        if best is None or statistics.mean(e2e_ms) < statistics.mean(best[0]):
+            best = (e2e_ms, e2e_exact, chunk)
+    ctx.set_host_chunk(16384)
+    e2e_ms, e2e_exact, chunk = best
+    return e2e_ms, e2e_exact, ws * n / (statistics.mean(e2e_ms) / 1e3), chunk
 
 
 def _event_ms(stream, fn, steps):

@@ -149,6 +149,11 @@ int tmvp_matvec_batch(tmvp_ctx *ctx, size_t n, int l, int eq, int transpose, uin
 /* Reserve `bytes` of device workspace up front (so that later calls do not
  * allocate).  Fails with TMVP_ENOMEM above the context's budget. */
 int tmvp_ctx_reserve(tmvp_ctx *ctx, size_t bytes);
+/* Batched decapsulation with host-resident ct / sk copies and processes them
+ * in chunks of n instances (two copy streams), so that copies overlap the
+ * kernels of the previous chunk; 0 = one copy, then the kernels.  Default
+ * 16384; n must be 0 or >= 1024. */
+int tmvp_ctx_set_host_chunk(tmvp_ctx *ctx, size_t n);
 
 /* ---------------------------------------------------------------------------
  * Request-serving loop with device-resident keys and continuous batching.
@@ -237,10 +242,13 @@ int tmvp_ctx_sync_status(tmvp_ctx *ctx, void *stream);
  * Mixed-parameter decapsulation.  No counterpart in the reference (one
  * parameter set per build, params.h:4).
  *
- * Up to 64 groups, each with its own parameter set (any of the six) and its
- * own device buffers (16-byte aligned, this context's GPU), decapsulate in one
- * pass: every IND-CPA step is ONE persistent tcgen05 launch over all groups;
- * the Keccak stages run per group on two streams.  tmvp_mixed_plan_create
+ * Up to 64 groups (at most 2^30 instances in all), each with its own
+ * parameter set (any of the six) and its own device buffers (16-byte aligned,
+ * this context's GPU), decapsulate in one pass: every stage is ONE launch over
+ * all groups -- GenMatrix, H(c), G and the final key as Keccak kernels, the two
+ * IND-CPA steps on the tcgen05 tensor cores (one CTA per instance, or the
+ * persistent pipelined kernel where the autotuner chose it for every set in
+ * the pass).  tmvp_mixed_plan_create
  * captures the pass for fixed buffers into a CUDA graph (the plan owns its
  * workspace); tmvp_mixed_plan_launch replays it, so the caller refills the
  * ciphertext / key buffers and relaunches.  Asynchronous on `stream`; use

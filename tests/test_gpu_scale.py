@@ -71,3 +71,36 @@ def test_matvec_benchmark_size(kem, oracle, form):
     summ = (o1.cpu().numpy().view(np.uint16).astype(np.uint32) +
             o2.cpu().numpy().view(np.uint16).astype(np.uint32)) & 8191
     assert np.array_equal(summ.astype(np.uint16), got)
+
+
+def test_chunked_host_decapsulation(kem):
+    """Host inputs larger than one chunk (16384) go through the overlapped
+    copy / compute path; the keys equal the device-buffer path's, including a
+    ragged last chunk and host outputs."""
+    import torch
+    T, ctx = kem
+    dev = torch.device("cuda", 0)
+    n = 40000
+    z = T.sizes(T.SABER)
+    coins = torch.from_numpy(T.splitmix_bytes(31, n * 96).reshape(n, 96)).to(dev)
+    ec = torch.from_numpy(T.splitmix_bytes(32, n * 32).reshape(n, 32)).to(dev)
+    pk = torch.empty((n, z.pk_bytes), dtype=torch.uint8, device=dev)
+    sk = torch.empty((n, z.sk_bytes), dtype=torch.uint8, device=dev)
+    ct = torch.empty((n, z.ct_bytes), dtype=torch.uint8, device=dev)
+    ss = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+    ctx.kem_keypair_ptr(T.SABER, n, pk, sk, coins)
+    ctx.kem_enc_ptr(T.SABER, n, ct, ss, pk, ec)
+    ct[n - 3, 7] ^= 1  # one rejection in the last chunk
+    torch.cuda.synchronize()
+    want = torch.empty_like(ss)
+    ctx.kem_dec_ptr(T.SABER, n, want, ct, sk)
+    torch.cuda.synchronize()
+    ct_h, sk_h = ct.cpu().pin_memory(), sk.cpu().pin_memory()
+    out_h = torch.zeros((n, 32), dtype=torch.uint8).pin_memory()
+    ctx.kem_dec_ptr(T.SABER, n, out_h, ct_h, sk_h)   # host in, host out
+    assert torch.equal(out_h, want.cpu())
+    out_d = torch.zeros_like(ss)
+    ctx.kem_dec_ptr(T.SABER, n, out_d, ct_h, sk)     # host ct, device sk and out
+    torch.cuda.synchronize()
+    assert torch.equal(out_d, want)
+    assert not torch.equal(want[n - 3], ss[n - 3]) and torch.equal(want[:n - 3], ss[:n - 3])
