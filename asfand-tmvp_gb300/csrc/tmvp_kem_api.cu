@@ -243,6 +243,10 @@ int run_cpa(tmvp_ctx *c, int form, int op, CpaArgs &a, cudaStream_t s) {
 
 inline unsigned blocks_for(size_t threads, unsigned bs) { return (unsigned)((threads + bs - 1) / bs); }
 
+// Threads per block of the Keccak kernels (one sponge per thread): small
+// blocks spread a batch evenly over the 152 SMs of an ALU-bound stage.
+constexpr unsigned kHashBlock = 64;
+
 int check_common(tmvp_ctx *c, int set, size_t n, int form, KemParams *P) {
   if (!c) return TMVP_EINVAL;
   if (!make_params(set, P)) return TMVP_EINVAL;
@@ -316,12 +320,12 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
   {
     StageTimer tm_(c, "dec_front", c->side);
-    k_dec_front<<<blocks_for(n, 128), 128, 0, c->side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 1);
+    k_dec_front<<<blocks_for(n, kHashBlock), kHashBlock, 0, c->side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 1);
   }
   TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
   {
     StageTimer tm_(c, "dec_hash_ct", c->side);
-    k_dec_front<<<blocks_for(n, 128), 128, 0, c->side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
+    k_dec_front<<<blocks_for(n, kHashBlock), kHashBlock, 0, c->side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
   }
   c->launches += 2;
   TRY_CUDA(cudaEventRecord(c->hc_ev, c->side));
@@ -336,7 +340,7 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   if ((r = run_cpa(c, form, kDecrypt, a, s))) return r;
   {
     StageTimer tm_(c, "dec_g", s);
-    k_dec_g<<<blocks_for(n, 128), 128, 0, s>>>(P, w.mbuf, w.kr, w.s_stream, (int)n);
+    k_dec_g<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, w.mbuf, w.kr, w.s_stream, (int)n);
   }
   c->launches++;
   TRY_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));  // join: GenMatrix
@@ -356,7 +360,7 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   TRY_CUDA(cudaStreamWaitEvent(s, c->hc_ev, 0));  // join: H(c)
   {
     StageTimer tm_(c, "final_key", s);
-    k_final_key<<<blocks_for(n, 128), 128, 0, s>>>(P, ct, w.hc, w.kr, w.fail, sk, ss, (int)n);
+    k_final_key<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, ct, w.hc, w.kr, w.fail, sk, ss, (int)n);
   }
   c->launches++;
   return TMVP_OK;
@@ -532,7 +536,7 @@ int tmvp_kem_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *p
   ShakeJob j1{bco.dev, 96, 32, s_stream, (size_t)P.gs_bytes, P.gs_bytes, 0, nullptr, 0, 0};
   {
     StageTimer tm_(c, "shake_jobs", s);
-    k_shake_jobs<<<blocks_for(2 * n, 128), 128, 0, s>>>(j0, j1, (int)n);
+    k_shake_jobs<<<blocks_for(2 * n, kHashBlock), kHashBlock, 0, s>>>(j0, j1, (int)n);
   }
   c->launches++;
   CpaArgs a{};
@@ -546,7 +550,7 @@ int tmvp_kem_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *p
   if ((r = run_cpa(c, form, kKeygen, a, s))) return set_err(r);
   {
     StageTimer tm_(c, "kp_final", s);
-    k_kp_final<<<blocks_for(n, 128), 128, 0, s>>>(P, bpk.dev, bsk.dev, bco.dev, (int)n);
+    k_kp_final<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, bpk.dev, bsk.dev, bco.dev, (int)n);
   }
   c->launches++;
   if ((r = download(bpk, s)) || (r = download(bsk, s))) return set_err(r);
@@ -578,7 +582,7 @@ int tmvp_kem_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, u
   if ((r = upload(bpk, s)) || (r = upload(bco, s))) return set_err(r);
   {
     StageTimer tm_(c, "enc_front", s);
-    k_enc_front<<<blocks_for(2 * n, 128), 128, 0, s>>>(P, bpk.dev, bco.dev, mbuf, kr, s_stream,
+    k_enc_front<<<blocks_for(2 * n, kHashBlock), kHashBlock, 0, s>>>(P, bpk.dev, bco.dev, mbuf, kr, s_stream,
                                                        a_stream, (int)n);
   }
   c->launches++;
@@ -596,7 +600,7 @@ int tmvp_kem_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, u
   if ((r = run_cpa(c, form, kEncrypt, a, s))) return set_err(r);
   {
     StageTimer tm_(c, "final_key", s);
-    k_final_key<<<blocks_for(n, 128), 128, 0, s>>>(P, bct.dev, nullptr, kr, nullptr, nullptr, bss.dev, (int)n);
+    k_final_key<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, bct.dev, nullptr, kr, nullptr, nullptr, bss.dev, (int)n);
   }
   c->launches++;
   if ((r = download(bct, s)) || (r = download(bss, s))) return set_err(r);
@@ -691,7 +695,7 @@ int tmvp_indcpa_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t
   ShakeJob j1{bse.dev, 64, 32, s_stream, (size_t)P.gs_bytes, P.gs_bytes, 0, nullptr, 0, 0};
   {
     StageTimer tm_(c, "shake_jobs", s);
-    k_shake_jobs<<<blocks_for(2 * n, 128), 128, 0, s>>>(j0, j1, (int)n);
+    k_shake_jobs<<<blocks_for(2 * n, kHashBlock), kHashBlock, 0, s>>>(j0, j1, (int)n);
   }
   c->launches++;
   CpaArgs a{};
@@ -737,7 +741,7 @@ int tmvp_indcpa_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct
               (size_t)P.gm_bytes, P.gm_bytes, 0, nullptr, 0, 0};
   {
     StageTimer tm_(c, "shake_jobs", s);
-    k_shake_jobs<<<blocks_for(2 * n, 128), 128, 0, s>>>(j0, j1, (int)n);
+    k_shake_jobs<<<blocks_for(2 * n, kHashBlock), kHashBlock, 0, s>>>(j0, j1, (int)n);
   }
   c->launches++;
   CpaArgs a{};
@@ -1076,20 +1080,20 @@ int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws,
   const MixTable *tdec = reinterpret_cast<const MixTable *>(tabs);
   const MixTable *tre = reinterpret_cast<const MixTable *>(tabs + tb);
   const HashGroup *th = reinterpret_cast<const HashGroup *>(tabs + 2 * tb);
-  const unsigned nb = blocks_for((size_t)total, 128);
+  const unsigned nb = blocks_for((size_t)total, kHashBlock);
   TRY_CUDA(cudaEventRecord(c->fork_ev, s));
   TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
-  k_mix_front<<<nb, 128, 0, c->side>>>(th, (int)ng, total, 1);
+  k_mix_front<<<nb, kHashBlock, 0, c->side>>>(th, (int)ng, total, 1);
   TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
-  k_mix_front<<<nb, 128, 0, c->side>>>(th, (int)ng, total, 2);
+  k_mix_front<<<nb, kHashBlock, 0, c->side>>>(th, (int)ng, total, 2);
   TRY_CUDA(cudaEventRecord(c->hc_ev, c->side));
   if (cpa_launch_mixed(kDecrypt, ga.data(), (int)ng, tdec, s, persist_dec ? shape_dec : -1) != 0)
     return TMVP_EDEVICE;
-  k_mix_g<<<nb, 128, 0, s>>>(th, (int)ng, total);
+  k_mix_g<<<nb, kHashBlock, 0, s>>>(th, (int)ng, total);
   TRY_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));  // GenMatrix
   if (cpa_launch_mixed(kReenc, gb.data(), (int)ng, tre, s, persist_re ? shape_re : -1) != 0) return TMVP_EDEVICE;
   TRY_CUDA(cudaStreamWaitEvent(s, c->hc_ev, 0));  // H(c)
-  k_mix_final<<<nb, 128, 0, s>>>(th, (int)ng, total);
+  k_mix_final<<<nb, kHashBlock, 0, s>>>(th, (int)ng, total);
   c->launches += 6;
   TRY_CUDA(cudaGetLastError());
   return TMVP_OK;
