@@ -2,9 +2,8 @@
 //
 // Callers that cannot allocate device memory use this entry point. Examples
 // are a host application whose GPU memory is carved up by its own pool
-// allocator, a serving process that forbids allocation after start-up so its
-// latency stays flat, and code that records the call into a graph where
-// cudaMalloc is not allowed.  Instead of a context workspace it uses one
+// allocator, and a serving process that forbids allocation after start-up so
+// its latency stays flat.  Instead of a context workspace it uses one
 // fixed array in device global memory, declared below, which every GPU that
 // loads the library holds until the process exits.
 //

@@ -270,8 +270,8 @@ void tmvp_mixed_plan_destroy(tmvp_mixed_plan *plan);
 
 /* Decapsulation that allocates nothing.  No counterpart in the reference.
  * For callers that cannot call cudaMalloc: a host whose GPU memory is owned
- * by its own pool allocator, a serving process that forbids allocation after
- * start-up, or code recorded into a graph where allocation is not allowed.
+ * by its own pool allocator, or a serving process that forbids allocation
+ * after start-up so that its latency stays flat.
  * Instead of a context workspace it uses one fixed array in device global
  * memory (7.4 MiB, sized for TMVP_NOALLOC_MAX_BATCH instances of the largest
  * parameter set), which every GPU that loads the library holds until the

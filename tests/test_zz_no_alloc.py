@@ -2,7 +2,7 @@
 
 Callers that cannot allocate device memory -- a host whose GPU memory belongs
 to its own pool allocator, a serving process that forbids allocation after
-start-up, code recorded into a graph -- use this entry point; it works out of
+start-up so its latency stays flat -- use this entry point; it works out of
 a fixed array in device global memory instead of a context workspace.  The
 test calls it through the C ABI twice in a row and checks each result against
 the allocating entry point (tmvp_kem_dec_batch), bit for bit, and that a batch
