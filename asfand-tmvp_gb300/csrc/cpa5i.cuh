@@ -1,5 +1,5 @@
 // cpa5i.cuh — the tcgen05 IND-CPA kernel specialised per parameter set: one
-// CTA of 128 threads per instance, with every width, count and offset a
+// CTA of 256 threads per instance, with every width, count and offset a
 // compile-time constant.
 //
 // Per instance:
@@ -53,6 +53,10 @@ struct ShapeC {
 
 constexpr int al16c(int x) { return (x + 15) & ~15; }
 
+// Threads per CTA (one instance): eight warps shorten every staging phase of
+// an instance; tensor memory is read by warps w and w + 4 (two M halves).
+constexpr int kI5Threads = 256;
+
 // Shared-memory layout of one CTA (byte offsets).  The operand region ENG
 // holds the Hankel core matrices H (l x kHankelBytes), the digit columns B and
 // s_ext; the packed GenMatrix / GenSecret / b streams and the packed secret
@@ -71,9 +75,13 @@ struct LayoutC {
   static constexpr bool HAS_CT = OP == kReenc || OP == kDecrypt;
   static constexpr bool HAS_SK = OP == kDecrypt;
   static constexpr bool NARROW = S::NCOLS <= 8;
+  // FOLD: both M halves in one MMA (columns 0..NCOLS-1 rows 0..127, columns
+  // NCOLS..2 NCOLS-1 rows 128..255): 12 block operands of 32 K rows per j
+  static constexpr bool FOLD = 2 * S::NCOLS <= 8;
   static constexpr int GROUPS = NARROW ? 1 : S::NU / 8;         // stored column groups
-  static constexpr int LBO_B = GROUPS * 128 + 16;
-  static constexpr int BJ = 16 * LBO_B;                          // digit columns of one j
+  static constexpr int LBO_B = FOLD ? 128 : GROUPS * 128 + 16;
+  static constexpr int BLK = 2 * 128 + 16;                       // FOLD: one block (2 K chunks + pad)
+  static constexpr int BJ = FOLD ? 12 * BLK : 16 * LBO_B;        // digit columns of one j
   static constexpr int ENG = 0;
   static constexpr int H = ENG;
   static constexpr int A = H;                                    // streams inside H
@@ -122,13 +130,13 @@ __device__ __forceinline__ void unpack8c(const uint8_t *base, int byte0, uint32_
   }
 }
 
-// One instance (CTA of 128 threads; sm: its dynamic shared memory).
+// One instance (CTA of kI5Threads threads; sm: its dynamic shared memory).
 template <int OP, int SET>
 __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst, uint8_t *sm) {
   using C = SetC<SET>;
   using S = ShapeC<OP, SET>;
   using LO = LayoutC<OP, SET>;
-  constexpr int L = C::L, NU = S::NU, NT = 128;
+  constexpr int L = C::L, NU = S::NU, NT = kI5Threads;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t mbar_in = smem_u32(sm + LO::BAR), mbar_mma = mbar_in + 8;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + LO::BAR + 16);
@@ -230,20 +238,47 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
         unpack8c<S::WB>(sm + LO::B, (32 * j + grp) * S::WB, X);
       }
       const int kq = 31 - grp;  // coefficients 8grp..8grp+7 are rows k' = 8kq+7..8kq
-      uint8_t *base = Bm + j * LO::BJ + (kq >> 1) * LO::LBO_B + 8 * (kq & 1);
       const int cb = p < S::RA ? p * S::DA : S::RA * S::DA + (p - S::RA) * S::DB;
       const int D = p < S::RA ? S::DA : S::DB;
+      if constexpr (LO::FOLD) {
+        // K step c = kq / 4 feeds block c (top half, columns 0..) and block
+        // c + 4 (bottom half, columns NCOLS..)
+        const int c = kq >> 2;
+        uint8_t *b1 = Bm + j * LO::BJ + c * LO::BLK + ((kq >> 1) & 1) * 128 + 8 * (kq & 1);
+        uint8_t *b2 = b1 + 4 * LO::BLK;
 #pragma unroll
-      for (int d = 0; d < (S::DA > S::DB ? S::DA : S::DB); d++) {
-        if (d < D) {
-          const int n = cb + d;
+        for (int d = 0; d < S::DB; d++) {
           const uint2 v = digit8<kFp8Tcgen05>(X, d);
-          *reinterpret_cast<uint2 *>(base + (n >> 3) * 128 + (n & 7) * 16) =
-              make_uint2(__byte_perm(v.y, 0, 0x0123), __byte_perm(v.x, 0, 0x0123));
+          const uint2 w = make_uint2(__byte_perm(v.y, 0, 0x0123), __byte_perm(v.x, 0, 0x0123));
+          *reinterpret_cast<uint2 *>(b1 + (cb + d) * 16) = w;
+          *reinterpret_cast<uint2 *>(b2 + (S::NCOLS + cb + d) * 16) = w;
+        }
+      } else {
+        uint8_t *base = Bm + j * LO::BJ + (kq >> 1) * LO::LBO_B + 8 * (kq & 1);
+#pragma unroll
+        for (int d = 0; d < (S::DA > S::DB ? S::DA : S::DB); d++) {
+          if (d < D) {
+            const int n = cb + d;
+            const uint2 v = digit8<kFp8Tcgen05>(X, d);
+            *reinterpret_cast<uint2 *>(base + (n >> 3) * 128 + (n & 7) * 16) =
+                make_uint2(__byte_perm(v.y, 0, 0x0123), __byte_perm(v.x, 0, 0x0123));
+          }
         }
       }
     }
-    constexpr int PADC = LO::GROUPS * 8 - S::NCOLS;  // zero columns of the stored groups
+    if constexpr (LO::FOLD) {
+      // zero slots of the blocks: the absent half (top for blocks 8..11,
+      // bottom for blocks 0..3) and the columns past 2 NCOLS
+      for (int idx = tid; idx < L * 12 * 2 * 8; idx += NT) {
+        const int col = idx & 7, a = (idx >> 3) & 1, m = (idx >> 4) % 12, j = idx / (16 * 12);
+        const bool top = col < S::NCOLS, bottom = col >= S::NCOLS && col < 2 * S::NCOLS;
+        const bool data = (top && m < 8) || (bottom && m >= 4);
+        if (!data)
+          *reinterpret_cast<uint4 *>(Bm + j * LO::BJ + m * LO::BLK + a * 128 + col * 16) =
+              make_uint4(0u, 0u, 0u, 0u);
+      }
+    }
+    constexpr int PADC = LO::FOLD ? 0 : LO::GROUPS * 8 - S::NCOLS;  // zero columns of the stored groups
     for (int idx = tid; idx < L * PADC * 16; idx += NT) {
       const int j = idx / (PADC * 16), r = idx % (PADC * 16), n = S::NCOLS + r % PADC, ac = r / PADC;
       *reinterpret_cast<uint4 *>(Bm + j * LO::BJ + ac * LO::LBO_B + (n >> 3) * 128 + (n & 7) * 16) =
@@ -266,6 +301,19 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
     constexpr uint32_t idesc = umma_idesc_e4m3(NU);
     const uint64_t ad0 = umma_desc(smem_u32(H), 256, 128);
     const uint32_t b0 = smem_u32(Bm), z0 = smem_u32(sm + LO::ZERO);
+    if constexpr (LO::FOLD) {
+      // window m of the Hankel sequence (core 4m) times block m: 12 MMAs per j
+#pragma unroll
+      for (int j = 0; j < L; j++) {
+#pragma unroll
+        for (int m = 0; m < 12; m++) {
+          const uint32_t bs = b0 + j * LO::BJ + m * LO::BLK;
+          const uint64_t bd = umma_desc(bs, 128, z0 - bs);
+          const uint64_t ad = ad0 + (uint64_t)((j * kHankelBytes + 4 * m * 128) >> 4);
+          umma_f8(tmem, ad, bd, idesc, (j | m) != 0);
+        }
+      }
+    } else {
 #pragma unroll
     for (int j = 0; j < L; j++) {
 #pragma unroll
@@ -280,6 +328,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
         }
       }
     }
+    }
     umma_commit(mbar_mma);
   }
   // 4. accumulators -> int32 columns (one warp polls, the others wait in the barrier)
@@ -289,14 +338,29 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
     done = __syncthreads_and(fin) != 0;
   }
   tc_fence_after();
-  if (done) {
+  // warp w reads TMEM lanes 32 (w % 4) .. +31; warps 4..7 take the second M half
+  const int q4 = warp & 3, hsel = warp >> 2;
+  if (done && LO::FOLD) {
+    // columns c < NCOLS: row 32 q4 + lane; columns NCOLS + c: that row + 128
+    if (hsel == 0) {
+      uint32_t r[16];
+      tmem_ld16(tmem + ((uint32_t)(32 * q4) << 16), r);
+      const int row = 32 * q4 + lane;
+#pragma unroll
+      for (int c = 0; c < S::NCOLS; c++) {
+        acc[c * 256 + row] = __float2int_rn(__uint_as_float(r[c]));
+        acc[c * 256 + 128 + row] = __float2int_rn(__uint_as_float(r[S::NCOLS + c]));
+      }
+    }
+  } else if (done) {
 #pragma unroll
     for (int hh = 0; hh < 2; hh++) {
+      if (NT == 256 && hh != hsel) continue;
 #pragma unroll
       for (int cc = 0; cc < NU; cc += 16) {
         uint32_t r[16];
-        tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + hh * NU + cc, r);
-        const int row = 128 * hh + 32 * warp + lane;
+        tmem_ld16(tmem + ((uint32_t)(32 * q4) << 16) + hh * NU + cc, r);
+        const int row = 128 * hh + 32 * q4 + lane;
 #pragma unroll
         for (int c = 0; c < 16; c++)
           if (cc + c < S::NCOLS) acc[(cc + c) * 256 + row] = __float2int_rn(__uint_as_float(r[c]));
@@ -446,7 +510,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
 }
 
 template <int OP, int SET>
-__global__ void __launch_bounds__(128, 4) k_cpa5i(CpaArgs a) {
+__global__ void __launch_bounds__(kI5Threads, 2) k_cpa5i(CpaArgs a) {
   extern __shared__ __align__(16) uint8_t sm[];
   cpa5i_body<OP, SET>(a, blockIdx.x, sm);
 }
@@ -454,7 +518,7 @@ __global__ void __launch_bounds__(128, 4) k_cpa5i(CpaArgs a) {
 // Mixed launch: CTA gi runs instance gi of the group table R (one CTA per
 // instance over all groups, whatever their parameter sets).
 template <int OP>
-__global__ void __launch_bounds__(128, 4) k_cpa5m(const __grid_constant__ MixRef R) {
+__global__ void __launch_bounds__(kI5Threads, 2) k_cpa5m(const __grid_constant__ MixRef R) {
   extern __shared__ __align__(16) uint8_t sm[];
   const int gi = blockIdx.x;
   const int g = find_group(R, gi);
@@ -494,7 +558,7 @@ inline int cap_tmem_residency(F fn, int &smem, int cols) {
     if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
       return (int)e;
     int nb = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, smem)) != cudaSuccess) return (int)e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kI5Threads, smem)) != cudaSuccess) return (int)e;
     if (nb <= cap) return 0;
     smem += 2048;
   }
@@ -526,7 +590,7 @@ inline int launch_cpa5m(const CpaArgs *groups, int ng, const MixTable *dev_tab, 
   if (e != cudaSuccess) return (int)e;
   int rc = cap_tmem_residency(fn, smem, cols);
   if (rc) return rc;
-  fn<<<R.total, 128, smem, s>>>(R);
+  fn<<<R.total, kI5Threads, smem, s>>>(R);
   return (int)cudaGetLastError();
 }
 
@@ -545,11 +609,11 @@ inline int launch_cpa5i(const CpaArgs &a, cudaStream_t s) {
     if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
       return (int)e;
     int nb = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, smem)) != cudaSuccess) return (int)e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kI5Threads, smem)) != cudaSuccess) return (int)e;
     if (nb <= cap) break;
     smem += 2048;
   }
-  fn<<<a.n, 128, smem, s>>>(a);
+  fn<<<a.n, kI5Threads, smem, s>>>(a);
   return (int)cudaGetLastError();
 }
 

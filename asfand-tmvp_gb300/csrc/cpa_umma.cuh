@@ -117,13 +117,27 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
-// Bounded wait for phase `parity` of an mbarrier: gives up after about two
-// seconds (or 2^26 polls) and returns false.
+// try_wait with a suspend-time hint: the thread sleeps until the phase
+// completes or about `ns` nanoseconds pass, instead of spinning.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint32_t mbar, uint32_t parity, uint32_t ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(mbar), "r"(parity), "r"(ns)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for phase `parity` of an mbarrier: sleeps in 20 us slices and
+// gives up after about two seconds (or 2^22 polls), returning false.
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
   const uint64_t t0 = global_ns();
-  for (uint32_t it = 0; it < (1u << 26); it++) {
-    if (mbar_try_wait(mbar, parity)) return true;
-    if ((it & 255u) == 255u && global_ns() - t0 > 2000000000ull) return false;
+  for (uint32_t it = 0; it < (1u << 22); it++) {
+    if (mbar_try_wait_sleep(mbar, parity, 20000u)) return true;
+    if ((it & 15u) == 15u && global_ns() - t0 > 2000000000ull) return false;
   }
   return false;
 }
