@@ -7,7 +7,7 @@
 //             -> k_cpa<kKeygen> -> k_kp_final (H(pk), z)
 //   encaps  : k_enc_front (H(coins), H(pk), G, GenSecret; GenMatrix)
 //             -> k_cpa<kEncrypt> -> k_final_key
-//   decaps  : k_dec_front (GenMatrix, then H(c)) on a side stream, concurrent
+//   decaps  : k_dec_front (GenMatrix; H(c)) on two side streams, concurrent
 //             with k_cpa<kDecrypt> -> k_dec_g; k_cpa<kReenc> waits only for
 //             GenMatrix, k_final_key (implicit rejection) also for H(c)
 // They replace the launch sequences of saber_enc / saber_dec
@@ -56,7 +56,8 @@ struct tmvp_ctx {
   size_t ws_cap = 0;
   int *d_err = nullptr;   // device-side input-range flag
   uint64_t launches = 0;
-  cudaStream_t side = nullptr;          // second stream for independent stages
+  cudaStream_t side = nullptr;          // GenMatrix beside the decryption (highest priority)
+  cudaStream_t side2 = nullptr;         // H(c), which only the final key needs (lowest priority)
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr, hc_ev = nullptr;
   size_t host_chunk = 16384;                       // chunk of host-input decapsulation (0: none)
   cudaStream_t copy[2] = {};                       // host-to-device copies of chunked calls
@@ -311,7 +312,7 @@ DecScratch dec_scratch(const KemParams &P, size_t n, Arena &A) {
 }
 
 // Decapsulation of n instances in device memory (16-byte aligned):
-// GenMatrix, then H(c), on the side stream, concurrent with the decryption and
+// GenMatrix and H(c) on two side streams, concurrent with the decryption and
 // G on s; the re-encryption waits for GenMatrix, the final key for H(c).
 int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const uint8_t *ct,
                  const uint8_t *sk, int form, cudaStream_t s, const DecScratch &w) {
@@ -323,12 +324,13 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
     k_dec_front<<<blocks_for(n, kHashBlock), kHashBlock, 0, c->side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 1);
   }
   TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
+  TRY_CUDA(cudaStreamWaitEvent(c->side2, c->fork_ev, 0));
   {
-    StageTimer tm_(c, "dec_hash_ct", c->side);
-    k_dec_front<<<blocks_for(n, kHashBlock), kHashBlock, 0, c->side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
+    StageTimer tm_(c, "dec_hash_ct", c->side2);
+    k_dec_front<<<blocks_for(n, kHashBlock), kHashBlock, 0, c->side2>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
   }
   c->launches += 2;
-  TRY_CUDA(cudaEventRecord(c->hc_ev, c->side));
+  TRY_CUDA(cudaEventRecord(c->hc_ev, c->side2));
   CpaArgs a{};
   a.P = P;
   a.n = (int)n;
@@ -420,8 +422,14 @@ int tmvp_ctx_create(int device, size_t mem_budget, tmvp_ctx **out) {
   c->device = device;
   c->budget = mem_budget;
   Guard g(c);
+  // GenMatrix, which the re-encryption waits for, runs at the highest stream
+  // priority, so its blocks are scheduled ahead of the decryption beside it;
+  // H(c), needed only by the final key, runs at the lowest and fills gaps
+  int pri_low = 0, pri_high = 0;
+  cudaDeviceGetStreamPriorityRange(&pri_low, &pri_high);
   if (cudaMalloc(&c->d_err, sizeof(int)) != cudaSuccess || cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, pri_high) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&c->side2, cudaStreamNonBlocking, pri_low) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->hc_ev, cudaEventDisableTiming) != cudaSuccess ||
@@ -450,6 +458,7 @@ void tmvp_ctx_destroy(tmvp_ctx *c) {
     if (c->ws) cudaFree(c->ws);
     if (c->d_err) cudaFree(c->d_err);
     if (c->side) cudaStreamDestroy(c->side);
+    if (c->side2) cudaStreamDestroy(c->side2);
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->join_ev) cudaEventDestroy(c->join_ev);
     if (c->hc_ev) cudaEventDestroy(c->hc_ev);
@@ -1085,8 +1094,9 @@ int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws,
   TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
   k_mix_front<<<nb, kHashBlock, 0, c->side>>>(th, (int)ng, total, 1);
   TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
-  k_mix_front<<<nb, kHashBlock, 0, c->side>>>(th, (int)ng, total, 2);
-  TRY_CUDA(cudaEventRecord(c->hc_ev, c->side));
+  TRY_CUDA(cudaStreamWaitEvent(c->side2, c->fork_ev, 0));
+  k_mix_front<<<nb, kHashBlock, 0, c->side2>>>(th, (int)ng, total, 2);
+  TRY_CUDA(cudaEventRecord(c->hc_ev, c->side2));
   if (cpa_launch_mixed(kDecrypt, ga.data(), (int)ng, tdec, s, persist_dec ? shape_dec : -1) != 0)
     return TMVP_EDEVICE;
   k_mix_g<<<nb, kHashBlock, 0, s>>>(th, (int)ng, total);
