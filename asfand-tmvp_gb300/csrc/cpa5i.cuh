@@ -5,7 +5,7 @@
 // Per instance:
 //   1. the packed inputs arrive by TMA bulk copies (cp.async.bulk) issued by
 //      one thread, counted on an mbarrier;
-//   2. secrets (CBD or unpacked), radix-16 e4m3 digit columns with K
+//   2. secrets (CBD or unpacked), radix-16 e4m3 digit columns (r16_digits) with K
 //      reversed, s_ext and the Hankel core matrices (cpa_umma.cuh);
 //   3. one thread issues the 16 l tcgen05.mma (M = 128, N = 16 / 32, K = 32)
 //      into tensor memory and commits them to an mbarrier;
@@ -43,7 +43,7 @@ struct ShapeC {
   static constexpr int R = OP == kDecrypt ? 1 : (OP == kKeygen ? L : L + 1);
   static constexpr int RA = OP == kDecrypt ? 0 : L;
   static constexpr int WA = C::EQ, WB = C::EP;
-  static constexpr int DA = (WA + 3) / 4, DB = (WB + 3) / 4;
+  static constexpr int DA = r16_digits(WA), DB = r16_digits(WB);
   static constexpr int NCOLS = RA * DA + (R - RA) * DB;
   static constexpr int NU = NCOLS <= 16 ? 16 : 32;
   static constexpr int TMEM_COLS = NU <= 16 ? 32 : 64;
@@ -248,7 +248,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
         uint8_t *b2 = b1 + 4 * LO::BLK;
 #pragma unroll
         for (int d = 0; d < S::DB; d++) {
-          const uint2 v = digit8<kFp8Tcgen05>(X, d);
+          const uint2 v = digit8<kFp8Tcgen05>(X, d, S::WB);
           const uint2 w = make_uint2(__byte_perm(v.y, 0, 0x0123), __byte_perm(v.x, 0, 0x0123));
           *reinterpret_cast<uint2 *>(b1 + (cb + d) * 16) = w;
           *reinterpret_cast<uint2 *>(b2 + (S::NCOLS + cb + d) * 16) = w;
@@ -259,7 +259,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
         for (int d = 0; d < (S::DA > S::DB ? S::DA : S::DB); d++) {
           if (d < D) {
             const int n = cb + d;
-            const uint2 v = digit8<kFp8Tcgen05>(X, d);
+            const uint2 v = digit8<kFp8Tcgen05>(X, d, p < S::RA ? S::WA : S::WB);
             *reinterpret_cast<uint2 *>(base + (n >> 3) * 128 + (n & 7) * 16) =
                 make_uint2(__byte_perm(v.y, 0, 0x0123), __byte_perm(v.x, 0, 0x0123));
           }

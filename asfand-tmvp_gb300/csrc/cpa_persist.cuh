@@ -124,8 +124,8 @@ __host__ __device__ inline Shape5 shape5(const CpaArgs &a) {
   s.RA = OP == kDecrypt ? 0 : s.L;
   s.wa = OP == kMatvec ? a.mv_eq : a.P.eq;
   s.wb = a.P.ep;
-  s.Da = (s.wa + 3) / 4;
-  s.Db = (s.wb + 3) / 4;
+  s.Da = r16_digits(s.wa);
+  s.Db = r16_digits(s.wb);
   s.ncols = s.RA * s.Da + (s.R - s.RA) * s.Db;
   s.NU = s.ncols <= 16 ? 16 : 32;
   return s;
@@ -316,7 +316,7 @@ __device__ __forceinline__ bool stage5(const CpaArgs &a, const Shape5 &S, const 
     uint8_t *base = B + j * 256 * NU + (kq >> 1) * 16 * NU + 8 * (kq & 1);
     for (int d = 0; d < D; d++) {
       const int n = cb + d;
-      const uint2 v = digit8<kFp8Tcgen05>(X, d);
+      const uint2 v = digit8<kFp8Tcgen05>(X, d, p < S.RA ? S.wa : S.wb);
       *reinterpret_cast<uint2 *>(base + (n >> 3) * 128 + (n & 7) * 16) =
           make_uint2(__byte_perm(v.y, 0, 0x0123), __byte_perm(v.x, 0, 0x0123));
     }

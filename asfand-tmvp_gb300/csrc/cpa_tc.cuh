@@ -14,7 +14,7 @@
 //   INT8 (mma.sync m16n8k32 s8 x u8 -> s32): two 8-bit limbs per coefficient.
 // The Toeplitz fragments are 4-byte windows of srev[k] = s_ext[510 - k],
 // read from four byte-shifted copies so that every window is an aligned word.
-// The tcgen05 form (cpa_umma.cuh) uses unsigned radix-16 digits 0..15, each
+// The tcgen05 form (cpa_umma.cuh) uses radix-16 digits (r16_digits), each
 // exact in e4m3, and no bias column.
 #pragma once
 #include <cstdint>
@@ -35,7 +35,7 @@ __device__ __forceinline__ void copy16(uint8_t *dst, const uint8_t *src, int nby
 // Digit columns of a w-bit public coefficient.
 template <int FORM>
 __host__ __device__ __forceinline__ int tc_digits(int w) {
-  return FORM == kFp8TC ? (w + 2) / 3 : (FORM == kFp8Tcgen05 ? (w + 3) / 4 : 2);
+  return FORM == kFp8TC ? (w + 2) / 3 : (FORM == kFp8Tcgen05 ? r16_digits(w) : 2);
 }
 
 // Number of B columns for R public polys whose first RA have width wa and the
@@ -70,11 +70,18 @@ __device__ __forceinline__ void unpack8(const uint8_t *base, int byte0, int w, u
 
 // Digit column words for eight coefficients held as 16-bit lanes.
 // FP8: bytes 0x50 | ((x >> 3d) & 7).  INT8: limb d = (x >> 8d) & 0xff.
-// tcgen05 FP8: e4m3 of (x >> 4d) & 15.
+// tcgen05 FP8: e4m3 of (x >> 4d) & 15, or of the signed 5-bit top digit of a
+// w-bit coefficient (r16_digits).
 template <int FORM>
-__device__ __forceinline__ uint2 digit8(const uint32_t (&X)[4], int d) {
+__device__ __forceinline__ uint2 digit8(const uint32_t (&X)[4], int d, int w = 16) {
   uint32_t t[4];
   if (FORM == kFp8Tcgen05) {
+    if (w - 4 * d == 5) {
+#pragma unroll
+      for (int i = 0; i < 4; i++) t[i] = (X[i] >> (4 * d)) & 0x001F001Fu;
+      return make_uint2(e4m3_sdigits4(__byte_perm(t[0], t[1], 0x6420)),
+                        e4m3_sdigits4(__byte_perm(t[2], t[3], 0x6420)));
+    }
 #pragma unroll
     for (int i = 0; i < 4; i++) t[i] = (X[i] >> (4 * d)) & 0x000F000Fu;
     return make_uint2(e4m3_digits4(__byte_perm(t[0], t[1], 0x6420)),

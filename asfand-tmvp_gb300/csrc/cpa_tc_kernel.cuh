@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(128, (Q >= 4 ? 3 : 4)) k_cpa_tc(CpaArgs a, TcL
       uint8_t *base = umma_b + j * 256 * NU + (kq >> 1) * 16 * NU + 8 * (kq & 1);
       for (int d = 0; d < D; d++) {
         const int n = cb + d;
-        uint2 v = digit8<FORM>(X, d);
+        uint2 v = digit8<FORM>(X, d, p < C::RA ? wa : wb);
         *reinterpret_cast<uint2 *>(base + (n >> 3) * 128 + (n & 7) * 16) =
             make_uint2(__byte_perm(v.y, 0, 0x0123), __byte_perm(v.x, 0, 0x0123));
       }

@@ -172,6 +172,22 @@ __device__ __forceinline__ uint32_t e4m3_digits4(uint32_t d) {
   return (big & m) | (lut & ~m);
 }
 
+// Radix-16 digits of a w-bit public coefficient x (results are needed mod
+// 2^w): unsigned nibbles, except that a 5-bit top digit t = x >> (w - 5) is
+// used as t - 32 when t >= 16.  That changes the product by a multiple of
+// 2^w only, and keeps every digit within e4m3's exact integers (|d| <= 16):
+// 13-bit coefficients need 3 digits instead of 4, 9-bit ones 2 instead of 3.
+__host__ __device__ constexpr int r16_digits(int w) { return w <= 5 ? 1 : 1 + (w - 5 + 3) / 4; }
+
+// e4m3 of four 5-bit top digits t (one per byte), each as the signed value
+// t (t < 16) or t - 32 (t >= 16); magnitude 16 encodes as 0x58.
+__device__ __forceinline__ uint32_t e4m3_sdigits4(uint32_t t) {
+  const uint32_t m = ((t >> 4) & 0x01010101u) * 0xFFu;           // bytes with t >= 16
+  const uint32_t mag = (m & (0x20202020u - t)) | (~m & t);       // 32 - t there (1..16), else t
+  const uint32_t is16 = (mag >> 4) & 0x01010101u;
+  return e4m3_digits4(mag & 0x0F0F0F0Fu) | (is16 * 0x58u) | (m & 0x80808080u);
+}
+
 // The encoded sequence s_ext[0..511] of each secret polynomial j < L, from
 // its encoded words S (64 per polynomial, byte e of word u = coefficient
 // 4u + e): s_ext[d] = -s[d + 1] for d < 255, s[d - 255] for 255 <= d <= 510,
