@@ -7,8 +7,9 @@
 //      one thread, counted on an mbarrier;
 //   2. secrets (CBD or unpacked), radix-16 e4m3 digit columns (r16_digits) with K
 //      reversed, s_ext and the Hankel core matrices (cpa_umma.cuh);
-//   3. one thread issues the 16 l tcgen05.mma (M = 128, N = 16 / 32, K = 32)
-//      into tensor memory and commits them to an mbarrier;
+//   3. one thread issues the 12 l tcgen05.mma (M = 128, N = 16 / 32, K = 32;
+//      both M halves share the MMAs of the middle K steps) into tensor memory
+//      and commits them to an mbarrier;
 //   4. accumulators -> int32 columns (tcgen05.ld) -> the rounding / packing /
 //      compare / decode epilogue, eight coefficients at a time.
 // Same results as the runtime-shaped kernels (cpa_tc_kernel.cuh,
@@ -78,10 +79,22 @@ struct LayoutC {
   // FOLD: both M halves in one MMA (columns 0..NCOLS-1 rows 0..127, columns
   // NCOLS..2 NCOLS-1 rows 128..255): 12 block operands of 32 K rows per j
   static constexpr bool FOLD = 2 * S::NCOLS <= 8;
+  // SPLIT (two stored column groups): K step k of one j sits in block k & 3,
+  // at group slots 2-3 for k < 4 and 0-1 for k >= 4, so step k - 4 lies two
+  // group strides after step k and one N = 32 MMA reads step k (top half)
+  // and step k - 4 (bottom half): 12 MMAs per j instead of 16
+  static constexpr bool SPLIT = !NARROW;
+  static_assert(!SPLIT || S::NU == 16, "SPLIT takes at most 16 digit columns");
   static constexpr int GROUPS = NARROW ? 1 : S::NU / 8;         // stored column groups
-  static constexpr int LBO_B = FOLD ? 128 : GROUPS * 128 + 16;
+  static constexpr int LB = 4 * 128 + 16;                        // SPLIT: K chunk stride (4 slots + pad)
+  static constexpr int RB = 2 * LB;                              // SPLIT: one block
+  static constexpr int LBO_B = FOLD ? 128 : (SPLIT ? LB : GROUPS * 128 + 16);
   static constexpr int BLK = 2 * 128 + 16;                       // FOLD: one block (2 K chunks + pad)
-  static constexpr int BJ = FOLD ? 12 * BLK : 16 * LBO_B;        // digit columns of one j
+  static constexpr int BJ = FOLD ? 12 * BLK : (SPLIT ? 4 * RB : 16 * LBO_B);  // digit columns of one j
+  // byte offset of K chunk a (16 K rows, K reversed) within one j (not FOLD)
+  __host__ __device__ static constexpr int chunk_off(int a) {
+    return SPLIT ? ((a >> 1) & 3) * RB + (a < 8 ? 256 : 0) + (a & 1) * LB : a * LBO_B;
+  }
   static constexpr int ENG = 0;
   static constexpr int H = ENG;
   static constexpr int A = H;                                    // streams inside H
@@ -254,7 +267,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
           *reinterpret_cast<uint2 *>(b2 + (S::NCOLS + cb + d) * 16) = w;
         }
       } else {
-        uint8_t *base = Bm + j * LO::BJ + (kq >> 1) * LO::LBO_B + 8 * (kq & 1);
+        uint8_t *base = Bm + j * LO::BJ + LO::chunk_off(kq >> 1) + 8 * (kq & 1);
 #pragma unroll
         for (int d = 0; d < (S::DA > S::DB ? S::DA : S::DB); d++) {
           if (d < D) {
@@ -281,7 +294,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
     constexpr int PADC = LO::FOLD ? 0 : LO::GROUPS * 8 - S::NCOLS;  // zero columns of the stored groups
     for (int idx = tid; idx < L * PADC * 16; idx += NT) {
       const int j = idx / (PADC * 16), r = idx % (PADC * 16), n = S::NCOLS + r % PADC, ac = r / PADC;
-      *reinterpret_cast<uint4 *>(Bm + j * LO::BJ + ac * LO::LBO_B + (n >> 3) * 128 + (n & 7) * 16) =
+      *reinterpret_cast<uint4 *>(Bm + j * LO::BJ + LO::chunk_off(ac) + (n >> 3) * 128 + (n & 7) * 16) =
           make_uint4(0u, 0u, 0u, 0u);
     }
     if (LO::NARROW)
@@ -313,12 +326,35 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
           umma_f8(tmem, ad, bd, idesc, (j | m) != 0);
         }
       }
+    } else if constexpr (LO::SPLIT) {
+      // window w of the Hankel sequence (core 4w) multiplies step w into the
+      // top half and step w - 4 into the bottom half (columns 16..31):
+      // windows 8..11 bottom only, 0..3 top only (these start each half's
+      // accumulation), then 4..7 both at N = 32
+      constexpr uint32_t id16 = umma_idesc_e4m3(16), id32 = umma_idesc_e4m3(32);
+#pragma unroll
+      for (int j = 0; j < L; j++) {
+        const uint32_t bj = b0 + j * LO::BJ;
+        const uint64_t hj = ad0 + (uint64_t)((j * kHankelBytes) >> 4);
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+          umma_f8(tmem + 16, hj + (uint64_t)((4 * (r + 8) * 128) >> 4), umma_desc(bj + r * LO::RB, LO::LB, 128),
+                  id16, (j | r) != 0);
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+          umma_f8(tmem, hj + (uint64_t)((4 * r * 128) >> 4), umma_desc(bj + r * LO::RB + 256, LO::LB, 128), id16,
+                  (j | r) != 0);
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+          umma_f8(tmem, hj + (uint64_t)((4 * (r + 4) * 128) >> 4), umma_desc(bj + r * LO::RB, LO::LB, 128), id32,
+                  true);
+      }
     } else {
 #pragma unroll
     for (int j = 0; j < L; j++) {
 #pragma unroll
       for (int ks = 0; ks < 8; ks++) {
-        const uint32_t bs = b0 + j * LO::BJ + 2 * ks * LO::LBO_B;
+        const uint32_t bs = b0 + j * LO::BJ + LO::chunk_off(2 * ks);
         // group 1 of a narrow B is the zero block, one stride byte offset away
         const uint64_t bd = umma_desc(bs, LO::LBO_B, LO::NARROW ? z0 - bs : 128);
 #pragma unroll
