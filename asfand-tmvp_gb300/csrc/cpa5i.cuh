@@ -376,18 +376,14 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
   tc_fence_after();
   // warp w reads TMEM lanes 32 (w % 4) .. +31; warps 4..7 take the second M half
   const int q4 = warp & 3, hsel = warp >> 2;
-  if (done && LO::FOLD) {
-    // columns c < NCOLS: row 32 q4 + lane; columns NCOLS + c: that row + 128
-    if (hsel == 0) {
-      uint32_t r[16];
-      tmem_ld16(tmem + ((uint32_t)(32 * q4) << 16), r);
-      const int row = 32 * q4 + lane;
-#pragma unroll
-      for (int c = 0; c < S::NCOLS; c++) {
-        acc[c * 256 + row] = __float2int_rn(__uint_as_float(r[c]));
-        acc[c * 256 + 128 + row] = __float2int_rn(__uint_as_float(r[S::NCOLS + c]));
-      }
-    }
+  // decryption and re-encryption: coefficient k = 128 hsel + 32 q4 + lane of
+  // every output polynomial stays in this thread's registers (FOLD: columns
+  // NCOLS.. of row k - 128 hold the second half)
+  constexpr bool FUSED = OP == kDecrypt || OP == kReenc;
+  static_assert(!FUSED || NU == 16, "fused epilogue reads one 16-column slice");
+  uint32_t racc[16];
+  if (done && FUSED) {
+    tmem_ld16(tmem + ((uint32_t)(32 * q4) << 16) + (LO::FOLD ? 0 : hsel * NU), racc);
   } else if (done) {
 #pragma unroll
     for (int hh = 0; hh < 2; hh++) {
@@ -455,27 +451,63 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
     return lo16 | (hi16 << 16);
   };
 
-  if (OP == kDecrypt) {
-    // m'_k = ((v + h2 - (c_m << (ep-et))) mod p) >> (ep-1), one byte per group
-    if (tid < 32) {
-      uint32_t V[4], CM[4];
-      combine8(0, tid, V);
-      unpack8c<C::ET>(sm + LO::CTO + L * C::POLYCOMP, tid * C::ET, CM);
-      uint32_t byte = 0;
+  // sum_d 16^d acc_d of the digit columns c0.. (FUSED path): each f32
+  // accumulator holds an exact integer |x| < 2^22, so x + 1.5 * 2^23 carries
+  // x + 0x4B400000 in its bit pattern; the offsets are removed at the end
+  auto combine1 = [&](int c0, int D) -> uint32_t {
+    uint32_t v = 0, off = 0;
 #pragma unroll
-      for (int k = 0; k < 8; k++) {
-        const uint32_t v = (k & 1) ? (V[k >> 1] >> 16) : (V[k >> 1] & 0xffffu);
-        const uint32_t cm = (k & 1) ? (CM[k >> 1] >> 16) : (CM[k >> 1] & 0xffffu);
-        const uint32_t t = (v + C::H2 - (cm << (C::EP - C::ET))) & pmask;
-        byte |= ((t >> (C::EP - 1)) & 1u) << k;
+    for (int d = 0; d < 4; d++) {
+      if (d < D) {
+        v += (1u << (4 * d)) * __float_as_uint(__uint_as_float(racc[c0 + d]) + 12582912.0f);
+        off += (1u << (4 * d)) * 0x4B400000u;
       }
-      uint8_t *mo = a.m_out + (size_t)inst * a.m_out_stride;
-      mo[tid] = (uint8_t)byte;
-      if (a.copy_hpk) mo[32 + tid] = a.sk[(size_t)inst * C::SK + C::SK - 64 + tid];
     }
-  } else if (OP == kEncrypt || OP == kReenc) {
+    return v - off;
+  };
+  // W-bit field at bit `bit` of a 4-byte-aligned shared-memory stream
+  auto field = [&](int byte_off, int bit, int W) -> uint32_t {
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(sm + byte_off) + (bit >> 5);
+    return __funnelshift_r(w[0], w[1], bit & 31) & ((1u << W) - 1u);
+  };
+
+  if constexpr (OP == kDecrypt) {
+    // m'_k = ((v_k + h2 - (c_m,k << (ep-et))) mod p) >> (ep-1): one bit per
+    // thread, gathered into bytes by a ballot per warp
+    const int k = 128 * hsel + 32 * q4 + lane;
+    if (LO::FOLD && hsel) {
+      // the second half's columns, moved down by register selects (no
+      // runtime-indexed array)
+#pragma unroll
+      for (int d = 0; d < S::NCOLS; d++) racc[d] = racc[S::NCOLS + d];
+    }
+    const uint32_t v = combine1(0, S::DB);
+    const uint32_t cm = field(LO::CTO + L * C::POLYCOMP, k * C::ET, C::ET);
+    const uint32_t t = (v + C::H2 - (cm << (C::EP - C::ET))) & pmask;
+    const uint32_t bits = __ballot_sync(0xffffffffu, ((t >> (C::EP - 1)) & 1u) != 0u);
+    uint8_t *mo = a.m_out + (size_t)inst * a.m_out_stride;
+    if (lane < 4) mo[4 * (4 * hsel + q4) + lane] = (uint8_t)(bits >> (8 * lane));
+    if (a.copy_hpk && warp == 0) mo[32 + lane] = a.sk[(size_t)inst * C::SK + C::SK - 64 + lane];
+  } else if constexpr (OP == kReenc) {
+    // round coefficient k of b' and encode that of v', compare with the ciphertext
+    const int k = 128 * hsel + 32 * q4 + lane;
+    const uint32_t mk = (sm[LO::MSG + (k >> 3)] >> (k & 7)) & 1u;
+    uint32_t diff = 0;
+#pragma unroll
+    for (int p = 0; p < S::R; p++) {
+      const uint32_t v = combine1(S::col_base(p), S::digits(p));
+      if (p < L) {
+        const uint32_t w = ((v + C::H1) & qmask) >> (C::EQ - C::EP);
+        diff |= w ^ field(LO::CTO + p * C::POLYCOMP, k * C::EP, C::EP);
+      } else {
+        const uint32_t w = ((v + C::H1 - (mk << (C::EP - 1))) & pmask) >> (C::EP - C::ET);
+        diff |= w ^ field(LO::CTO + L * C::POLYCOMP, k * C::ET, C::ET);
+      }
+    }
+    const int any = __syncthreads_or(diff != 0u);
+    if (tid == 0) a.fail[inst] = (uint8_t)(any != 0);
+  } else if (OP == kEncrypt) {
     const uint8_t *msg = sm + LO::MSG;
-    int diff = 0;
     for (int idx = tid; idx < S::R * 32; idx += NT) {
       const int p = idx >> 5, grp = idx & 31;
       uint32_t V[4], W[4];
@@ -483,35 +515,16 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
       if (p < L) {
 #pragma unroll
         for (int i = 0; i < 4; i++) W[i] = round_lanes(V[i]);
-        const int byte0 = (32 * p + grp) * C::EP;
-        if (OP == kReenc) {
-          uint32_t Cv[4];
-          unpack8c<C::EP>(sm + LO::CTO, byte0, Cv);
-          diff |= (Cv[0] ^ W[0]) | (Cv[1] ^ W[1]) | (Cv[2] ^ W[2]) | (Cv[3] ^ W[3]);
-        } else {
-          pack8(sm + LO::OUT + byte0, W, C::EP);
-        }
+        pack8(sm + LO::OUT + (32 * p + grp) * C::EP, W, C::EP);
       } else {
         const uint32_t mb = msg[grp];
 #pragma unroll
         for (int i = 0; i < 4; i++) W[i] = encode_lanes(V[i], (mb >> (2 * i)) & 1u, (mb >> (2 * i + 1)) & 1u);
-        const int byte0 = L * C::POLYCOMP + grp * C::ET;
-        if (OP == kReenc) {
-          uint32_t Cv[4];
-          unpack8c<C::ET>(sm + LO::CTO, byte0, Cv);
-          diff |= (Cv[0] ^ W[0]) | (Cv[1] ^ W[1]) | (Cv[2] ^ W[2]) | (Cv[3] ^ W[3]);
-        } else {
-          pack8(sm + LO::OUT + byte0, W, C::ET);
-        }
+        pack8(sm + LO::OUT + L * C::POLYCOMP + grp * C::ET, W, C::ET);
       }
     }
-    if (OP == kReenc) {
-      const int any = __syncthreads_or(diff != 0);
-      if (tid == 0) a.fail[inst] = (uint8_t)(any != 0);
-    } else {
-      __syncthreads();
-      copy16(a.ct_out + (size_t)inst * C::CT, sm + LO::OUT, C::CT);
-    }
+    __syncthreads();
+    copy16(a.ct_out + (size_t)inst * C::CT, sm + LO::OUT, C::CT);
   } else if (OP == kKeygen) {
     constexpr int bbytes = L * C::POLYCOMP;
     uint8_t *outb = sm + LO::OUT;
