@@ -5,8 +5,9 @@
 // Per instance:
 //   1. the packed inputs arrive by TMA bulk copies (cp.async.bulk) issued by
 //      one thread, counted on an mbarrier;
-//   2. secrets (CBD or unpacked), radix-16 e4m3 digit columns (r16_digits) with K
-//      reversed, s_ext and the Hankel core matrices (cpa_umma.cuh);
+//   2. secrets (CBD or unpacked), radix-16 digit columns (r16_digits, raw
+//      e4m3 bytes worth digit * 2^-9) with K reversed, s_ext and the Hankel
+//      core matrices (cpa_umma.cuh);
 //   3. one thread issues the 12 l tcgen05.mma (M = 128, N = 16 / 32, K = 32;
 //      both M halves share the MMAs of the middle K steps) into tensor memory
 //      and commits them to an mbarrier;
@@ -16,6 +17,7 @@
 // cpa_persist.cuh); the arithmetic per instance is the same.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 
 #include "cpa_persist.cuh"
 
@@ -143,6 +145,44 @@ __device__ __forceinline__ void unpack8c(const uint8_t *base, int byte0, uint32_
   }
 }
 
+// Four signed 5-bit top digits t (one per byte) as raw e4m3 bytes: t for
+// t < 16, else 0x80 | (32 - t), the number t - 32 (magnitudes up to 16).
+__device__ __forceinline__ uint32_t raw_sdigits4(uint32_t t) {
+  const uint32_t m = ((t >> 4) & 0x01010101u) * 0xFFu;  // bytes with t >= 16
+  return (m & ((0x20202020u - t) | 0x80808080u)) | (~m & t);
+}
+
+// Radix-16 digit d (r16_digits) of eight W-bit coefficients X (four words of
+// two 16-bit lanes, coefficient 2i in the low lane of X[i]) as raw bytes in
+// K-reversed order: .x = coefficients 7, 6, 5, 4 and .y = 3, 2, 1, 0.  The
+// e4m3 byte b in 0..16 is the number b * 2^-9 (0..7 subnormal, 8..15 the
+// lowest normal binade, 16 = 2^-5), so every digit is its own encoding and
+// the accumulators carry the factor 2^-9.
+template <int W>
+__device__ __forceinline__ uint2 raw_digits8(const uint32_t (&X)[4], int d) {
+  const int lo = 4 * d;
+  const int wd = W - lo < 4 ? W - lo : (W - lo == 5 ? 5 : 4);
+  const uint32_t mask = ((1u << wd) - 1u) * 0x01010101u;
+  uint32_t a, b;
+  if (lo + wd <= 8) {  // inside the low byte of each lane
+    a = __byte_perm(X[2], X[3], 0x0246) >> lo;
+    b = __byte_perm(X[0], X[1], 0x0246) >> lo;
+  } else if (lo >= 8) {  // inside the high byte
+    a = __byte_perm(X[2], X[3], 0x1357) >> (lo - 8);
+    b = __byte_perm(X[0], X[1], 0x1357) >> (lo - 8);
+  } else {  // across both
+    a = __byte_perm(X[2] >> lo, X[3] >> lo, 0x0246);
+    b = __byte_perm(X[0] >> lo, X[1] >> lo, 0x0246);
+  }
+  a &= mask;
+  b &= mask;
+  if (wd == 5) {
+    a = raw_sdigits4(a);
+    b = raw_sdigits4(b);
+  }
+  return make_uint2(a, b);
+}
+
 // One instance (CTA of kI5Threads threads; sm: its dynamic shared memory).
 template <int OP, int SET>
 __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst, uint8_t *sm) {
@@ -239,44 +279,38 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
       }
     }
     // 2. digit columns (K reversed, core-matrix order), then the zero columns
+    auto put_digits = [&](const uint32_t (&X)[4], auto wc, int cb, int j, int kq) {
+      constexpr int W = decltype(wc)::value;
+#pragma unroll
+      for (int d = 0; d < r16_digits(W); d++) {
+        const uint2 v = raw_digits8<W>(X, d);
+        if constexpr (LO::FOLD) {
+          // K step kq / 4 feeds block kq / 4 (top half, columns 0..) and
+          // block kq / 4 + 4 (bottom half, columns NCOLS..)
+          uint8_t *b1 = Bm + j * LO::BJ + (kq >> 2) * LO::BLK + ((kq >> 1) & 1) * 128 + 8 * (kq & 1);
+          *reinterpret_cast<uint2 *>(b1 + (cb + d) * 16) = v;
+          *reinterpret_cast<uint2 *>(b1 + 4 * LO::BLK + (S::NCOLS + cb + d) * 16) = v;
+        } else {
+          const int n = cb + d;
+          *reinterpret_cast<uint2 *>(Bm + j * LO::BJ + LO::chunk_off(kq >> 1) + 8 * (kq & 1) + (n >> 3) * 128 +
+                                     (n & 7) * 16) = v;
+        }
+      }
+    };
     for (int idx = tid; idx < S::R * L * 32; idx += NT) {
       const int grp = idx & 31, j = (idx >> 5) % L, p = idx / (32 * L);
+      const int kq = 31 - grp;  // coefficients 8grp..8grp+7 are rows k' = 8kq+7..8kq
       uint32_t X[4];
       if (OP == kDecrypt) {
         unpack8c<S::WB>(sm + LO::CTO, (32 * j + grp) * S::WB, X);
+        put_digits(X, std::integral_constant<int, S::WB>{}, 0, j, kq);
       } else if (p < S::RA) {
         const int ij = (OP == kKeygen) ? (j * L + p) : (p * L + j);
         unpack8c<S::WA>(sm + LO::A, (32 * ij + grp) * S::WA, X);
+        put_digits(X, std::integral_constant<int, S::WA>{}, p * S::DA, j, kq);
       } else {
         unpack8c<S::WB>(sm + LO::B, (32 * j + grp) * S::WB, X);
-      }
-      const int kq = 31 - grp;  // coefficients 8grp..8grp+7 are rows k' = 8kq+7..8kq
-      const int cb = p < S::RA ? p * S::DA : S::RA * S::DA + (p - S::RA) * S::DB;
-      const int D = p < S::RA ? S::DA : S::DB;
-      if constexpr (LO::FOLD) {
-        // K step c = kq / 4 feeds block c (top half, columns 0..) and block
-        // c + 4 (bottom half, columns NCOLS..)
-        const int c = kq >> 2;
-        uint8_t *b1 = Bm + j * LO::BJ + c * LO::BLK + ((kq >> 1) & 1) * 128 + 8 * (kq & 1);
-        uint8_t *b2 = b1 + 4 * LO::BLK;
-#pragma unroll
-        for (int d = 0; d < S::DB; d++) {
-          const uint2 v = digit8<kFp8Tcgen05>(X, d, S::WB);
-          const uint2 w = make_uint2(__byte_perm(v.y, 0, 0x0123), __byte_perm(v.x, 0, 0x0123));
-          *reinterpret_cast<uint2 *>(b1 + (cb + d) * 16) = w;
-          *reinterpret_cast<uint2 *>(b2 + (S::NCOLS + cb + d) * 16) = w;
-        }
-      } else {
-        uint8_t *base = Bm + j * LO::BJ + LO::chunk_off(kq >> 1) + 8 * (kq & 1);
-#pragma unroll
-        for (int d = 0; d < (S::DA > S::DB ? S::DA : S::DB); d++) {
-          if (d < D) {
-            const int n = cb + d;
-            const uint2 v = digit8<kFp8Tcgen05>(X, d, p < S::RA ? S::WA : S::WB);
-            *reinterpret_cast<uint2 *>(base + (n >> 3) * 128 + (n & 7) * 16) =
-                make_uint2(__byte_perm(v.y, 0, 0x0123), __byte_perm(v.x, 0, 0x0123));
-          }
-        }
+        put_digits(X, std::integral_constant<int, S::WB>{}, S::RA * S::DA + (p - S::RA) * S::DB, j, kq);
       }
     }
     if constexpr (LO::FOLD) {
@@ -395,7 +429,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
         const int row = 128 * hh + 32 * q4 + lane;
 #pragma unroll
         for (int c = 0; c < 16; c++)
-          if (cc + c < S::NCOLS) acc[(cc + c) * 256 + row] = __float2int_rn(__uint_as_float(r[c]));
+          if (cc + c < S::NCOLS) acc[(cc + c) * 256 + row] = __float2int_rn(__uint_as_float(r[c]) * 512.0f);
       }
     }
   } else {
@@ -452,15 +486,16 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
   };
 
   // sum_d 16^d acc_d of the digit columns c0.. (FUSED path): each f32
-  // accumulator holds an exact integer |x| < 2^22, so x + 1.5 * 2^23 carries
-  // x + 0x4B400000 in its bit pattern; the offsets are removed at the end
+  // accumulator holds x * 2^-9 for an exact integer |x| < 2^22, so adding
+  // 1.5 * 2^14 leaves x + 0x46C00000 in its bit pattern; the offsets are
+  // removed at the end
   auto combine1 = [&](int c0, int D) -> uint32_t {
     uint32_t v = 0, off = 0;
 #pragma unroll
     for (int d = 0; d < 4; d++) {
       if (d < D) {
-        v += (1u << (4 * d)) * __float_as_uint(__uint_as_float(racc[c0 + d]) + 12582912.0f);
-        off += (1u << (4 * d)) * 0x4B400000u;
+        v += (1u << (4 * d)) * __float_as_uint(__uint_as_float(racc[c0 + d]) + 24576.0f);
+        off += (1u << (4 * d)) * 0x46C00000u;
       }
     }
     return v - off;
