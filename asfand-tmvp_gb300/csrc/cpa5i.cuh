@@ -8,9 +8,9 @@
 //   2. secrets (CBD or unpacked), radix-16 digit columns (r16_digits, raw
 //      e4m3 bytes worth digit * 2^-9) with K reversed, s_ext and the Hankel
 //      core matrices (cpa_umma.cuh);
-//   3. one thread issues the 12 l tcgen05.mma (M = 128, N = 16 / 32, K = 32;
-//      both M halves share the MMAs of the middle K steps) into tensor memory
-//      and commits them to an mbarrier;
+//   3. one thread issues the 8 l tcgen05.mma (M = 128, N = 16 / 32, K = 32;
+//      each window of the Hankel sequence serves both M halves through the
+//      negacyclic wrap) into tensor memory and commits them to an mbarrier;
 //   4. accumulators -> int32 columns (tcgen05.ld) -> the rounding / packing /
 //      compare / decode epilogue, eight coefficients at a time.
 // Same results as the runtime-shaped kernels (cpa_tc_kernel.cuh,
@@ -48,8 +48,10 @@ struct ShapeC {
   static constexpr int WA = C::EQ, WB = C::EP;
   static constexpr int DA = r16_digits(WA), DB = r16_digits(WB);
   static constexpr int NCOLS = RA * DA + (R - RA) * DB;
-  static constexpr int NU = NCOLS <= 16 ? 16 : 32;
-  static constexpr int TMEM_COLS = NU <= 16 ? 32 : 64;
+  static_assert(NCOLS <= 16, "at most two 8-column groups per K step");
+  static constexpr int G = NCOLS <= 8 ? 1 : 2;     // 8-column groups per K step
+  static constexpr int NU = 16 * G;                // N of every MMA (two K steps side by side)
+  static constexpr int TMEM_COLS = 32 * G;         // two accumulator regions of NU columns
   static constexpr int col_base(int p) { return p < RA ? p * DA : RA * DA + (p - RA) * DB; }
   static constexpr int digits(int p) { return p < RA ? DA : DB; }
 };
@@ -60,15 +62,22 @@ constexpr int al16c(int x) { return (x + 15) & ~15; }
 // an instance; tensor memory is read by warps w and w + 4 (two M halves).
 constexpr int kI5Threads = 256;
 
+// Hankel core matrices per secret polynomial: windows 0..7 (core 4w) over
+// row groups 0..15 and two K chunks reach core 4 * 7 + 15 + 2 = 45.
+constexpr int kHankelCores5 = 46;
+constexpr int kHankelBytes5 = kHankelCores5 * 128;
+
 // Shared-memory layout of one CTA (byte offsets).  The operand region ENG
-// holds the Hankel core matrices H (l x kHankelBytes), the digit columns B and
-// s_ext; the packed GenMatrix / GenSecret / b streams and the packed secret
-// key are only read before H is written, so they land inside H.  Digit
-// columns: K chunk a of column group c at a * LBO_B + c * 128, with
-// LBO_B = 16 N + 16 (the 16-byte pad spreads the chunks of one column over
-// the banks).  When at most 8 columns are used (decryption), only group 0 is
-// stored and the MMA's group 1 reads a shared zero block through the stride
-// byte offset.
+// holds the Hankel core matrices H (l x kHankelBytes5), the digit columns B
+// and s_ext; the packed GenMatrix / GenSecret / b streams and the packed
+// secret key are only read before H is written, so they land inside H.
+//
+// Digit columns of one j: K step t (32 K rows, K reversed) has G groups of 8
+// columns and sits in block t & 3, at group slots 0..G-1 for t >= 4 and
+// G..2G-1 for t < 4, so one N = 16 G descriptor on block r reads step r + 4
+// (columns 0..8G-1) beside step r (columns 8G..16G-1).  Within a block the
+// second K chunk of every slot lies LB = 2G * 128 + 16 bytes after the
+// first (the pad spreads one column's chunks over the banks).
 template <int OP, int SET>
 struct LayoutC {
   using C = SetC<SET>;
@@ -77,25 +86,13 @@ struct LayoutC {
   static constexpr bool HAS_B = OP == kEncrypt || OP == kReenc;
   static constexpr bool HAS_CT = OP == kReenc || OP == kDecrypt;
   static constexpr bool HAS_SK = OP == kDecrypt;
-  static constexpr bool NARROW = S::NCOLS <= 8;
-  // FOLD: both M halves in one MMA (columns 0..NCOLS-1 rows 0..127, columns
-  // NCOLS..2 NCOLS-1 rows 128..255): 12 block operands of 32 K rows per j
-  static constexpr bool FOLD = 2 * S::NCOLS <= 8;
-  // SPLIT (two stored column groups): K step k of one j sits in block k & 3,
-  // at group slots 2-3 for k < 4 and 0-1 for k >= 4, so step k - 4 lies two
-  // group strides after step k and one N = 32 MMA reads step k (top half)
-  // and step k - 4 (bottom half): 12 MMAs per j instead of 16
-  static constexpr bool SPLIT = !NARROW;
-  static_assert(!SPLIT || S::NU == 16, "SPLIT takes at most 16 digit columns");
-  static constexpr int GROUPS = NARROW ? 1 : S::NU / 8;         // stored column groups
-  static constexpr int LB = 4 * 128 + 16;                        // SPLIT: K chunk stride (4 slots + pad)
-  static constexpr int RB = 2 * LB;                              // SPLIT: one block
-  static constexpr int LBO_B = FOLD ? 128 : (SPLIT ? LB : GROUPS * 128 + 16);
-  static constexpr int BLK = 2 * 128 + 16;                       // FOLD: one block (2 K chunks + pad)
-  static constexpr int BJ = FOLD ? 12 * BLK : (SPLIT ? 4 * RB : 16 * LBO_B);  // digit columns of one j
-  // byte offset of K chunk a (16 K rows, K reversed) within one j (not FOLD)
+  static constexpr int G = S::G;
+  static constexpr int LB = 2 * G * 128 + 16;  // second K chunk of a block
+  static constexpr int RB = 2 * LB;            // one block
+  static constexpr int BJ = 4 * RB;            // digit columns of one j
+  // byte offset of K chunk a (16 K rows, K reversed) within one j
   __host__ __device__ static constexpr int chunk_off(int a) {
-    return SPLIT ? ((a >> 1) & 3) * RB + (a < 8 ? 256 : 0) + (a & 1) * LB : a * LBO_B;
+    return ((a >> 1) & 3) * RB + (a < 8 ? G * 128 : 0) + (a & 1) * LB;
   }
   static constexpr int ENG = 0;
   static constexpr int H = ENG;
@@ -103,9 +100,8 @@ struct LayoutC {
   static constexpr int SS = HAS_AS ? al16c(A + C::GM + 16) : A;
   static constexpr int B = HAS_AS ? al16c(SS + C::GS + 16) : SS;
   static constexpr int SKO = H;
-  static constexpr int BM = H + C::L * kHankelBytes;
-  static constexpr int ZERO = BM + C::L * BJ;                    // zero block (NARROW)
-  static constexpr int EXT = ZERO + (NARROW ? LBO_B + 128 : 0);
+  static constexpr int BM = H + C::L * kHankelBytes5;
+  static constexpr int EXT = BM + C::L * BJ;
   static constexpr int ENG_END_OPS = EXT + C::L * 512;
   static constexpr int ENG_BYTES = ENG_END_OPS > S::NCOLS * 1024 ? ENG_END_OPS : S::NCOLS * 1024;
   static constexpr int CTO = al16c(ENG + ENG_BYTES);
@@ -120,7 +116,7 @@ struct LayoutC {
   static constexpr int IN_BYTES = (HAS_AS ? C::GM + C::GS : 0) + (HAS_B ? C::L * C::POLYCOMP + 32 : 0) +
                                   (HAS_CT ? C::CT : 0) + (HAS_SK ? C::INDCPA_SK : 0);
   static_assert(!HAS_AS || B + (HAS_B ? C::L * C::POLYCOMP + 16 : 0) <= BM, "streams fit inside H");
-  static_assert(!HAS_SK || C::INDCPA_SK + 16 <= C::L * kHankelBytes, "secret key fits inside H");
+  static_assert(!HAS_SK || C::INDCPA_SK + 16 <= C::L * kHankelBytes5, "secret key fits inside H");
 };
 
 // Eight W-bit little-endian fields from byte `byte0` (16 bytes of slack after
@@ -284,17 +280,9 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
 #pragma unroll
       for (int d = 0; d < r16_digits(W); d++) {
         const uint2 v = raw_digits8<W>(X, d);
-        if constexpr (LO::FOLD) {
-          // K step kq / 4 feeds block kq / 4 (top half, columns 0..) and
-          // block kq / 4 + 4 (bottom half, columns NCOLS..)
-          uint8_t *b1 = Bm + j * LO::BJ + (kq >> 2) * LO::BLK + ((kq >> 1) & 1) * 128 + 8 * (kq & 1);
-          *reinterpret_cast<uint2 *>(b1 + (cb + d) * 16) = v;
-          *reinterpret_cast<uint2 *>(b1 + 4 * LO::BLK + (S::NCOLS + cb + d) * 16) = v;
-        } else {
-          const int n = cb + d;
-          *reinterpret_cast<uint2 *>(Bm + j * LO::BJ + LO::chunk_off(kq >> 1) + 8 * (kq & 1) + (n >> 3) * 128 +
-                                     (n & 7) * 16) = v;
-        }
+        const int n = cb + d;
+        *reinterpret_cast<uint2 *>(Bm + j * LO::BJ + LO::chunk_off(kq >> 1) + 8 * (kq & 1) + (n >> 3) * 128 +
+                                   (n & 7) * 16) = v;
       }
     };
     for (int idx = tid; idx < S::R * L * 32; idx += NT) {
@@ -313,124 +301,75 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
         put_digits(X, std::integral_constant<int, S::WB>{}, S::RA * S::DA + (p - S::RA) * S::DB, j, kq);
       }
     }
-    if constexpr (LO::FOLD) {
-      // zero slots of the blocks: the absent half (top for blocks 8..11,
-      // bottom for blocks 0..3) and the columns past 2 NCOLS
-      for (int idx = tid; idx < L * 12 * 2 * 8; idx += NT) {
-        const int col = idx & 7, a = (idx >> 3) & 1, m = (idx >> 4) % 12, j = idx / (16 * 12);
-        const bool top = col < S::NCOLS, bottom = col >= S::NCOLS && col < 2 * S::NCOLS;
-        const bool data = (top && m < 8) || (bottom && m >= 4);
-        if (!data)
-          *reinterpret_cast<uint4 *>(Bm + j * LO::BJ + m * LO::BLK + a * 128 + col * 16) =
-              make_uint4(0u, 0u, 0u, 0u);
-      }
-    }
-    constexpr int PADC = LO::FOLD ? 0 : LO::GROUPS * 8 - S::NCOLS;  // zero columns of the stored groups
+    constexpr int PADC = 8 * LO::G - S::NCOLS;  // zero columns of the stored groups
     for (int idx = tid; idx < L * PADC * 16; idx += NT) {
       const int j = idx / (PADC * 16), r = idx % (PADC * 16), n = S::NCOLS + r % PADC, ac = r / PADC;
       *reinterpret_cast<uint4 *>(Bm + j * LO::BJ + LO::chunk_off(ac) + (n >> 3) * 128 + (n & 7) * 16) =
           make_uint4(0u, 0u, 0u, 0u);
     }
-    if (LO::NARROW)
-      for (int i = tid; i < (LO::LBO_B + 128) / 16; i += NT)
-        reinterpret_cast<uint4 *>(sm + LO::ZERO)[i] = make_uint4(0u, 0u, 0u, 0u);
   }
   __syncthreads();  // secret words complete before s_ext reads them
   if (ready) stage_ext(ext, sencw, L, tid, NT, [](uint32_t v) { return v ^ 0x80808080u; });
   __syncthreads();
-  if (ready) stage_hankel(H, ext, L, tid, NT);
+  if (ready) stage_hankel(H, ext, L, tid, NT, kHankelCores5);
   fence_async_smem();  // generic-proxy writes -> visible to the tensor core
   ok = __syncthreads_and(ok) != 0;
   if (!ok && tid == 0 && a.err) atomicOr(a.err, 1);
 
-  // 3. the MMAs (one thread); descriptors differ only in the start address
+  // 3. the MMAs (one thread).  Window w of the Hankel sequence (core 4w)
+  // holds rows r of s_ext[r + 32w + e]; rows 128 + r of K step t equal
+  // window t + 4 for t < 4, and -(window t - 4) for t >= 4 (s_ext[d + 256] =
+  // -s_ext[d] for d < 255).  The descriptor on block r reads steps r + 4 and
+  // r, so window r + 4 gives (top, step r + 4 | bottom, step r) in region 0
+  // and window r gives (-bottom, step r + 4 | top, step r) in region 1:
+  // 8 MMAs per j, top = region0[0] + region1[1], bottom = region0[1] - region1[0].
   if (ready && tid == 0) {
     constexpr uint32_t idesc = umma_idesc_e4m3(NU);
     const uint64_t ad0 = umma_desc(smem_u32(H), 256, 128);
-    const uint32_t b0 = smem_u32(Bm), z0 = smem_u32(sm + LO::ZERO);
-    if constexpr (LO::FOLD) {
-      // window m of the Hankel sequence (core 4m) times block m: 12 MMAs per j
-#pragma unroll
-      for (int j = 0; j < L; j++) {
-#pragma unroll
-        for (int m = 0; m < 12; m++) {
-          const uint32_t bs = b0 + j * LO::BJ + m * LO::BLK;
-          const uint64_t bd = umma_desc(bs, 128, z0 - bs);
-          const uint64_t ad = ad0 + (uint64_t)((j * kHankelBytes + 4 * m * 128) >> 4);
-          umma_f8(tmem, ad, bd, idesc, (j | m) != 0);
-        }
-      }
-    } else if constexpr (LO::SPLIT) {
-      // window w of the Hankel sequence (core 4w) multiplies step w into the
-      // top half and step w - 4 into the bottom half (columns 16..31):
-      // windows 8..11 bottom only, 0..3 top only (these start each half's
-      // accumulation), then 4..7 both at N = 32
-      constexpr uint32_t id16 = umma_idesc_e4m3(16), id32 = umma_idesc_e4m3(32);
-#pragma unroll
-      for (int j = 0; j < L; j++) {
-        const uint32_t bj = b0 + j * LO::BJ;
-        const uint64_t hj = ad0 + (uint64_t)((j * kHankelBytes) >> 4);
-#pragma unroll
-        for (int r = 0; r < 4; r++)
-          umma_f8(tmem + 16, hj + (uint64_t)((4 * (r + 8) * 128) >> 4), umma_desc(bj + r * LO::RB, LO::LB, 128),
-                  id16, (j | r) != 0);
-#pragma unroll
-        for (int r = 0; r < 4; r++)
-          umma_f8(tmem, hj + (uint64_t)((4 * r * 128) >> 4), umma_desc(bj + r * LO::RB + 256, LO::LB, 128), id16,
-                  (j | r) != 0);
-#pragma unroll
-        for (int r = 0; r < 4; r++)
-          umma_f8(tmem, hj + (uint64_t)((4 * (r + 4) * 128) >> 4), umma_desc(bj + r * LO::RB, LO::LB, 128), id32,
-                  true);
-      }
-    } else {
+    const uint32_t b0 = smem_u32(Bm);
 #pragma unroll
     for (int j = 0; j < L; j++) {
+      const uint64_t hj = ad0 + (uint64_t)((j * kHankelBytes5) >> 4);
 #pragma unroll
-      for (int ks = 0; ks < 8; ks++) {
-        const uint32_t bs = b0 + j * LO::BJ + LO::chunk_off(2 * ks);
-        // group 1 of a narrow B is the zero block, one stride byte offset away
-        const uint64_t bd = umma_desc(bs, LO::LBO_B, LO::NARROW ? z0 - bs : 128);
-#pragma unroll
-        for (int hh = 0; hh < 2; hh++) {
-          const uint64_t ad = ad0 + (uint64_t)((j * kHankelBytes + (16 * hh + 4 * ks) * 128) >> 4);
-          umma_f8(tmem + hh * NU, ad, bd, idesc, (j | ks) != 0);
-        }
+      for (int r = 0; r < 4; r++) {
+        const uint64_t bd = umma_desc(b0 + j * LO::BJ + r * LO::RB, LO::LB, 128);
+        umma_f8(tmem, hj + (uint64_t)((4 * (r + 4) * 128) >> 4), bd, idesc, (j | r) != 0);
+        umma_f8(tmem + NU, hj + (uint64_t)((4 * r * 128) >> 4), bd, idesc, (j | r) != 0);
       }
-    }
     }
     umma_commit(mbar_mma);
   }
-  // 4. accumulators -> int32 columns (one warp polls, the others wait in the barrier)
+  // 4. accumulators (one warp polls the MMA barrier, the others wait in the barrier)
   if (ready) {
     bool fin = true;
     if (warp == 0) fin = mbar_wait_bounded(mbar_mma, 0);
     done = __syncthreads_and(fin) != 0;
   }
   tc_fence_after();
-  // warp w reads TMEM lanes 32 (w % 4) .. +31; warps 4..7 take the second M half
+  // warp w reads TMEM lanes 32 (w % 4) .. +31 for coefficient
+  // k = 128 hsel + 32 q4 + lane (hsel = w / 4): every digit column of k,
+  // top = region0[0] + region1[1], bottom = region0[1] - region1[0]
   const int q4 = warp & 3, hsel = warp >> 2;
-  // decryption and re-encryption: coefficient k = 128 hsel + 32 q4 + lane of
-  // every output polynomial stays in this thread's registers (FOLD: columns
-  // NCOLS.. of row k - 128 hold the second half)
+  const int k = 128 * hsel + 32 * q4 + lane;
+  constexpr int G8 = 8 * LO::G;
   constexpr bool FUSED = OP == kDecrypt || OP == kReenc;
-  static_assert(!FUSED || NU == 16, "fused epilogue reads one 16-column slice");
-  uint32_t racc[16];
-  if (done && FUSED) {
-    tmem_ld16(tmem + ((uint32_t)(32 * q4) << 16) + (LO::FOLD ? 0 : hsel * NU), racc);
-  } else if (done) {
+  float xacc[G8];  // digit column c of coefficient k, times 2^-9 (exact)
+  if (done) {
+    const uint32_t t0 = tmem + ((uint32_t)(32 * q4) << 16);
+    uint32_t f[G8], g[G8];
+    if constexpr (G8 == 8) {
+      tmem_ld8(t0 + (hsel ? 8 : 0), f);
+      tmem_ld8(t0 + (hsel ? 16 : 24), g);
+    } else {
+      tmem_ld16(t0 + (hsel ? 16 : 0), f);
+      tmem_ld16(t0 + (hsel ? 32 : 48), g);
+    }
+    const uint32_t sgn = hsel ? 0x80000000u : 0u;
 #pragma unroll
-    for (int hh = 0; hh < 2; hh++) {
-      if (NT == 256 && hh != hsel) continue;
+    for (int c = 0; c < G8; c++) xacc[c] = __uint_as_float(f[c]) + __uint_as_float(g[c] ^ sgn);
+    if constexpr (!FUSED) {
 #pragma unroll
-      for (int cc = 0; cc < NU; cc += 16) {
-        uint32_t r[16];
-        tmem_ld16(tmem + ((uint32_t)(32 * q4) << 16) + hh * NU + cc, r);
-        const int row = 128 * hh + 32 * q4 + lane;
-#pragma unroll
-        for (int c = 0; c < 16; c++)
-          if (cc + c < S::NCOLS) acc[(cc + c) * 256 + row] = __float2int_rn(__uint_as_float(r[c]) * 512.0f);
-      }
+      for (int c = 0; c < S::NCOLS; c++) acc[c * 256 + k] = __float2int_rn(xacc[c] * 512.0f);
     }
   } else {
     // an input copy or the tensor core did not complete in time: report, and
@@ -494,7 +433,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
 #pragma unroll
     for (int d = 0; d < 4; d++) {
       if (d < D) {
-        v += (1u << (4 * d)) * __float_as_uint(__uint_as_float(racc[c0 + d]) + 24576.0f);
+        v += (1u << (4 * d)) * __float_as_uint(xacc[c0 + d] + 24576.0f);
         off += (1u << (4 * d)) * 0x46C00000u;
       }
     }
@@ -509,13 +448,6 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
   if constexpr (OP == kDecrypt) {
     // m'_k = ((v_k + h2 - (c_m,k << (ep-et))) mod p) >> (ep-1): one bit per
     // thread, gathered into bytes by a ballot per warp
-    const int k = 128 * hsel + 32 * q4 + lane;
-    if (LO::FOLD && hsel) {
-      // the second half's columns, moved down by register selects (no
-      // runtime-indexed array)
-#pragma unroll
-      for (int d = 0; d < S::NCOLS; d++) racc[d] = racc[S::NCOLS + d];
-    }
     const uint32_t v = combine1(0, S::DB);
     const uint32_t cm = field(LO::CTO + L * C::POLYCOMP, k * C::ET, C::ET);
     const uint32_t t = (v + C::H2 - (cm << (C::EP - C::ET))) & pmask;
@@ -525,7 +457,6 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
     if (a.copy_hpk && warp == 0) mo[32 + lane] = a.sk[(size_t)inst * C::SK + C::SK - 64 + lane];
   } else if constexpr (OP == kReenc) {
     // round coefficient k of b' and encode that of v', compare with the ciphertext
-    const int k = 128 * hsel + 32 * q4 + lane;
     const uint32_t mk = (sm[LO::MSG + (k >> 3)] >> (k & 7)) & 1u;
     uint32_t diff = 0;
 #pragma unroll

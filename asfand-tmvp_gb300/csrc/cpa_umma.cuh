@@ -157,6 +157,17 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
       : "memory");
 }
 
+// 8 consecutive f32 columns of this warp's 32 TMEM lanes (load and wait in
+// one asm statement, as tmem_ld16).
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
+}
+
 // Byte-wise e4m3 encoding of four digits 0..15 (one per byte).
 constexpr uint32_t kE4m3Lo8 = 0x44403800u;  // 3, 2, 1, 0
 constexpr uint32_t kE4m3Hi8 = 0x4E4C4A48u;  // 7, 6, 5, 4
@@ -212,30 +223,31 @@ __device__ __forceinline__ void stage_ext(uint32_t *ext, const uint32_t *S, int 
   }
 }
 
-// The Hankel core matrices of every j < L (H: kHankelBytes per polynomial):
+// The first `cores` Hankel core matrices of every j < L (H: cores * 128 bytes
+// per polynomial):
 // row i of core m is s_ext[8m + i .. 8m + i + 15], so row x = 8m + i sits at
-// byte 16x.  Rows x = 4q + sh (q = 0..123) with the same byte shift sh are
+// byte 16x.  Rows x = 4q + sh (q < 2 cores) with the same byte shift sh are
 // windows of consecutive words.  Thread group g (four threads, sh = 0..3)
 // makes the rows q = 2u + (g & 1) for a run of u, from a window of ext words
 // that slides by two words per row; the eight threads of two neighbouring
 // groups store eight consecutive rows (128 contiguous bytes) at a time.
 __device__ __forceinline__ void stage_hankel(uint8_t *H, const uint32_t *ext, int L, int tid,
-                                             int nthreads) {
-  const int pairs = nthreads >> 3;             // group pairs
-  const int run = (62 + pairs - 1) / pairs;     // rows per thread and polynomial
+                                             int nthreads, int cores = kHankelCores) {
+  const int pairs = nthreads >> 3;                 // group pairs
+  const int run = (cores + pairs - 1) / pairs;      // rows per thread and polynomial
   const int sh = tid & 3, par = (tid >> 2) & 1, u0 = (tid >> 3) * run;
   const uint32_t sel = (uint32_t)(sh | ((sh + 1) << 4) | ((sh + 2) << 8) | ((sh + 3) << 12));
-  if (u0 >= 62) return;
+  if (u0 >= cores) return;
   for (int j = 0; j < L; j++) {
     const uint32_t *e = ext + 128 * j;
-    uint8_t *hj = H + (size_t)j * kHankelBytes;
+    uint8_t *hj = H + (size_t)j * cores * 128;
     int q = 2 * u0 + par;
     uint32_t w0 = e[q], w1 = e[q + 1], w2 = e[q + 2], w3 = e[q + 3], w4 = e[q + 4];
-    for (int u = u0; u < u0 + run && u < 62; u++, q += 2) {
+    for (int u = u0; u < u0 + run && u < cores; u++, q += 2) {
       *reinterpret_cast<uint4 *>(hj + 16 * (4 * q + sh)) =
           make_uint4(__byte_perm(w0, w1, sel), __byte_perm(w1, w2, sel), __byte_perm(w2, w3, sel),
                      __byte_perm(w3, w4, sel));
-      if (u + 1 < u0 + run && u + 1 < 62) {
+      if (u + 1 < u0 + run && u + 1 < cores) {
         w0 = w2; w1 = w3; w2 = w4;
         w3 = e[q + 5];
         w4 = e[q + 6];
