@@ -60,6 +60,10 @@ struct tmvp_ctx {
   cudaStream_t side2 = nullptr;         // H(c), which only the final key needs (lowest priority)
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr, hc_ev = nullptr;
   size_t host_chunk = 16384;                       // chunk of host-input decapsulation (0: none)
+  size_t dev_chunk = 32768;                        // chunk of device-input decapsulation (0: none)
+  static constexpr int kLanes = 3;                 // extra streams for chunk chains
+  cudaStream_t lane[kLanes] = {};
+  cudaEvent_t lane_ev[kLanes] = {};
   cudaStream_t copy[2] = {};                       // host-to-device copies of chunked calls
   cudaEvent_t ev_loaded[2][2] = {}, ev_free[2] = {};  // per input slot (and copy stream)
   std::mutex mu;
@@ -315,16 +319,18 @@ DecScratch dec_scratch(const KemParams &P, size_t n, Arena &A) {
 // GenMatrix and H(c) on two side streams, concurrent with the decryption and
 // G on s; the re-encryption waits for GenMatrix, the final key for H(c).
 int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const uint8_t *ct,
-                 const uint8_t *sk, int form, cudaStream_t s, const DecScratch &w) {
+                 const uint8_t *sk, int form, cudaStream_t s, const DecScratch &w, bool fork = true) {
   int r;
-  TRY_CUDA(cudaEventRecord(c->fork_ev, s));
-  TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+  if (fork) {
+    TRY_CUDA(cudaEventRecord(c->fork_ev, s));
+    TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+    TRY_CUDA(cudaStreamWaitEvent(c->side2, c->fork_ev, 0));
+  }
   {
     StageTimer tm_(c, "dec_front", c->side);
     k_dec_front<<<blocks_for(n, kHashBlock), kHashBlock, 0, c->side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 1);
   }
   TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
-  TRY_CUDA(cudaStreamWaitEvent(c->side2, c->fork_ev, 0));
   {
     StageTimer tm_(c, "dec_hash_ct", c->side2);
     k_dec_front<<<blocks_for(n, kHashBlock), kHashBlock, 0, c->side2>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
@@ -365,6 +371,47 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
     k_final_key<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, ct, w.hc, w.kr, w.fail, sk, ss, (int)n);
   }
   c->launches++;
+  return TMVP_OK;
+}
+
+DecScratch dec_slice(const KemParams &P, const DecScratch &w, size_t off) {
+  DecScratch v;
+  v.a_stream = w.a_stream + off * P.gm_bytes;
+  v.s_stream = w.s_stream + off * P.gs_bytes;
+  v.mbuf = w.mbuf + off * 64;
+  v.kr = w.kr + off * 64;
+  v.fail = w.fail + off;
+  v.hc = w.hc + off * 32;
+  return v;
+}
+
+// Decapsulation of n device-resident instances in chunks of cn: the chain of
+// chunk k (decryption, G, re-encryption, final key) runs on lane k mod 4 (the
+// caller's stream or one of the context's lane streams), while GenMatrix and
+// H(c) of all chunks run in order on the two side streams.  Chunk k's
+// re-encryption so overlaps GenMatrix and the decryption of chunk k + 1
+// instead of running after the whole batch's Keccak work.  w covers all n.
+int dec_lanes(tmvp_ctx *c, const KemParams &P, size_t n, size_t cn, uint8_t *ss, const uint8_t *ct,
+              const uint8_t *sk, int form, cudaStream_t s, const DecScratch &w) {
+  int r;
+  const size_t chunks = (n + cn - 1) / cn;
+  const int extra = (int)std::min<size_t>(tmvp_ctx::kLanes, chunks - 1);
+  TRY_CUDA(cudaEventRecord(c->fork_ev, s));
+  TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+  TRY_CUDA(cudaStreamWaitEvent(c->side2, c->fork_ev, 0));
+  for (int i = 0; i < extra; i++) TRY_CUDA(cudaStreamWaitEvent(c->lane[i], c->fork_ev, 0));
+  for (size_t off = 0, k = 0; off < n; off += cn, k++) {
+    const size_t m = std::min(cn, n - off);
+    const int li = (int)(k % (tmvp_ctx::kLanes + 1));
+    cudaStream_t ls = li == 0 ? s : c->lane[li - 1];
+    if ((r = dec_pipeline(c, P, m, ss + off * 32, ct + off * P.ct_bytes, sk + off * P.sk_bytes, form, ls,
+                          dec_slice(P, w, off), false)))
+      return r;
+  }
+  for (int i = 0; i < extra; i++) {
+    TRY_CUDA(cudaEventRecord(c->lane_ev[i], c->lane[i]));
+    TRY_CUDA(cudaStreamWaitEvent(s, c->lane_ev[i], 0));
+  }
   return TMVP_OK;
 }
 
@@ -444,6 +491,12 @@ int tmvp_ctx_create(int device, size_t mem_budget, tmvp_ctx **out) {
     delete c;
     return set_err(TMVP_EDEVICE);
   }
+  for (int i = 0; i < tmvp_ctx::kLanes; i++)
+    if (cudaStreamCreateWithPriority(&c->lane[i], cudaStreamNonBlocking, pri_low) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->lane_ev[i], cudaEventDisableTiming) != cudaSuccess) {
+    delete c;
+    return set_err(TMVP_EDEVICE);
+  }
   *out = c;
   return set_err(TMVP_OK);
 }
@@ -462,6 +515,10 @@ void tmvp_ctx_destroy(tmvp_ctx *c) {
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->join_ev) cudaEventDestroy(c->join_ev);
     if (c->hc_ev) cudaEventDestroy(c->hc_ev);
+    for (int i = 0; i < tmvp_ctx::kLanes; i++) {
+      if (c->lane[i]) cudaStreamDestroy(c->lane[i]);
+      if (c->lane_ev[i]) cudaEventDestroy(c->lane_ev[i]);
+    }
     for (int i = 0; i < 2; i++) {
       if (c->copy[i]) cudaStreamDestroy(c->copy[i]);
       for (int k = 0; k < 2; k++)
@@ -478,6 +535,13 @@ int tmvp_ctx_set_host_chunk(tmvp_ctx *c, size_t n) {
   if (!c || (n != 0 && n < 1024)) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(c->mu);
   c->host_chunk = n;
+  return set_err(TMVP_OK);
+}
+
+int tmvp_ctx_set_dev_chunk(tmvp_ctx *c, size_t n) {
+  if (!c || (n != 0 && n < 1024)) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->dev_chunk = n;
   return set_err(TMVP_OK);
 }
 
@@ -671,7 +735,11 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
   stage_assign(bct, A);
   stage_assign(bsk, A);
   if ((r = upload(bct, s)) || (r = upload(bsk, s))) return set_err(r);
-  if ((r = dec_pipeline(c, P, n, bss.dev, bct.dev, bsk.dev, form, s, w))) return set_err(r);
+  if (c->dev_chunk && n > c->dev_chunk)
+    r = dec_lanes(c, P, n, c->dev_chunk, bss.dev, bct.dev, bsk.dev, form, s, w);
+  else
+    r = dec_pipeline(c, P, n, bss.dev, bct.dev, bsk.dev, form, s, w);
+  if (r) return set_err(r);
   if ((r = download(bss, s))) return set_err(r);
   return set_err(finish(c, s, bss.host));
 }

@@ -109,6 +109,7 @@ def lib(build_if_missing: bool = False):
         getattr(L, nm).restype = None
     L.tmvp_ctx_reserve.argtypes = [P, S]
     L.tmvp_ctx_set_host_chunk.argtypes = [P, S]
+    L.tmvp_ctx_set_dev_chunk.argtypes = [P, S]
     L.tmvp_kem_dec_batch_noalloc.argtypes = [I, S, P, P, P, I, P]
     L.tmvp_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]
     L.tmvp_server_destroy.argtypes = [P]
@@ -312,6 +313,10 @@ class Context:
 
     def set_host_chunk(self, n: int):
         _check(lib().tmvp_ctx_set_host_chunk(self.h, n), "tmvp_ctx_set_host_chunk")
+
+    def set_dev_chunk(self, n: int):
+        """Chunk size of device-buffer decapsulation chains (0: one chain)."""
+        _check(lib().tmvp_ctx_set_dev_chunk(self.h, n), "tmvp_ctx_set_dev_chunk")
 
     def sync_status(self, stream=None):
         _check(lib().tmvp_ctx_sync_status(self.h, stream), "tmvp_ctx_sync_status")

@@ -274,12 +274,15 @@ def run_ours(args):
         reenc = max(stages.items(), key=lambda kv: kv[1][1])[0]
     cnt, ms = stages[reenc]
     avg_s = ms / cnt / 1e3
+    per_launch = n * args.steps / cnt  # instances per launch (device batches run in chunks)
     traffic = _ncu_traffic(reenc)
-    ops = n * 12 * POLY_OPS  # 12 negacyclic 256x256 products per re-encryption
+    if traffic is not None:
+        traffic = traffic * per_launch / n  # the ncu figure is per full-batch launch
+    ops = per_launch * 12 * POLY_OPS  # 12 negacyclic 256x256 products per re-encryption
     ach = ops / avg_s / 1e12
     props = torch.cuda.get_device_properties(dev)
     sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
-    mma_floor_s = n * REENC_MMAS * MMA_CYCLES / (props.multi_processor_count * sm_mhz * 1e6)
+    mma_floor_s = per_launch * REENC_MMAS * MMA_CYCLES / (props.multi_processor_count * sm_mhz * 1e6)
     roof = {"kernel": reenc, "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
             "frac": ach / bf16,
             "peak_source": f"{peak_src} bf16 dense; achieved = schoolbook-equivalent integer ops",
@@ -293,7 +296,8 @@ def run_ours(args):
     if front:
         fs = front[1] / front[0] / 1e3
         roof["keccak_front"] = {"kernel": "dec_front (GenMatrix, 23 Keccak-f per instance)",
-                                "gperm_per_s": n * 23 / fs / 1e9, "avg_launch_ms": fs * 1e3,
+                                "gperm_per_s": (n * args.steps / front[0]) * 23 / fs / 1e9,
+                                "avg_launch_ms": fs * 1e3,
                                 "bound": "integer ALU pipe"}
 
     line = {

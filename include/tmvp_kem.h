@@ -154,6 +154,13 @@ int tmvp_ctx_reserve(tmvp_ctx *ctx, size_t bytes);
  * kernels of the previous chunk; 0 = one copy, then the kernels.  Default
  * 16384; n must be 0 or >= 1024. */
 int tmvp_ctx_set_host_chunk(tmvp_ctx *ctx, size_t n);
+/* Batched decapsulation with device-resident buffers splits batches larger
+ * than n into chunks whose decryption / G / re-encryption / final-key chains
+ * run on up to four streams (the caller's and three of the context's), so
+ * that one chunk's re-encryption overlaps the next chunk's GenMatrix and
+ * decryption; 0 = one chain over the whole batch.  Default 32768; n must be
+ * 0 or >= 1024.  Results do not depend on it. */
+int tmvp_ctx_set_dev_chunk(tmvp_ctx *ctx, size_t n);
 
 /* ---------------------------------------------------------------------------
  * Request-serving loop with device-resident keys and continuous batching.

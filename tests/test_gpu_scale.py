@@ -104,3 +104,35 @@ def test_chunked_host_decapsulation(kem):
     torch.cuda.synchronize()
     assert torch.equal(out_d, want)
     assert not torch.equal(want[n - 3], ss[n - 3]) and torch.equal(want[:n - 3], ss[:n - 3])
+
+
+@pytest.mark.parametrize("chunk", [0, 8192, 12000])
+def test_chunked_device_decapsulation(kem, chunk):
+    """Device buffers larger than the device chunk run as chains on four
+    streams (the caller's and three lanes); every chunk size, including a
+    ragged last chunk and more chunks than lanes, gives the keys of the
+    encapsulation and rejects a tampered ciphertext in the last chunk."""
+    import torch
+    T, ctx = kem
+    dev = torch.device("cuda", 0)
+    n = 40000
+    z = T.sizes(T.SABER)
+    coins = torch.from_numpy(T.splitmix_bytes(41, n * 96).reshape(n, 96)).to(dev)
+    ec = torch.from_numpy(T.splitmix_bytes(42, n * 32).reshape(n, 32)).to(dev)
+    pk = torch.empty((n, z.pk_bytes), dtype=torch.uint8, device=dev)
+    sk = torch.empty((n, z.sk_bytes), dtype=torch.uint8, device=dev)
+    ct = torch.empty((n, z.ct_bytes), dtype=torch.uint8, device=dev)
+    ss = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+    ctx.kem_keypair_ptr(T.SABER, n, pk, sk, coins)
+    ctx.kem_enc_ptr(T.SABER, n, ct, ss, pk, ec)
+    ct[n - 5, 100] ^= 4
+    torch.cuda.synchronize()
+    try:
+        ctx.set_dev_chunk(chunk)
+        out = torch.zeros_like(ss)
+        ctx.kem_dec_ptr(T.SABER, n, out, ct, sk)
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_dev_chunk(32768)
+    assert torch.equal(out[:n - 5], ss[:n - 5]) and torch.equal(out[n - 4:], ss[n - 4:])
+    assert not torch.equal(out[n - 5], ss[n - 5])
