@@ -5,9 +5,9 @@
 // Per instance:
 //   1. the packed inputs arrive by TMA bulk copies (cp.async.bulk) issued by
 //      one thread, counted on an mbarrier;
-//   2. secrets (CBD or unpacked), radix-16 digit columns (r16_digits, raw
-//      e4m3 bytes worth digit * 2^-9) with K reversed, s_ext and the Hankel
-//      core matrices (cpa_umma.cuh);
+//   2. secrets (CBD or unpacked) straight into s_ext, radix-16 digit columns
+//      (r16_digits, raw e4m3 bytes worth digit * 2^-9) with K reversed, then
+//      the Hankel core matrices (cpa_umma.cuh);
 //   3. one thread issues the 8 l tcgen05.mma (M = 128, N = 16 / 32, K = 32;
 //      each window of the Hankel sequence serves both M halves through the
 //      negacyclic wrap) into tensor memory and commits them to an mbarrier;
@@ -106,8 +106,7 @@ struct LayoutC {
   static constexpr int ENG_BYTES = ENG_END_OPS > S::NCOLS * 1024 ? ENG_END_OPS : S::NCOLS * 1024;
   static constexpr int CTO = al16c(ENG + ENG_BYTES);
   static constexpr int MSG = HAS_CT ? al16c(CTO + C::CT + 16) : CTO;
-  static constexpr int SENC = HAS_B ? al16c(MSG + 32 + 16) : MSG;
-  static constexpr int SEC8 = al16c(SENC + C::L * 256);
+  static constexpr int SEC8 = HAS_B ? al16c(MSG + 32 + 16) : MSG;
   static constexpr int OUT = OP == kKeygen ? al16c(SEC8 + C::L * 256) : SEC8;
   static constexpr int OUT_BYTES = OP == kEncrypt ? C::CT + 16
                                    : (OP == kKeygen ? C::L * C::POLYCOMP + C::INDCPA_SK + 16 : 0);
@@ -123,11 +122,11 @@ struct LayoutC {
 // the stream), as four words of two 16-bit lanes.
 template <int W>
 __device__ __forceinline__ void unpack8c(const uint8_t *base, int byte0, uint32_t (&X)[4]) {
-  const uint32_t *wp = reinterpret_cast<const uint32_t *>(base + (byte0 & ~3));
+  const uint32_t wp = smem_u32(base) + (uint32_t)(byte0 & ~3);
   const int sh = 8 * (byte0 & 3);
   uint32_t q[5];
 #pragma unroll
-  for (int i = 0; i < 5; i++) q[i] = wp[i];
+  for (int i = 0; i < 5; i++) q[i] = lds32(wp + 4 * i);
   uint32_t a[4];
 #pragma unroll
   for (int i = 0; i < 4; i++) a[i] = __funnelshift_r(q[i], q[i + 1], sh);
@@ -218,74 +217,92 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
   ready = __syncthreads_and(ready) != 0;
 
   uint32_t *sec8w = reinterpret_cast<uint32_t *>(sm + LO::SEC8);
-  uint32_t *sencw = reinterpret_cast<uint32_t *>(sm + LO::SENC);
   uint8_t *H = sm + LO::H, *Bm = sm + LO::BM;
-  uint32_t *ext = reinterpret_cast<uint32_t *>(sm + LO::EXT);
+  const uint32_t ext32 = smem_u32(sm + LO::EXT);
   int *acc = reinterpret_cast<int *>(sm + LO::ENG);
   bool ok = true, done = false;
   if (ready) {
-    // 1. secrets
-    if (OP == kDecrypt && !C::SABLE) {
-      // 13-bit two's complement (SABER pack.cu:53-84), eight coefficients at a time
-      constexpr uint32_t m = ((1u << C::EQ) - 1u) * 0x10001u;
-      for (int g8 = tid; g8 < L * 32; g8 += NT) {
+    // 1. secrets, straight into s_ext (s_ext[d] = -s[d + 1] for d < 255,
+    // s[d - 255] for 255 <= d <= 510, 0 at 511; 128 words per j).  Warp
+    // j < L makes polynomial j: lane g encodes the words 2g, 2g + 1
+    // (coefficients 8g..8g+7) and takes word 2g + 2 from the next lane
+    // (word 0 for lane 31).
+    if (warp < L) {
+      const int j = warp, g = lane;
+      uint32_t sb[2];
+      if (OP == kDecrypt && !C::SABLE) {
+        // 13-bit two's complement (SABER pack.cu:53-84)
+        constexpr uint32_t m = ((1u << C::EQ) - 1u) * 0x10001u;
         uint32_t X[4];
-        unpack8c<C::EQ>(sm + LO::SKO, g8 * C::EQ, X);
+        unpack8c<C::EQ>(sm + LO::SKO, (32 * j + g) * C::EQ, X);
         uint32_t bad = 0;
 #pragma unroll
         for (int i = 0; i < 4; i++) bad |= ((X[i] + 0x00800080u) & m) & 0xFF00FF00u;
-        const uint32_t s0 = __byte_perm(X[0], X[1], 0x6420), s1 = __byte_perm(X[2], X[3], 0x6420);
-        ok = ok && bad == 0u && small4(s0) && small4(s1);
-        sencw[2 * g8] = enc4<kFp8Tcgen05>(s0);
-        sencw[2 * g8 + 1] = enc4<kFp8Tcgen05>(s1);
-      }
-    } else {
-      for (int w = tid; w < L * 64; w += NT) {
-        uint32_t sb;
-        if (OP == kDecrypt) {
-          // 2-bit two's complement (SABLE pack.cu:371-376): one byte = 4 coefficients
-          const uint32_t x = sm[LO::SKO + w];
-          const uint32_t spread = (x & 3u) | ((x & 0xcu) << 6) | ((x & 0x30u) << 12) | ((x & 0xc0u) << 18);
-          sb = spread | (((spread >> 1) & 0x01010101u) * 0xfcu);
-        } else if (C::MU == 8) {
-          // CBD mu = 8 (SABER poly.cu:864-887)
-          const uint32_t x = *reinterpret_cast<const uint32_t *>(sm + LO::SS + 4 * w);
-          uint32_t n = x - ((x >> 1) & 0x55555555u);
-          n = (n & 0x33333333u) + ((n >> 2) & 0x33333333u);
-          sb = __vsub4(n & 0x0f0f0f0fu, (n >> 4) & 0x0f0f0f0fu);
-        } else if (C::MU == 2) {
-          // CBD mu = 2 (SABLE fips202.cu:625-651)
-          const uint32_t x = sm[LO::SS + w];
-          const uint32_t spread = (x & 3u) | ((x & 0xcu) << 6) | ((x & 0x30u) << 12) | ((x & 0xc0u) << 18);
-          sb = __vsub4(spread & 0x01010101u, (spread >> 1) & 0x01010101u);
-        } else {
-          // CBD mu = 6, 10: fields of mu bits, popcount halves
-          uint32_t r = 0;
+        ok = bad == 0u;
+        sb[0] = __byte_perm(X[0], X[1], 0x6420);
+        sb[1] = __byte_perm(X[2], X[3], 0x6420);
+      } else {
 #pragma unroll
-          for (int b = 0; b < 4; b++) {
-            const uint32_t x = get_bits(sm + LO::SS, (4 * w + b) * C::MU, C::MU);
-            const int v = __popc(x & ((1u << (C::MU / 2)) - 1u)) - __popc(x >> (C::MU / 2));
-            r |= ((uint32_t)v & 0xffu) << (8 * b);
+        for (int h = 0; h < 2; h++) {
+          const int w = 64 * j + 2 * g + h;
+          if (OP == kDecrypt) {
+            // 2-bit two's complement (SABLE pack.cu:371-376): one byte = 4 coefficients
+            const uint32_t x = sm[LO::SKO + w];
+            const uint32_t spread = (x & 3u) | ((x & 0xcu) << 6) | ((x & 0x30u) << 12) | ((x & 0xc0u) << 18);
+            sb[h] = spread | (((spread >> 1) & 0x01010101u) * 0xfcu);
+          } else if (C::MU == 8) {
+            // CBD mu = 8 (SABER poly.cu:864-887)
+            const uint32_t x = lds32(smem_u32(sm + LO::SS) + 4 * w);
+            uint32_t n = x - ((x >> 1) & 0x55555555u);
+            n = (n & 0x33333333u) + ((n >> 2) & 0x33333333u);
+            sb[h] = __vsub4(n & 0x0f0f0f0fu, (n >> 4) & 0x0f0f0f0fu);
+          } else if (C::MU == 2) {
+            // CBD mu = 2 (SABLE fips202.cu:625-651)
+            const uint32_t x = sm[LO::SS + w];
+            const uint32_t spread = (x & 3u) | ((x & 0xcu) << 6) | ((x & 0x30u) << 12) | ((x & 0xc0u) << 18);
+            sb[h] = __vsub4(spread & 0x01010101u, (spread >> 1) & 0x01010101u);
+          } else {
+            // CBD mu = 6, 10: fields of mu bits, popcount halves
+            uint32_t r = 0;
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+              const uint32_t x = get_bits(sm + LO::SS, (4 * w + b) * C::MU, C::MU);
+              const int v = __popc(x & ((1u << (C::MU / 2)) - 1u)) - __popc(x >> (C::MU / 2));
+              r |= ((uint32_t)v & 0xffu) << (8 * b);
+            }
+            sb[h] = r;
           }
-          sb = r;
         }
-        ok = ok && small4(sb);
-        if (OP == kKeygen) sec8w[w] = sb;
-        sencw[w] = enc4<kFp8Tcgen05>(sb);
       }
+      ok = ok && small4(sb[0]) && small4(sb[1]);
+      if (OP == kKeygen) {
+        sec8w[64 * j + 2 * g] = sb[0];
+        sec8w[64 * j + 2 * g + 1] = sb[1];
+      }
+      const uint32_t e0 = enc4<kFp8Tcgen05>(sb[0]), e1 = enc4<kFp8Tcgen05>(sb[1]);
+      const uint32_t nx = __shfl_sync(0xffffffffu, e0, (lane + 1) & 31);
+      const uint32_t p0 = __byte_perm(e0, e1, 0x4321), p1 = __byte_perm(e1, nx, 0x4321);
+      // word 63: s_ext[255] = s[0] keeps its sign; word 127: s_ext[511] = 0
+      const uint32_t n1 = p1 ^ (g == 31 ? 0x00808080u : 0x80808080u);
+      const uint32_t q1 = g == 31 ? __byte_perm(e1, 0u, 0x4321) : p1;
+      sts64(ext32 + 512 * j + 8 * g, p0 ^ 0x80808080u, n1);
+      sts64(ext32 + 512 * j + 256 + 8 * g, p0, q1);
     }
-    // 2. digit columns (K reversed, core-matrix order), then the zero columns
+    // 2. digit columns (K reversed, core-matrix order).  The columns past
+    // NCOLS of each stored group are left as they are: they only feed
+    // accumulator columns that are never read.
+    const uint32_t bm32 = smem_u32(Bm);
     auto put_digits = [&](const uint32_t (&X)[4], auto wc, int cb, int j, int kq) {
       constexpr int W = decltype(wc)::value;
 #pragma unroll
       for (int d = 0; d < r16_digits(W); d++) {
         const uint2 v = raw_digits8<W>(X, d);
         const int n = cb + d;
-        *reinterpret_cast<uint2 *>(Bm + j * LO::BJ + LO::chunk_off(kq >> 1) + 8 * (kq & 1) + (n >> 3) * 128 +
-                                   (n & 7) * 16) = v;
+        sts64(bm32 + j * LO::BJ + LO::chunk_off(kq >> 1) + 8 * (kq & 1) + (n >> 3) * 128 + (n & 7) * 16, v.x, v.y);
       }
     };
-    for (int idx = tid; idx < S::R * L * 32; idx += NT) {
+    // items go to the warps past L first (warps below L made the secrets)
+    for (int idx = (tid + NT - 32 * L) % NT; idx < S::R * L * 32; idx += NT) {
       const int grp = idx & 31, j = (idx >> 5) % L, p = idx / (32 * L);
       const int kq = 31 - grp;  // coefficients 8grp..8grp+7 are rows k' = 8kq+7..8kq
       uint32_t X[4];
@@ -301,17 +318,9 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
         put_digits(X, std::integral_constant<int, S::WB>{}, S::RA * S::DA + (p - S::RA) * S::DB, j, kq);
       }
     }
-    constexpr int PADC = 8 * LO::G - S::NCOLS;  // zero columns of the stored groups
-    for (int idx = tid; idx < L * PADC * 16; idx += NT) {
-      const int j = idx / (PADC * 16), r = idx % (PADC * 16), n = S::NCOLS + r % PADC, ac = r / PADC;
-      *reinterpret_cast<uint4 *>(Bm + j * LO::BJ + LO::chunk_off(ac) + (n >> 3) * 128 + (n & 7) * 16) =
-          make_uint4(0u, 0u, 0u, 0u);
-    }
   }
-  __syncthreads();  // secret words complete before s_ext reads them
-  if (ready) stage_ext(ext, sencw, L, tid, NT, [](uint32_t v) { return v ^ 0x80808080u; });
-  __syncthreads();
-  if (ready) stage_hankel(H, ext, L, tid, NT, kHankelCores5);
+  __syncthreads();  // s_ext complete, and the streams inside H read, before H is written
+  if (ready) stage_hankel_ct<L, NT, kHankelCores5>(smem_u32(H), ext32, tid);
   fence_async_smem();  // generic-proxy writes -> visible to the tensor core
   ok = __syncthreads_and(ok) != 0;
   if (!ok && tid == 0 && a.err) atomicOr(a.err, 1);

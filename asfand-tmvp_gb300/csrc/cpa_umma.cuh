@@ -223,6 +223,44 @@ __device__ __forceinline__ void stage_ext(uint32_t *ext, const uint32_t *S, int 
   }
 }
 
+// Shared-memory accesses through 32-bit shared-window addresses.
+__device__ __forceinline__ uint32_t lds32(uint32_t a) {
+  uint32_t v;
+  asm volatile("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ void sts64(uint32_t a, uint32_t x, uint32_t y) {
+  asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(a), "r"(x), "r"(y) : "memory");
+}
+__device__ __forceinline__ void sts128(uint32_t a, uint32_t x, uint32_t y, uint32_t z, uint32_t w) {
+  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(x), "r"(y), "r"(z), "r"(w) : "memory");
+}
+
+// stage_hankel with compile-time sizes and 32-bit shared addresses (H, ext:
+// shared-window byte addresses): the same thread groups, each thread's rows
+// unrolled from one load of the ext words they span.
+template <int L, int NT, int CORES>
+__device__ __forceinline__ void stage_hankel_ct(uint32_t H, uint32_t ext, int tid) {
+  constexpr int PAIRS = NT >> 3;
+  constexpr int RUN = (CORES + PAIRS - 1) / PAIRS;  // rows per thread and polynomial
+  const int sh = tid & 3, par = (tid >> 2) & 1, u0 = (tid >> 3) * RUN;
+  if (u0 >= CORES) return;
+  const uint32_t sel = 0x3210u + 0x1111u * (uint32_t)sh;
+  const int q = 2 * u0 + par;
+#pragma unroll
+  for (int j = 0; j < L; j++) {
+    uint32_t w[2 * RUN + 3];
+#pragma unroll
+    for (int i = 0; i < 2 * RUN + 3; i++) w[i] = lds32(ext + 512 * j + 4 * (q + i));
+    const uint32_t h = H + (uint32_t)(j * CORES * 128) + 16 * (4 * q + sh);
+#pragma unroll
+    for (int r = 0; r < RUN; r++)
+      if (CORES % PAIRS == 0 || u0 + r < CORES)
+        sts128(h + 128 * r, __byte_perm(w[2 * r], w[2 * r + 1], sel), __byte_perm(w[2 * r + 1], w[2 * r + 2], sel),
+               __byte_perm(w[2 * r + 2], w[2 * r + 3], sel), __byte_perm(w[2 * r + 3], w[2 * r + 4], sel));
+  }
+}
+
 // The first `cores` Hankel core matrices of every j < L (H: cores * 128 bytes
 // per polynomial):
 // row i of core m is s_ext[8m + i .. 8m + i + 15], so row x = 8m + i sits at
