@@ -227,8 +227,10 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
     // j < L makes polynomial j: lane g encodes the words 2g, 2g + 1
     // (coefficients 8g..8g+7) and takes word 2g + 2 from the next lane
     // (word 0 for lane 31).
-    if (warp < L) {
-      const int j = warp, g = lane;
+    // the secrets of j go to a warp that makes no digit columns where one is free
+    const int sj = S::R == 1 ? warp - L : (warp - S::R + 8) % 8;
+    if (sj >= 0 && sj < L) {
+      const int j = sj, g = lane;
       uint32_t sb[2];
       if (OP == kDecrypt && !C::SABLE) {
         // 13-bit two's complement (SABER pack.cu:53-84)
@@ -288,35 +290,38 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
       sts64(ext32 + 512 * j + 8 * g, p0 ^ 0x80808080u, n1);
       sts64(ext32 + 512 * j + 256 + 8 * g, p0, q1);
     }
-    // 2. digit columns (K reversed, core-matrix order).  The columns past
+    // 2. digit columns (K reversed, core-matrix order): lane g converts
+    // coefficients 8g..8g+7 (K rows k' = 8kq+7..8kq, kq = 31 - g) of one
+    // polynomial per item.  Warp p < R makes polynomial p of every j (one
+    // item per j); with R == 1 (decryption) warp j makes j.  The columns past
     // NCOLS of each stored group are left as they are: they only feed
     // accumulator columns that are never read.
-    const uint32_t bm32 = smem_u32(Bm);
-    auto put_digits = [&](const uint32_t (&X)[4], auto wc, int cb, int j, int kq) {
+    const int kq = 31 - lane;
+    const uint32_t bl = smem_u32(Bm) + LO::chunk_off(kq >> 1) + 8 * (kq & 1);
+    auto item = [&](auto wc, uint32_t src, int cb, int j) {
       constexpr int W = decltype(wc)::value;
+      uint32_t X[4];
+      unpack8c<W>(sm + src, lane * W, X);
 #pragma unroll
       for (int d = 0; d < r16_digits(W); d++) {
         const uint2 v = raw_digits8<W>(X, d);
         const int n = cb + d;
-        sts64(bm32 + j * LO::BJ + LO::chunk_off(kq >> 1) + 8 * (kq & 1) + (n >> 3) * 128 + (n & 7) * 16, v.x, v.y);
+        sts64(bl + j * LO::BJ + (n >> 3) * 128 + (n & 7) * 16, v.x, v.y);
       }
     };
-    // items go to the warps past L first (warps below L made the secrets)
-    for (int idx = (tid + NT - 32 * L) % NT; idx < S::R * L * 32; idx += NT) {
-      const int grp = idx & 31, j = (idx >> 5) % L, p = idx / (32 * L);
-      const int kq = 31 - grp;  // coefficients 8grp..8grp+7 are rows k' = 8kq+7..8kq
-      uint32_t X[4];
-      if (OP == kDecrypt) {
-        unpack8c<S::WB>(sm + LO::CTO, (32 * j + grp) * S::WB, X);
-        put_digits(X, std::integral_constant<int, S::WB>{}, 0, j, kq);
-      } else if (p < S::RA) {
+    if constexpr (S::R == 1) {
+      if (warp < L) item(std::integral_constant<int, S::WB>{}, LO::CTO + 32 * warp * S::WB, 0, warp);
+    } else if (warp < S::RA) {
+      const int p = warp;
+#pragma unroll
+      for (int j = 0; j < L; j++) {
         const int ij = (OP == kKeygen) ? (j * L + p) : (p * L + j);
-        unpack8c<S::WA>(sm + LO::A, (32 * ij + grp) * S::WA, X);
-        put_digits(X, std::integral_constant<int, S::WA>{}, p * S::DA, j, kq);
-      } else {
-        unpack8c<S::WB>(sm + LO::B, (32 * j + grp) * S::WB, X);
-        put_digits(X, std::integral_constant<int, S::WB>{}, S::RA * S::DA + (p - S::RA) * S::DB, j, kq);
+        item(std::integral_constant<int, S::WA>{}, LO::A + 32 * ij * S::WA, p * S::DA, j);
       }
+    } else if (warp < S::R) {
+#pragma unroll
+      for (int j = 0; j < L; j++)
+        item(std::integral_constant<int, S::WB>{}, LO::B + 32 * j * S::WB, S::RA * S::DA + (warp - S::RA) * S::DB, j);
     }
   }
   __syncthreads();  // s_ext complete, and the streams inside H read, before H is written
@@ -373,9 +378,13 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
       tmem_ld16(t0 + (hsel ? 16 : 0), f);
       tmem_ld16(t0 + (hsel ? 32 : 48), g);
     }
-    const uint32_t sgn = hsel ? 0x80000000u : 0u;
+    if (hsel) {
 #pragma unroll
-    for (int c = 0; c < G8; c++) xacc[c] = __uint_as_float(f[c]) + __uint_as_float(g[c] ^ sgn);
+      for (int c = 0; c < S::NCOLS; c++) xacc[c] = __uint_as_float(f[c]) - __uint_as_float(g[c]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < S::NCOLS; c++) xacc[c] = __uint_as_float(f[c]) + __uint_as_float(g[c]);
+    }
     if constexpr (!FUSED) {
 #pragma unroll
       for (int c = 0; c < S::NCOLS; c++) acc[c * 256 + k] = __float2int_rn(xacc[c] * 512.0f);
