@@ -174,12 +174,21 @@ __device__ __forceinline__ int hash_group(const HashGroup *T, int ng, int gi) {
   return lo;
 }
 
+// part 1: GenMatrix of every instance; part 2: H(c); part 0: both, threads
+// total..2 total - 1 hashing.
 __global__ void __launch_bounds__(128) k_mix_front(const HashGroup *T, int ng, int total, int part) {
-  const int gi = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-  if (gi >= total) return;
+  int gi = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  bool gen = part == 1;
+  if (part == 0) {
+    if (gi >= 2 * total) return;
+    gen = gi < total;
+    if (!gen) gi -= total;
+  } else if (gi >= total) {
+    return;
+  }
   const HashGroup &G = T[hash_group(T, ng, gi)];
   const size_t i = (size_t)(gi - G.first);
-  if (part == 1) dec_genmatrix_one(G.P, G.sk, G.a_stream, i);
+  if (gen) dec_genmatrix_one(G.P, G.sk, G.a_stream, i);
   else dec_hash_ct_one(G.P, G.ct, G.hc, i);
 }
 

@@ -56,11 +56,10 @@ struct tmvp_ctx {
   size_t ws_cap = 0;
   int *d_err = nullptr;   // device-side input-range flag
   uint64_t launches = 0;
-  cudaStream_t side = nullptr;          // GenMatrix beside the decryption (highest priority)
-  cudaStream_t side2 = nullptr;         // H(c), which only the final key needs (lowest priority)
-  cudaEvent_t fork_ev = nullptr, join_ev = nullptr, hc_ev = nullptr;
+  cudaStream_t side = nullptr;          // GenMatrix and H(c) beside the decryption (highest priority)
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   size_t host_chunk = 16384;                       // chunk of host-input decapsulation (0: none)
-  size_t dev_chunk = 32768;                        // chunk of device-input decapsulation (0: none)
+  size_t dev_chunk = 0;                            // chunk of device-input decapsulation (0: none)
   static constexpr int kLanes = 3;                 // extra streams for chunk chains
   cudaStream_t lane[kLanes] = {};
   cudaEvent_t lane_ev[kLanes] = {};
@@ -315,28 +314,23 @@ DecScratch dec_scratch(const KemParams &P, size_t n, Arena &A) {
   return w;
 }
 
-// Decapsulation of n instances in device memory (16-byte aligned):
-// GenMatrix and H(c) on two side streams, concurrent with the decryption and
-// G on s; the re-encryption waits for GenMatrix, the final key for H(c).
+// Decapsulation of n instances in device memory (16-byte aligned): GenMatrix
+// and H(c) in one launch (2n sponges, so the integer pipe has warps enough)
+// on the high-priority side stream, concurrent with the decryption and G on
+// s; the re-encryption and the final key wait for it.
 int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const uint8_t *ct,
                  const uint8_t *sk, int form, cudaStream_t s, const DecScratch &w, bool fork = true) {
   int r;
   if (fork) {
     TRY_CUDA(cudaEventRecord(c->fork_ev, s));
     TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
-    TRY_CUDA(cudaStreamWaitEvent(c->side2, c->fork_ev, 0));
   }
   {
     StageTimer tm_(c, "dec_front", c->side);
-    k_dec_front<<<blocks_for(n, kHashBlock), kHashBlock, 0, c->side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 1);
+    k_dec_front<<<blocks_for(2 * n, kHashBlock), kHashBlock, 0, c->side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 0);
   }
   TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
-  {
-    StageTimer tm_(c, "dec_hash_ct", c->side2);
-    k_dec_front<<<blocks_for(n, kHashBlock), kHashBlock, 0, c->side2>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
-  }
-  c->launches += 2;
-  TRY_CUDA(cudaEventRecord(c->hc_ev, c->side2));
+  c->launches++;
   CpaArgs a{};
   a.P = P;
   a.n = (int)n;
@@ -365,7 +359,6 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   b.ct = ct;
   b.fail = w.fail;
   if ((r = run_cpa(c, form, kReenc, b, s))) return r;
-  TRY_CUDA(cudaStreamWaitEvent(s, c->hc_ev, 0));  // join: H(c)
   {
     StageTimer tm_(c, "final_key", s);
     k_final_key<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, ct, w.hc, w.kr, w.fail, sk, ss, (int)n);
@@ -398,7 +391,6 @@ int dec_lanes(tmvp_ctx *c, const KemParams &P, size_t n, size_t cn, uint8_t *ss,
   const int extra = (int)std::min<size_t>(tmvp_ctx::kLanes, chunks - 1);
   TRY_CUDA(cudaEventRecord(c->fork_ev, s));
   TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
-  TRY_CUDA(cudaStreamWaitEvent(c->side2, c->fork_ev, 0));
   for (int i = 0; i < extra; i++) TRY_CUDA(cudaStreamWaitEvent(c->lane[i], c->fork_ev, 0));
   for (size_t off = 0, k = 0; off < n; off += cn, k++) {
     const size_t m = std::min(cn, n - off);
@@ -469,17 +461,15 @@ int tmvp_ctx_create(int device, size_t mem_budget, tmvp_ctx **out) {
   c->device = device;
   c->budget = mem_budget;
   Guard g(c);
-  // GenMatrix, which the re-encryption waits for, runs at the highest stream
-  // priority, so its blocks are scheduled ahead of the decryption beside it;
-  // H(c), needed only by the final key, runs at the lowest and fills gaps
+  // GenMatrix and H(c), which the re-encryption and the final key wait for,
+  // run at the highest stream priority, so their blocks are scheduled ahead
+  // of the decryption beside them; chunk lanes run at the lowest
   int pri_low = 0, pri_high = 0;
   cudaDeviceGetStreamPriorityRange(&pri_low, &pri_high);
   if (cudaMalloc(&c->d_err, sizeof(int)) != cudaSuccess || cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess ||
       cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, pri_high) != cudaSuccess ||
-      cudaStreamCreateWithPriority(&c->side2, cudaStreamNonBlocking, pri_low) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->hc_ev, cudaEventDisableTiming) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->copy[0], cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->copy[1], cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_loaded[0][0], cudaEventDisableTiming) != cudaSuccess ||
@@ -511,10 +501,8 @@ void tmvp_ctx_destroy(tmvp_ctx *c) {
     if (c->ws) cudaFree(c->ws);
     if (c->d_err) cudaFree(c->d_err);
     if (c->side) cudaStreamDestroy(c->side);
-    if (c->side2) cudaStreamDestroy(c->side2);
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->join_ev) cudaEventDestroy(c->join_ev);
-    if (c->hc_ev) cudaEventDestroy(c->hc_ev);
     for (int i = 0; i < tmvp_ctx::kLanes; i++) {
       if (c->lane[i]) cudaStreamDestroy(c->lane[i]);
       if (c->lane_ev[i]) cudaEventDestroy(c->lane_ev[i]);
@@ -1160,19 +1148,16 @@ int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws,
   const unsigned nb = blocks_for((size_t)total, kHashBlock);
   TRY_CUDA(cudaEventRecord(c->fork_ev, s));
   TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
-  k_mix_front<<<nb, kHashBlock, 0, c->side>>>(th, (int)ng, total, 1);
+  // GenMatrix and H(c) of every group in one launch (2 total sponges)
+  k_mix_front<<<blocks_for(2 * (size_t)total, kHashBlock), kHashBlock, 0, c->side>>>(th, (int)ng, total, 0);
   TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
-  TRY_CUDA(cudaStreamWaitEvent(c->side2, c->fork_ev, 0));
-  k_mix_front<<<nb, kHashBlock, 0, c->side2>>>(th, (int)ng, total, 2);
-  TRY_CUDA(cudaEventRecord(c->hc_ev, c->side2));
   if (cpa_launch_mixed(kDecrypt, ga.data(), (int)ng, tdec, s, persist_dec ? shape_dec : -1) != 0)
     return TMVP_EDEVICE;
   k_mix_g<<<nb, kHashBlock, 0, s>>>(th, (int)ng, total);
   TRY_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));  // GenMatrix
   if (cpa_launch_mixed(kReenc, gb.data(), (int)ng, tre, s, persist_re ? shape_re : -1) != 0) return TMVP_EDEVICE;
-  TRY_CUDA(cudaStreamWaitEvent(s, c->hc_ev, 0));  // H(c)
   k_mix_final<<<nb, kHashBlock, 0, s>>>(th, (int)ng, total);
-  c->launches += 6;
+  c->launches += 5;
   TRY_CUDA(cudaGetLastError());
   return TMVP_OK;
 }
