@@ -64,7 +64,8 @@ struct tmvp_ctx {
   cudaStream_t lane[kLanes] = {};
   cudaEvent_t lane_ev[kLanes] = {};
   cudaStream_t copy[2] = {};                       // host-to-device copies of chunked calls
-  cudaEvent_t ev_loaded[2][2] = {}, ev_free[2] = {};  // per input slot (and copy stream)
+  static constexpr int kSlots = 3;                 // input slots of chunked host calls
+  cudaEvent_t ev_loaded[kSlots][2] = {}, ev_free[kSlots] = {};  // per input slot (and copy stream)
   std::mutex mu;
   // optional per-stage timing: CUDA events recorded on the launching stream
   bool timing = false;
@@ -471,16 +472,17 @@ int tmvp_ctx_create(int device, size_t mem_budget, tmvp_ctx **out) {
       cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->copy[0], cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&c->copy[1], cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_loaded[0][0], cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_loaded[0][1], cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_loaded[1][0], cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_loaded[1][1], cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_free[0], cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_free[1], cudaEventDisableTiming) != cudaSuccess) {
+      cudaStreamCreateWithFlags(&c->copy[1], cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return set_err(TMVP_EDEVICE);
   }
+  for (int i = 0; i < tmvp_ctx::kSlots; i++)
+    if (cudaEventCreateWithFlags(&c->ev_loaded[i][0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_loaded[i][1], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_free[i], cudaEventDisableTiming) != cudaSuccess) {
+      delete c;
+      return set_err(TMVP_EDEVICE);
+    }
   for (int i = 0; i < tmvp_ctx::kLanes; i++)
     if (cudaStreamCreateWithPriority(&c->lane[i], cudaStreamNonBlocking, pri_low) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->lane_ev[i], cudaEventDisableTiming) != cudaSuccess) {
@@ -507,8 +509,9 @@ void tmvp_ctx_destroy(tmvp_ctx *c) {
       if (c->lane[i]) cudaStreamDestroy(c->lane[i]);
       if (c->lane_ev[i]) cudaEventDestroy(c->lane_ev[i]);
     }
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < 2; i++)
       if (c->copy[i]) cudaStreamDestroy(c->copy[i]);
+    for (int i = 0; i < tmvp_ctx::kSlots; i++) {
       for (int k = 0; k < 2; k++)
         if (c->ev_loaded[i][k]) cudaEventDestroy(c->ev_loaded[i][k]);
       if (c->ev_free[i]) cudaEventDestroy(c->ev_free[i]);
@@ -681,38 +684,50 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
   Buf bss = classify(ss, n * 32, c->device), bct = classify(ct, n * P.ct_bytes, c->device),
       bsk = classify(sk, n * P.sk_bytes, c->device);
   if ((bct.host || bsk.host) && c->host_chunk && n > c->host_chunk) {
-    // host inputs: chunks whose copies overlap the previous chunk's kernels
+    // host inputs: chunk k's copies (two copy streams, three input slots)
+    // overlap the kernels of chunks k-1 and k-2, and chunk k's chain runs on
+    // lane k mod 2 (the caller's stream or a context lane, each with its own
+    // scratch), so consecutive chunks' chains overlap too
+    constexpr int NL = 2, NS = tmvp_ctx::kSlots;
     const size_t cn = c->host_chunk;
     const size_t inb = up(cn * P.ct_bytes) + up(cn * P.sk_bytes);
-    size_t need = dec_ws_bytes(P, cn) + 2 * inb + (bss.host ? up(cn * 32) : 0);
+    size_t need = NL * dec_ws_bytes(P, cn) + NS * inb + (bss.host ? NL * up(cn * 32) : 0);
     if ((r = ensure_ws(c, need))) return set_err(r);
     Arena A{c->ws};
-    DecScratch w = dec_scratch(P, cn, A);
-    uint8_t *slot_in[2] = {A.take(inb), A.take(inb)};
-    uint8_t *ss_stage = bss.host ? A.take(cn * 32) : nullptr;
+    DecScratch w[NL];
+    uint8_t *slot_in[NS], *ss_stage[NL] = {};
+    for (int l = 0; l < NL; l++) w[l] = dec_scratch(P, cn, A);
+    for (int k = 0; k < NS; k++) slot_in[k] = A.take(inb);
+    if (bss.host)
+      for (int l = 0; l < NL; l++) ss_stage[l] = A.take(cn * 32);
+    TRY_CUDA(cudaEventRecord(c->fork_ev, s));
+    TRY_CUDA(cudaStreamWaitEvent(c->lane[0], c->fork_ev, 0));
     for (size_t off = 0, k = 0; off < n; off += cn, k++) {
       const size_t m = std::min(cn, n - off);
-      const int sl = (int)(k & 1);
+      const int sl = (int)(k % NS), ln = (int)(k % NL);
+      cudaStream_t ls = ln == 0 ? s : c->lane[0];
       uint8_t *ct_k = bct.host ? slot_in[sl] : bct.dev + off * P.ct_bytes;
       uint8_t *sk_k = bsk.host ? slot_in[sl] + up(cn * P.ct_bytes) : bsk.dev + off * P.sk_bytes;
-      // the copies of chunk k wait until chunk k-2's kernels have read this
+      // the copies of chunk k wait until chunk k-3's kernels have read this
       // slot; ct and sk go on two copy streams (two copy engines)
       for (int q = 0; q < 2; q++) {
-        if (k >= 2) TRY_CUDA(cudaStreamWaitEvent(c->copy[q], c->ev_free[sl], 0));
+        if (k >= (size_t)NS) TRY_CUDA(cudaStreamWaitEvent(c->copy[q], c->ev_free[sl], 0));
         const Buf &b = q == 0 ? bct : bsk;
         const size_t rec = q == 0 ? P.ct_bytes : P.sk_bytes;
         if (b.host)
           TRY_CUDA(cudaMemcpyAsync(q == 0 ? ct_k : sk_k, (const uint8_t *)b.user + off * rec, m * rec,
                                    cudaMemcpyDefault, c->copy[q]));
         TRY_CUDA(cudaEventRecord(c->ev_loaded[sl][q], c->copy[q]));
-        TRY_CUDA(cudaStreamWaitEvent(s, c->ev_loaded[sl][q], 0));
+        TRY_CUDA(cudaStreamWaitEvent(ls, c->ev_loaded[sl][q], 0));
       }
-      uint8_t *ss_k = bss.host ? ss_stage : bss.dev + off * 32;
-      if ((r = dec_pipeline(c, P, m, ss_k, ct_k, sk_k, form, s, w))) return set_err(r);
-      TRY_CUDA(cudaEventRecord(c->ev_free[sl], s));
+      uint8_t *ss_k = bss.host ? ss_stage[ln] : bss.dev + off * 32;
+      if ((r = dec_pipeline(c, P, m, ss_k, ct_k, sk_k, form, ls, w[ln]))) return set_err(r);
+      TRY_CUDA(cudaEventRecord(c->ev_free[sl], ls));
       if (bss.host)
-        TRY_CUDA(cudaMemcpyAsync((uint8_t *)bss.user + off * 32, ss_stage, m * 32, cudaMemcpyDefault, s));
+        TRY_CUDA(cudaMemcpyAsync((uint8_t *)bss.user + off * 32, ss_k, m * 32, cudaMemcpyDefault, ls));
     }
+    TRY_CUDA(cudaEventRecord(c->lane_ev[0], c->lane[0]));
+    TRY_CUDA(cudaStreamWaitEvent(s, c->lane_ev[0], 0));
     return set_err(finish(c, s, bss.host));
   }
   size_t need = dec_ws_bytes(P, n) + stage_bytes(bss) + stage_bytes(bct) + stage_bytes(bsk);
