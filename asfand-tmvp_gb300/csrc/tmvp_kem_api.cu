@@ -59,12 +59,13 @@ struct tmvp_ctx {
   cudaStream_t side = nullptr;          // GenMatrix and H(c) beside the decryption (highest priority)
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   size_t host_chunk = 16384;                       // chunk of host-input decapsulation (0: none)
-  size_t dev_chunk = 0;                            // chunk of device-input decapsulation (0: none)
-  static constexpr int kLanes = 3;                 // extra streams for chunk chains
+  size_t dev_chunk = 32768;                        // chunk of device-input decapsulation (0: none)
+  static constexpr int kLanes = 4;                 // streams for chunk chains
   cudaStream_t lane[kLanes] = {};
+  cudaStream_t lane_side[kLanes] = {};             // the Keccak front of each lane (highest priority)
   cudaEvent_t lane_ev[kLanes] = {};
   cudaStream_t copy[2] = {};                       // host-to-device copies of chunked calls
-  static constexpr int kSlots = 3;                 // input slots of chunked host calls
+  static constexpr int kSlots = 5;                 // input slots of chunked host calls
   cudaEvent_t ev_loaded[kSlots][2] = {}, ev_free[kSlots] = {};  // per input slot (and copy stream)
   std::mutex mu;
   // optional per-stage timing: CUDA events recorded on the launching stream
@@ -320,17 +321,19 @@ DecScratch dec_scratch(const KemParams &P, size_t n, Arena &A) {
 // on the high-priority side stream, concurrent with the decryption and G on
 // s; the re-encryption and the final key wait for it.
 int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const uint8_t *ct,
-                 const uint8_t *sk, int form, cudaStream_t s, const DecScratch &w, bool fork = true) {
+                 const uint8_t *sk, int form, cudaStream_t s, const DecScratch &w, bool fork = true,
+                 cudaStream_t side = nullptr) {
   int r;
+  if (!side) side = c->side;
   if (fork) {
     TRY_CUDA(cudaEventRecord(c->fork_ev, s));
-    TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+    TRY_CUDA(cudaStreamWaitEvent(side, c->fork_ev, 0));
   }
   {
-    StageTimer tm_(c, "dec_front", c->side);
-    k_dec_front<<<blocks_for(2 * n, kHashBlock), kHashBlock, 0, c->side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 0);
+    StageTimer tm_(c, "dec_front", side);
+    k_dec_front<<<blocks_for(2 * n, kHashBlock), kHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 0);
   }
-  TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
+  TRY_CUDA(cudaEventRecord(c->join_ev, side));
   c->launches++;
   CpaArgs a{};
   a.P = P;
@@ -380,25 +383,22 @@ DecScratch dec_slice(const KemParams &P, const DecScratch &w, size_t off) {
 }
 
 // Decapsulation of n device-resident instances in chunks of cn: the chain of
-// chunk k (decryption, G, re-encryption, final key) runs on lane k mod 4 (the
-// caller's stream or one of the context's lane streams), while GenMatrix and
-// H(c) of all chunks run in order on the two side streams.  Chunk k's
-// re-encryption so overlaps GenMatrix and the decryption of chunk k + 1
-// instead of running after the whole batch's Keccak work.  w covers all n.
+// chunk k (decryption, G, re-encryption, final key) runs on the context's
+// lane k mod 4 and its Keccak front on that lane's high-priority side stream,
+// so one chunk's re-encryption overlaps the next chunk's Keccak work and
+// decryption.  w covers all n.
 int dec_lanes(tmvp_ctx *c, const KemParams &P, size_t n, size_t cn, uint8_t *ss, const uint8_t *ct,
               const uint8_t *sk, int form, cudaStream_t s, const DecScratch &w) {
   int r;
   const size_t chunks = (n + cn - 1) / cn;
-  const int extra = (int)std::min<size_t>(tmvp_ctx::kLanes, chunks - 1);
+  const int extra = (int)std::min<size_t>(tmvp_ctx::kLanes, chunks);
   TRY_CUDA(cudaEventRecord(c->fork_ev, s));
-  TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
   for (int i = 0; i < extra; i++) TRY_CUDA(cudaStreamWaitEvent(c->lane[i], c->fork_ev, 0));
   for (size_t off = 0, k = 0; off < n; off += cn, k++) {
     const size_t m = std::min(cn, n - off);
-    const int li = (int)(k % (tmvp_ctx::kLanes + 1));
-    cudaStream_t ls = li == 0 ? s : c->lane[li - 1];
-    if ((r = dec_pipeline(c, P, m, ss + off * 32, ct + off * P.ct_bytes, sk + off * P.sk_bytes, form, ls,
-                          dec_slice(P, w, off), false)))
+    const int li = (int)(k % tmvp_ctx::kLanes);
+    if ((r = dec_pipeline(c, P, m, ss + off * 32, ct + off * P.ct_bytes, sk + off * P.sk_bytes, form, c->lane[li],
+                          dec_slice(P, w, off), true, c->lane_side[li])))
       return r;
   }
   for (int i = 0; i < extra; i++) {
@@ -483,8 +483,13 @@ int tmvp_ctx_create(int device, size_t mem_budget, tmvp_ctx **out) {
       delete c;
       return set_err(TMVP_EDEVICE);
     }
+  // chunk k runs on lane k mod 4: its Keccak front at the highest priority,
+  // its chain at the lowest (measured: falling priorities per lane, which
+  // favour earlier chunks, were slower on device batches and no faster on
+  // host batches)
   for (int i = 0; i < tmvp_ctx::kLanes; i++)
     if (cudaStreamCreateWithPriority(&c->lane[i], cudaStreamNonBlocking, pri_low) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&c->lane_side[i], cudaStreamNonBlocking, pri_high) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->lane_ev[i], cudaEventDisableTiming) != cudaSuccess) {
     delete c;
     return set_err(TMVP_EDEVICE);
@@ -507,6 +512,7 @@ void tmvp_ctx_destroy(tmvp_ctx *c) {
     if (c->join_ev) cudaEventDestroy(c->join_ev);
     for (int i = 0; i < tmvp_ctx::kLanes; i++) {
       if (c->lane[i]) cudaStreamDestroy(c->lane[i]);
+      if (c->lane_side[i]) cudaStreamDestroy(c->lane_side[i]);
       if (c->lane_ev[i]) cudaEventDestroy(c->lane_ev[i]);
     }
     for (int i = 0; i < 2; i++)
@@ -684,11 +690,11 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
   Buf bss = classify(ss, n * 32, c->device), bct = classify(ct, n * P.ct_bytes, c->device),
       bsk = classify(sk, n * P.sk_bytes, c->device);
   if ((bct.host || bsk.host) && c->host_chunk && n > c->host_chunk) {
-    // host inputs: chunk k's copies (two copy streams, three input slots)
-    // overlap the kernels of chunks k-1 and k-2, and chunk k's chain runs on
-    // lane k mod 2 (the caller's stream or a context lane, each with its own
-    // scratch), so consecutive chunks' chains overlap too
-    constexpr int NL = 2, NS = tmvp_ctx::kSlots;
+    // host inputs: chunk k's copies (one copy stream, five input slots) run
+    // ahead of the kernels, and chunk k's chain runs on lane k mod 4 (as in
+    // dec_lanes, each lane with its own scratch and Keccak-front stream), so
+    // consecutive chunks' chains overlap
+    constexpr int NL = tmvp_ctx::kLanes, NS = tmvp_ctx::kSlots;
     const size_t cn = c->host_chunk;
     const size_t inb = up(cn * P.ct_bytes) + up(cn * P.sk_bytes);
     size_t need = NL * dec_ws_bytes(P, cn) + NS * inb + (bss.host ? NL * up(cn * 32) : 0);
@@ -701,33 +707,39 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
     if (bss.host)
       for (int l = 0; l < NL; l++) ss_stage[l] = A.take(cn * 32);
     TRY_CUDA(cudaEventRecord(c->fork_ev, s));
-    TRY_CUDA(cudaStreamWaitEvent(c->lane[0], c->fork_ev, 0));
-    for (size_t off = 0, k = 0; off < n; off += cn, k++) {
-      const size_t m = std::min(cn, n - off);
+    for (int l = 0; l < tmvp_ctx::kLanes; l++) TRY_CUDA(cudaStreamWaitEvent(c->lane[l], c->fork_ev, 0));
+    for (size_t off = 0, k = 0, m = 0; off < n; off += m, k++) {
+      m = std::min(cn, n - off);
       const int sl = (int)(k % NS), ln = (int)(k % NL);
-      cudaStream_t ls = ln == 0 ? s : c->lane[0];
+      cudaStream_t ls = c->lane[ln];
       uint8_t *ct_k = bct.host ? slot_in[sl] : bct.dev + off * P.ct_bytes;
       uint8_t *sk_k = bsk.host ? slot_in[sl] + up(cn * P.ct_bytes) : bsk.dev + off * P.sk_bytes;
-      // the copies of chunk k wait until chunk k-3's kernels have read this
-      // slot; ct and sk go on two copy streams (two copy engines)
+      // the copies of chunk k wait until chunk k-5's kernels have read this
+      // slot.  ct and sk of a chunk go back to back on one copy stream, in
+      // chunk order: the host link is the limit (~210 GB/s), so a second
+      // stream would only delay chunk k's last byte by sharing the link
+      // with chunk k+1's copies
+      if (k >= (size_t)NS) TRY_CUDA(cudaStreamWaitEvent(c->copy[0], c->ev_free[sl], 0));
       for (int q = 0; q < 2; q++) {
-        if (k >= (size_t)NS) TRY_CUDA(cudaStreamWaitEvent(c->copy[q], c->ev_free[sl], 0));
         const Buf &b = q == 0 ? bct : bsk;
         const size_t rec = q == 0 ? P.ct_bytes : P.sk_bytes;
         if (b.host)
           TRY_CUDA(cudaMemcpyAsync(q == 0 ? ct_k : sk_k, (const uint8_t *)b.user + off * rec, m * rec,
-                                   cudaMemcpyDefault, c->copy[q]));
-        TRY_CUDA(cudaEventRecord(c->ev_loaded[sl][q], c->copy[q]));
-        TRY_CUDA(cudaStreamWaitEvent(ls, c->ev_loaded[sl][q], 0));
+                                   cudaMemcpyDefault, c->copy[0]));
       }
+      TRY_CUDA(cudaEventRecord(c->ev_loaded[sl][0], c->copy[0]));
+      TRY_CUDA(cudaStreamWaitEvent(ls, c->ev_loaded[sl][0], 0));
       uint8_t *ss_k = bss.host ? ss_stage[ln] : bss.dev + off * 32;
-      if ((r = dec_pipeline(c, P, m, ss_k, ct_k, sk_k, form, ls, w[ln]))) return set_err(r);
+      if ((r = dec_pipeline(c, P, m, ss_k, ct_k, sk_k, form, ls, w[ln], true, c->lane_side[ln])))
+        return set_err(r);
       TRY_CUDA(cudaEventRecord(c->ev_free[sl], ls));
       if (bss.host)
         TRY_CUDA(cudaMemcpyAsync((uint8_t *)bss.user + off * 32, ss_k, m * 32, cudaMemcpyDefault, ls));
     }
-    TRY_CUDA(cudaEventRecord(c->lane_ev[0], c->lane[0]));
-    TRY_CUDA(cudaStreamWaitEvent(s, c->lane_ev[0], 0));
+    for (int l = 0; l < tmvp_ctx::kLanes; l++) {
+      TRY_CUDA(cudaEventRecord(c->lane_ev[l], c->lane[l]));
+      TRY_CUDA(cudaStreamWaitEvent(s, c->lane_ev[l], 0));
+    }
     return set_err(finish(c, s, bss.host));
   }
   size_t need = dec_ws_bytes(P, n) + stage_bytes(bss) + stage_bytes(bct) + stage_bytes(bsk);

@@ -156,10 +156,10 @@ int tmvp_ctx_reserve(tmvp_ctx *ctx, size_t bytes);
 int tmvp_ctx_set_host_chunk(tmvp_ctx *ctx, size_t n);
 /* Batched decapsulation with device-resident buffers splits batches larger
  * than n into chunks whose decryption / G / re-encryption / final-key chains
- * run on up to four streams (the caller's and three of the context's), so
+ * run on four of the context's streams (joined back into the caller's), so
  * that one chunk's re-encryption overlaps the next chunk's GenMatrix and
- * decryption; 0 = one chain over the whole batch.  Default 0; n must be 0
- * or >= 1024.  Results do not depend on it. */
+ * decryption; 0 = one chain over the whole batch.  Default 32768; n must
+ * be 0 or >= 1024.  Results do not depend on it. */
 int tmvp_ctx_set_dev_chunk(tmvp_ctx *ctx, size_t n);
 
 /* ---------------------------------------------------------------------------

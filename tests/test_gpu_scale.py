@@ -133,6 +133,6 @@ def test_chunked_device_decapsulation(kem, chunk):
         ctx.kem_dec_ptr(T.SABER, n, out, ct, sk)
         torch.cuda.synchronize()
     finally:
-        ctx.set_dev_chunk(0)
+        ctx.set_dev_chunk(32768)
     assert torch.equal(out[:n - 5], ss[:n - 5]) and torch.equal(out[n - 4:], ss[n - 4:])
     assert not torch.equal(out[n - 5], ss[n - 5])
