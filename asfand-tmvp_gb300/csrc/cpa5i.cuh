@@ -43,7 +43,7 @@ template <int OP, int SET>
 struct ShapeC {
   using C = SetC<SET>;
   static constexpr int L = C::L;
-  static constexpr int R = OP == kDecrypt ? 1 : (OP == kKeygen ? L : L + 1);
+  static constexpr int R = OP == kDecrypt ? 1 : (OP == kKeygen || OP == kMatvec ? L : L + 1);
   static constexpr int RA = OP == kDecrypt ? 0 : L;
   static constexpr int WA = C::EQ, WB = C::EP;
   static constexpr int DA = r16_digits(WA), DB = r16_digits(WB);
@@ -86,6 +86,9 @@ struct LayoutC {
   static constexpr bool HAS_B = OP == kEncrypt || OP == kReenc;
   static constexpr bool HAS_CT = OP == kReenc || OP == kDecrypt;
   static constexpr bool HAS_SK = OP == kDecrypt;
+  // matvec: A as 16-bit coefficients (l x l x 512 bytes) inside H, int8 secrets after it
+  static constexpr bool HAS_MV = OP == kMatvec;
+  static constexpr int MV_A = C::L * C::L * 512, MV_S = C::L * 256;
   static constexpr int G = S::G;
   static constexpr int LB = 2 * G * 128 + 16;  // second K chunk of a block
   static constexpr int RB = 2 * LB;            // one block
@@ -97,7 +100,7 @@ struct LayoutC {
   static constexpr int ENG = 0;
   static constexpr int H = ENG;
   static constexpr int A = H;                                    // streams inside H
-  static constexpr int SS = HAS_AS ? al16c(A + C::GM + 16) : A;
+  static constexpr int SS = HAS_AS ? al16c(A + C::GM + 16) : (HAS_MV ? al16c(A + MV_A) : A);
   static constexpr int B = HAS_AS ? al16c(SS + C::GS + 16) : SS;
   static constexpr int SKO = H;
   static constexpr int BM = H + C::L * kHankelBytes5;
@@ -113,9 +116,10 @@ struct LayoutC {
   static constexpr int BAR = al16c(OUT + OUT_BYTES);  // mbarriers in, mma; TMEM base
   static constexpr int TOTAL = BAR + 32;
   static constexpr int IN_BYTES = (HAS_AS ? C::GM + C::GS : 0) + (HAS_B ? C::L * C::POLYCOMP + 32 : 0) +
-                                  (HAS_CT ? C::CT : 0) + (HAS_SK ? C::INDCPA_SK : 0);
+                                  (HAS_CT ? C::CT : 0) + (HAS_SK ? C::INDCPA_SK : 0) + (HAS_MV ? MV_A + MV_S : 0);
   static_assert(!HAS_AS || B + (HAS_B ? C::L * C::POLYCOMP + 16 : 0) <= BM, "streams fit inside H");
   static_assert(!HAS_SK || C::INDCPA_SK + 16 <= C::L * kHankelBytes5, "secret key fits inside H");
+  static_assert(!HAS_MV || SS + MV_S + 16 <= BM, "matvec inputs fit inside H");
 };
 
 // Eight W-bit little-endian fields from byte `byte0` (16 bytes of slack after
@@ -207,6 +211,10 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
     }
     if (LO::HAS_CT) bulk_g2s(d + LO::CTO, a.ct + (size_t)inst * C::CT, C::CT, mbar_in);
     if (LO::HAS_SK) bulk_g2s(d + LO::SKO, a.sk + (size_t)inst * C::SK, C::INDCPA_SK, mbar_in);
+    if (LO::HAS_MV) {
+      bulk_g2s(d + LO::A, reinterpret_cast<const uint8_t *>(a.mv_A) + (size_t)inst * LO::MV_A, LO::MV_A, mbar_in);
+      bulk_g2s(d + LO::SS, reinterpret_cast<const uint8_t *>(a.mv_s) + (size_t)inst * LO::MV_S, LO::MV_S, mbar_in);
+    }
   }
   tc_fence_before();
   __syncthreads();
@@ -247,7 +255,9 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
 #pragma unroll
         for (int h = 0; h < 2; h++) {
           const int w = 64 * j + 2 * g + h;
-          if (OP == kDecrypt) {
+          if (OP == kMatvec) {
+            sb[h] = lds32(smem_u32(sm + LO::SS) + 4 * w);  // four int8 coefficients
+          } else if (OP == kDecrypt) {
             // 2-bit two's complement (SABLE pack.cu:371-376): one byte = 4 coefficients
             const uint32_t x = sm[LO::SKO + w];
             const uint32_t spread = (x & 3u) | ((x & 0xcu) << 6) | ((x & 0x30u) << 12) | ((x & 0xc0u) << 18);
@@ -309,7 +319,27 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
         sts64(bl + j * LO::BJ + (n >> 3) * 128 + (n & 7) * 16, v.x, v.y);
       }
     };
-    if constexpr (S::R == 1) {
+    if constexpr (OP == kMatvec) {
+      // coefficients already in 16-bit lanes: digit d of the low 13 bits
+      // (the result is needed mod 2^eq, eq <= 13)
+      if (warp < L) {
+        const int p = warp;
+#pragma unroll
+        for (int j = 0; j < L; j++) {
+          const int ij = a.mv_transpose ? (j * L + p) : (p * L + j);
+          const uint32_t src = smem_u32(sm + LO::A) + (uint32_t)(512 * ij + 16 * lane);
+          uint32_t X[4];
+#pragma unroll
+          for (int i = 0; i < 4; i++) X[i] = lds32(src + 4 * i);
+#pragma unroll
+          for (int d = 0; d < S::DA; d++) {
+            const uint2 v = raw_digits8<S::WA>(X, d);
+            const int n = p * S::DA + d;
+            sts64(bl + j * LO::BJ + (n >> 3) * 128 + (n & 7) * 16, v.x, v.y);
+          }
+        }
+      }
+    } else if constexpr (S::R == 1) {
       if (warp < L) item(std::integral_constant<int, S::WB>{}, LO::CTO + 32 * warp * S::WB, 0, warp);
     } else if (warp < S::RA) {
       const int p = warp;
@@ -366,7 +396,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
   const int q4 = warp & 3, hsel = warp >> 2;
   const int k = 128 * hsel + 32 * q4 + lane;
   constexpr int G8 = 8 * LO::G;
-  constexpr bool FUSED = OP == kDecrypt || OP == kReenc;
+  constexpr bool FUSED = OP == kDecrypt || OP == kReenc || OP == kMatvec;
   float xacc[G8];  // digit column c of coefficient k, times 2^-9 (exact)
   if (done) {
     const uint32_t t0 = tmem + ((uint32_t)(32 * q4) << 16);
@@ -490,6 +520,12 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
     }
     const int any = __syncthreads_or(diff != 0u);
     if (tid == 0) a.fail[inst] = (uint8_t)(any != 0);
+  } else if constexpr (OP == kMatvec) {
+    // coefficient k of every output polynomial, mod 2^eq
+    const uint32_t m = (1u << a.mv_eq) - 1u;
+    uint16_t *o = a.mv_out + (size_t)inst * (L * 256) + k;
+#pragma unroll
+    for (int p = 0; p < L; p++) o[256 * p] = (uint16_t)(combine1(S::col_base(p), S::DA) & m);
   } else if (OP == kEncrypt) {
     const uint8_t *msg = sm + LO::MSG;
     for (int idx = tid; idx < S::R * 32; idx += NT) {
