@@ -95,6 +95,18 @@ __global__ void __launch_bounds__(128) k_dec_g(KemParams P, const uint8_t *mbuf,
   if (t < (size_t)n) dec_g_one(P, mbuf, kr, s_stream, t);
 }
 
+// GenMatrix stream of public key t (seed_A at the end of pk + t * pk_stride),
+// for callers that keep one expanded A per key (GenMatrix, saber_enc
+// cuda_kernel.cu:116-127).
+__global__ void __launch_bounds__(128) k_genmatrix(KemParams P, const uint8_t *pk, size_t pk_stride,
+                                                    uint8_t *a_stream, int n) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)n) return;
+  uint64_t seed[4];
+  load_words(seed, pk + t * pk_stride + (size_t)P.l * P.polycompbytes, 4);
+  shake128_32(reinterpret_cast<uint64_t *>(a_stream + t * P.gm_bytes), P.gm_bytes, seed);
+}
+
 // GenMatrix of instance t from the seed of the pk embedded in sk.
 __device__ __forceinline__ void dec_genmatrix_one(const KemParams &P, const uint8_t *sk, uint8_t *a_stream,
                                                   size_t t) {

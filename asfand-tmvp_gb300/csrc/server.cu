@@ -38,7 +38,7 @@ using Clock = std::chrono::steady_clock;
 using tmvp::KemParams;
 
 constexpr int kSets = 6;
-constexpr int kMaxCt = 1472, kMaxSk = 3040, kMaxPk = 1312;
+constexpr int kMaxCt = 1472, kMaxSk = 3040, kMaxPk = 1312, kMaxGm = 16 * 416;
 
 __global__ void k_gather16(const uint8_t *table, int stride, const uint32_t *idx, uint8_t *out,
                            int n) {
@@ -65,7 +65,7 @@ struct Slot {
   cudaEvent_t ev = nullptr;
   uint8_t *h_in = nullptr, *h_out = nullptr;
   uint32_t *h_idx = nullptr;
-  uint8_t *d_in = nullptr, *d_out = nullptr, *d_key = nullptr;
+  uint8_t *d_in = nullptr, *d_out = nullptr, *d_key = nullptr, *d_a = nullptr;
   uint32_t *d_idx = nullptr;
   std::vector<Req> batch;
   int set = 0, op = 0, err = 0;
@@ -76,6 +76,7 @@ struct Slot {
 
 struct KeyTable {
   uint8_t *pk = nullptr, *sk = nullptr;  // device
+  uint8_t *a = nullptr;                  // device: each key's GenMatrix stream (expanded once)
   size_t n = 0, cap = 0;
   std::vector<uint8_t> h_pk;             // host copy (for the load generator)
 };
@@ -115,6 +116,7 @@ void free_slot(Slot &s) {
   if (s.d_in) cudaFree(s.d_in);
   if (s.d_out) cudaFree(s.d_out);
   if (s.d_key) cudaFree(s.d_key);
+  if (s.d_a) cudaFree(s.d_a);
   if (s.d_idx) cudaFree(s.d_idx);
   s = Slot();
 }
@@ -122,6 +124,7 @@ void free_slot(Slot &s) {
 // Device bytes one slot holds for max_batch requests of the largest set.
 size_t slot_bytes(int mb) {
   size_t per = (size_t)kMaxCt + (kMaxCt + 32) + kMaxSk + 4 +  // in, out, keys, idx
+               kMaxGm +                                       // the batch's expanded matrices
                16 * 416 + 768 + 64 + 64 + 1 + 32;             // KEM workspace (FireSaber)
   return per * (size_t)mb + 64 * 256;
 }
@@ -138,7 +141,8 @@ int alloc_slot(Slot &s, int device, int mb) {
       cudaMalloc(&s.d_in, (size_t)mb * kMaxCt) != cudaSuccess ||
       cudaMalloc(&s.d_out, (size_t)mb * (kMaxCt + 32)) != cudaSuccess ||
       cudaMalloc(&s.d_key, (size_t)mb * kMaxSk) != cudaSuccess ||
-      cudaMalloc(&s.d_idx, (size_t)mb * 4) != cudaSuccess)
+      cudaMalloc(&s.d_idx, (size_t)mb * 4) != cudaSuccess ||
+      cudaMalloc(&s.d_a, (size_t)mb * kMaxGm) != cudaSuccess)
     return TMVP_ENOMEM;
   s.batch.reserve(mb);
   return TMVP_OK;
@@ -162,14 +166,18 @@ void launch_batch(tmvp_server *S, Slot &s) {
   size_t words = (size_t)n * (kb >> 4);
   k_gather16<<<(unsigned)((words + 255) / 256), 256, 0, s.st>>>(
       s.op == TMVP_OP_DECAPS ? K.sk : K.pk, kb, s.d_idx, s.d_key, n);
+  // each key's A was expanded when the key was added: gather it instead of
+  // running GenMatrix (23 of a Saber decapsulation's 39 Keccak-f) per request
+  const size_t awords = (size_t)n * (P.gm_bytes >> 4);
+  k_gather16<<<(unsigned)((awords + 255) / 256), 256, 0, s.st>>>(K.a, P.gm_bytes, s.d_idx, s.d_a, n);
   int rc;
   if (s.op == TMVP_OP_DECAPS) {
-    rc = tmvp_kem_dec_batch(s.ctx, (tmvp_param_set)s.set, n, s.d_out, s.d_in, s.d_key,
-                            (tmvp_form)S->cfg.form, s.st);
+    rc = tmvp_kem_dec_batch_a(s.ctx, (tmvp_param_set)s.set, n, s.d_out, s.d_in, s.d_key, s.d_a,
+                              (tmvp_form)S->cfg.form, s.st);
   } else {
-    rc = tmvp_kem_enc_batch(s.ctx, (tmvp_param_set)s.set, n, s.d_out,
-                            s.d_out + (size_t)n * P.ct_bytes, s.d_key, s.d_in,
-                            (tmvp_form)S->cfg.form, s.st);
+    rc = tmvp_kem_enc_batch_a(s.ctx, (tmvp_param_set)s.set, n, s.d_out,
+                              s.d_out + (size_t)n * P.ct_bytes, s.d_key, s.d_in, s.d_a,
+                              (tmvp_form)S->cfg.form, s.st);
   }
   const int outb = s.op == TMVP_OP_DECAPS ? 32 : P.ct_bytes + 32;
   e |= cudaMemcpyAsync(s.h_out, s.d_out, (size_t)n * outb, cudaMemcpyDeviceToHost, s.st);
@@ -346,6 +354,7 @@ void tmvp_server_destroy(tmvp_server *S) {
   for (auto &k : S->keys) {
     if (k.pk) cudaFree(k.pk);
     if (k.sk) cudaFree(k.sk);
+    if (k.a) cudaFree(k.a);
   }
   cudaSetDevice(prev);
   delete S;
@@ -366,26 +375,38 @@ int tmvp_server_add_keys(tmvp_server *S, tmvp_param_set set, size_t n, const uin
   cudaSetDevice(S->device);
   if (K.n + n > K.cap) {
     size_t cap = std::max(K.n + n, K.cap * 2);
-    uint8_t *npk = nullptr, *nsk = nullptr;
-    if (cudaMalloc(&npk, cap * P.pk_bytes) != cudaSuccess ||
-        cudaMalloc(&nsk, cap * P.sk_bytes) != cudaSuccess) {
+    uint8_t *npk = nullptr, *nsk = nullptr, *na = nullptr;
+    if (cudaMalloc(&npk, cap * P.pk_bytes) != cudaSuccess || cudaMalloc(&nsk, cap * P.sk_bytes) != cudaSuccess ||
+        cudaMalloc(&na, cap * P.gm_bytes) != cudaSuccess) {
       if (npk) cudaFree(npk);
+      if (nsk) cudaFree(nsk);
       cudaSetDevice(prev);
       return TMVP_ENOMEM;
     }
     if (K.n) {
       cudaMemcpy(npk, K.pk, K.n * P.pk_bytes, cudaMemcpyDeviceToDevice);
       cudaMemcpy(nsk, K.sk, K.n * P.sk_bytes, cudaMemcpyDeviceToDevice);
+      cudaMemcpy(na, K.a, K.n * P.gm_bytes, cudaMemcpyDeviceToDevice);
       cudaFree(K.pk);
       cudaFree(K.sk);
+      cudaFree(K.a);
     }
     K.pk = npk;
     K.sk = nsk;
+    K.a = na;
     K.cap = cap;
   }
   int e = 0;
   e |= cudaMemcpy(K.pk + K.n * P.pk_bytes, pk, n * P.pk_bytes, cudaMemcpyDefault);
   e |= cudaMemcpy(K.sk + K.n * P.sk_bytes, sk, n * P.sk_bytes, cudaMemcpyDefault);
+  // expand each new key's A once (device pk rows -> GenMatrix streams)
+  if (!e) {
+    Slot &s0 = S->slots[0];
+    if (tmvp_genmatrix_batch(s0.ctx, set, n, K.a + K.n * P.gm_bytes, K.pk + K.n * P.pk_bytes, P.pk_bytes, s0.st) !=
+            TMVP_OK ||
+        cudaStreamSynchronize(s0.st) != cudaSuccess)
+      e = 1;
+  }
   K.h_pk.resize((K.n + n) * P.pk_bytes);
   cudaMemcpy(K.h_pk.data() + K.n * P.pk_bytes, pk, n * P.pk_bytes, cudaMemcpyDefault);
   for (size_t i = 0; i < n; i++) key_ids[i] = ((uint32_t)set << 29) | (uint32_t)(K.n + i);

@@ -322,14 +322,17 @@ DecScratch dec_scratch(const KemParams &P, size_t n, Arena &A) {
 // s; the re-encryption and the final key wait for it.
 int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const uint8_t *ct,
                  const uint8_t *sk, int form, cudaStream_t s, const DecScratch &w, bool fork = true,
-                 cudaStream_t side = nullptr) {
+                 cudaStream_t side = nullptr, const uint8_t *a_cached = nullptr) {
   int r;
   if (!side) side = c->side;
   if (fork) {
     TRY_CUDA(cudaEventRecord(c->fork_ev, s));
     TRY_CUDA(cudaStreamWaitEvent(side, c->fork_ev, 0));
   }
-  {
+  if (a_cached) {  // GenMatrix given: the front is H(c) alone
+    StageTimer tm_(c, "dec_front", side);
+    k_dec_front<<<blocks_for(n, kHashBlock), kHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
+  } else {
     StageTimer tm_(c, "dec_front", side);
     k_dec_front<<<blocks_for(2 * n, kHashBlock), kHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 0);
   }
@@ -353,7 +356,7 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   CpaArgs b{};
   b.P = P;
   b.n = (int)n;
-  b.a_stream = w.a_stream;
+  b.a_stream = a_cached ? a_cached : w.a_stream;
   b.s_stream = w.s_stream;
   b.pk = sk;
   b.pk_stride = P.sk_bytes;
@@ -627,8 +630,13 @@ int tmvp_kem_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *p
   return set_err(finish(c, s, bpk.host || bsk.host));
 }
 
-int tmvp_kem_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, uint8_t *ss,
-                       const uint8_t *pk, const uint8_t *coins, tmvp_form form, void *stream) {
+}  // extern "C"
+
+namespace {
+// Encapsulation of n instances; a_cached (device, [n][gm_bytes]) replaces
+// the GenMatrix half of the front when given.
+int enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, uint8_t *ss, const uint8_t *pk,
+              const uint8_t *coins, const uint8_t *a_cached, tmvp_form form, void *stream) {
   KemParams P;
   int r = check_common(c, set, n, form, &P);
   if (r) return set_err(r);
@@ -639,11 +647,12 @@ int tmvp_kem_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, u
   cudaStream_t s = (cudaStream_t)stream;
   Buf bct = classify(ct, n * P.ct_bytes, c->device), bss = classify(ss, n * 32, c->device),
       bpk = classify(pk, n * P.pk_bytes, c->device), bco = classify(coins, n * 32, c->device);
-  size_t need = up(n * P.gm_bytes) + up(n * P.gs_bytes) + 2 * up(n * 64) + stage_bytes(bct) +
+  size_t need = (a_cached ? 0 : up(n * P.gm_bytes)) + up(n * P.gs_bytes) + 2 * up(n * 64) + stage_bytes(bct) +
                 stage_bytes(bss) + stage_bytes(bpk) + stage_bytes(bco);
   if ((r = ensure_ws(c, need))) return set_err(r);
   Arena A{c->ws};
-  uint8_t *a_stream = A.take(n * P.gm_bytes), *s_stream = A.take(n * P.gs_bytes);
+  uint8_t *a_stream = a_cached ? const_cast<uint8_t *>(a_cached) : A.take(n * P.gm_bytes);
+  uint8_t *s_stream = A.take(n * P.gs_bytes);
   uint8_t *mbuf = A.take(n * 64), *kr = A.take(n * 64);
   stage_assign(bct, A);
   stage_assign(bss, A);
@@ -652,8 +661,9 @@ int tmvp_kem_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, u
   if ((r = upload(bpk, s)) || (r = upload(bco, s))) return set_err(r);
   {
     StageTimer tm_(c, "enc_front", s);
-    k_enc_front<<<blocks_for(2 * n, kHashBlock), kHashBlock, 0, s>>>(P, bpk.dev, bco.dev, mbuf, kr, s_stream,
-                                                       a_stream, (int)n);
+    // threads n..2n-1 expand GenMatrix, unless it is given
+    k_enc_front<<<blocks_for((a_cached ? 1 : 2) * n, kHashBlock), kHashBlock, 0, s>>>(P, bpk.dev, bco.dev, mbuf,
+                                                                                      kr, s_stream, a_stream, (int)n);
   }
   c->launches++;
   CpaArgs a{};
@@ -675,6 +685,71 @@ int tmvp_kem_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, u
   c->launches++;
   if ((r = download(bct, s)) || (r = download(bss, s))) return set_err(r);
   return set_err(finish(c, s, bct.host || bss.host));
+}
+}  // namespace
+
+extern "C" {
+
+int tmvp_kem_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, uint8_t *ss,
+                       const uint8_t *pk, const uint8_t *coins, tmvp_form form, void *stream) {
+  return enc_batch(c, set, n, ct, ss, pk, coins, nullptr, form, stream);
+}
+
+size_t tmvp_genmatrix_bytes(tmvp_param_set set) {
+  KemParams P;
+  return make_params(set, &P) ? (size_t)P.gm_bytes : 0;
+}
+
+int tmvp_genmatrix_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *a_stream, const uint8_t *pk,
+                         size_t pk_stride, void *stream) {
+  KemParams P;
+  if (!c || !make_params(set, &P) || n > (size_t)INT_MAX) return set_err(TMVP_EINVAL);
+  if (n == 0) return set_err(TMVP_OK);
+  if (!a_stream || !pk || pk_stride < (size_t)P.pk_bytes) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  if (classify(a_stream, n * P.gm_bytes, c->device).host || classify(pk, n * pk_stride, c->device).host)
+    return set_err(TMVP_EINVAL);  // device buffers only
+  cudaStream_t s = (cudaStream_t)stream;
+  k_genmatrix<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, pk, pk_stride, a_stream, (int)n);
+  c->launches++;
+  return set_err(finish(c, s, false));
+}
+
+int tmvp_kem_enc_batch_a(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, uint8_t *ss,
+                         const uint8_t *pk, const uint8_t *coins, const uint8_t *a_stream, tmvp_form form,
+                         void *stream) {
+  KemParams P;
+  if (!c || !make_params(set, &P) || !a_stream) return set_err(TMVP_EINVAL);
+  if (n && classify(a_stream, n * P.gm_bytes, c->device).host) return set_err(TMVP_EINVAL);
+  return enc_batch(c, set, n, ct, ss, pk, coins, a_stream, form, stream);
+}
+
+int tmvp_kem_dec_batch_a(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, const uint8_t *ct,
+                         const uint8_t *sk, const uint8_t *a_stream, tmvp_form form, void *stream) {
+  KemParams P;
+  int r = check_common(c, set, n, form, &P);
+  if (r) return set_err(r);
+  if (n == 0) return set_err(TMVP_OK);
+  if (!ss || !ct || !sk || !a_stream) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  cudaStream_t s = (cudaStream_t)stream;
+  Buf bss = classify(ss, n * 32, c->device), bct = classify(ct, n * P.ct_bytes, c->device),
+      bsk = classify(sk, n * P.sk_bytes, c->device), ba = classify(a_stream, n * P.gm_bytes, c->device);
+  if (ba.host) return set_err(TMVP_EINVAL);  // the expanded matrices stay on the device
+  size_t need = dec_ws_bytes(P, n) + stage_bytes(bss) + stage_bytes(bct) + stage_bytes(bsk);
+  if ((r = ensure_ws(c, need))) return set_err(r);
+  Arena A{c->ws};
+  DecScratch w = dec_scratch(P, n, A);
+  stage_assign(bss, A);
+  stage_assign(bct, A);
+  stage_assign(bsk, A);
+  if ((r = upload(bct, s)) || (r = upload(bsk, s))) return set_err(r);
+  if ((r = dec_pipeline(c, P, n, bss.dev, bct.dev, bsk.dev, form, s, w, true, nullptr, a_stream)))
+    return set_err(r);
+  if ((r = download(bss, s))) return set_err(r);
+  return set_err(finish(c, s, bss.host));
 }
 
 int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, const uint8_t *ct,

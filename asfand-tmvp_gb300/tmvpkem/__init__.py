@@ -88,6 +88,11 @@ def lib(build_if_missing: bool = False):
     L.tmvp_kem_keypair_batch.argtypes = [P, I, S, P, P, P, I, P]
     L.tmvp_kem_enc_batch.argtypes = [P, I, S, P, P, P, P, I, P]
     L.tmvp_kem_dec_batch.argtypes = [P, I, S, P, P, P, I, P]
+    L.tmvp_genmatrix_bytes.argtypes = [I]
+    L.tmvp_genmatrix_bytes.restype = S
+    L.tmvp_genmatrix_batch.argtypes = [P, I, S, P, P, S, P]
+    L.tmvp_kem_enc_batch_a.argtypes = [P, I, S, P, P, P, P, P, I, P]
+    L.tmvp_kem_dec_batch_a.argtypes = [P, I, S, P, P, P, P, I, P]
     L.tmvp_indcpa_keypair_batch.argtypes = [P, I, S, P, P, P, I, P]
     L.tmvp_indcpa_enc_batch.argtypes = [P, I, S, P, P, P, P, I, P]
     L.tmvp_indcpa_dec_batch.argtypes = [P, I, S, P, P, P, I, P]
@@ -206,6 +211,11 @@ class ServerStats(ctypes.Structure):
 OP_ENCAPS, OP_DECAPS = 0, 1
 
 
+def genmatrix_bytes(set_id: int) -> int:
+    """Bytes of one key's GenMatrix stream (tmvp_genmatrix_bytes)."""
+    return int(lib().tmvp_genmatrix_bytes(set_id))
+
+
 def sizes(set_id: int) -> Sizes:
     s = Sizes()
     rc = lib().tmvp_param_sizes(set_id, ctypes.byref(s))
@@ -301,6 +311,20 @@ class Context:
     def kem_dec_ptr(self, set_id, n, ss, ct, sk, form=FORM_AUTO, stream=None):
         _check(lib().tmvp_kem_dec_batch(self.h, set_id, n, _ptr(ss), _ptr(ct), _ptr(sk), form,
                                         stream), "tmvp_kem_dec_batch")
+
+    def genmatrix_ptr(self, set_id, n, a_stream, pk, pk_stride=None, stream=None):
+        """a_stream[i] = SHAKE-128(seed_A of pk row i): each key's expanded A (device buffers)."""
+        stride = sizes(set_id).pk_bytes if pk_stride is None else pk_stride
+        _check(lib().tmvp_genmatrix_batch(self.h, set_id, n, _ptr(a_stream), _ptr(pk), stride, stream),
+               "tmvp_genmatrix_batch")
+
+    def kem_enc_a_ptr(self, set_id, n, ct, ss, pk, coins, a_stream, form=FORM_AUTO, stream=None):
+        _check(lib().tmvp_kem_enc_batch_a(self.h, set_id, n, _ptr(ct), _ptr(ss), _ptr(pk), _ptr(coins),
+                                          _ptr(a_stream), form, stream), "tmvp_kem_enc_batch_a")
+
+    def kem_dec_a_ptr(self, set_id, n, ss, ct, sk, a_stream, form=FORM_AUTO, stream=None):
+        _check(lib().tmvp_kem_dec_batch_a(self.h, set_id, n, _ptr(ss), _ptr(ct), _ptr(sk), _ptr(a_stream),
+                                          form, stream), "tmvp_kem_dec_batch_a")
 
     def matvec_ptr(self, n, l, eq, transpose, out, A, s, form=FORM_AUTO, stream=None):
         _check(lib().tmvp_matvec_batch(self.h, n, l, eq, int(transpose), _ptr(out), _ptr(A),

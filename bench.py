@@ -256,6 +256,19 @@ def run_ours(args):
         e2e_ms, e2e_exact, e2e_value, e2e_chunk = [float("nan")], True, None, (None, {})
     else:
         e2e_ms, e2e_exact, e2e_value, e2e_chunk = _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws)
+    # ---- the same decapsulations with each key's A expanded once beforehand (the
+    # serving loop's device-resident keys): GenMatrix leaves the per-call work
+    cached = None
+    if hasattr(ctx, "kem_dec_a_ptr") and not args.no_extra:
+        a_keys = torch.empty((n, T.genmatrix_bytes(SABER)), dtype=torch.uint8, device=dev)
+        ctx.genmatrix_ptr(SABER, n, a_keys, pk, None, sp)
+        ss_a = torch.empty_like(ss)
+        ms_a = _event_ms(stream, lambda: ctx.kem_dec_a_ptr(SABER, n, ss_a, ct, sk, a_keys, T.FORM_AUTO, sp),
+                         args.steps)
+        cached = {"decaps_per_s": n / (ms_a / 1e3), "ms": ms_a, "bit_exact": bool(torch.equal(ss_a, ss_ref)),
+                  "note": "Saber decapsulation at batch 65536 with each key's GenMatrix stream expanded once "
+                          "(tmvp_genmatrix_batch), as the serving loop keeps it per key"}
+        del a_keys
     # ---- bit-exactness against the CPU oracle on a sample
     oracle_ok = None
     if not args.no_oracle:
@@ -321,6 +334,7 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * (CT_BYTES + SK_BYTES),
                 "d2h_bytes_per_step": n * 32, "ms_per_step": statistics.mean(e2e_ms),
                 "host_chunk": e2e_chunk[0], "ms_by_host_chunk": e2e_chunk[1]},
+        "cached_genmatrix": cached,
         "oracle_sample_note": "256 random instances decapsulated by the CPU oracle and compared",
         "gpu_launches": launches,
         "clocks": clocks,

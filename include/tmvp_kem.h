@@ -128,6 +128,26 @@ int tmvp_kem_enc_batch(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *ct,
 int tmvp_kem_dec_batch(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *ss,
                        const uint8_t *ct, const uint8_t *sk, tmvp_form form, void *stream);
 
+/* Expanded public matrices kept per key (no counterpart in the reference,
+ * which expands A on every call: GenMatrix, saber_enc / saber_dec
+ * cuda_kernel.cu:116-127, :383).  tmvp_genmatrix_batch writes
+ * a_stream[i] = SHAKE-128(seed_A of pk + i * pk_stride), the
+ * tmvp_genmatrix_bytes(set) bytes that GenMatrix unpacks; the _a variants of
+ * encapsulation and decapsulation take those streams (one per instance, in
+ * device memory) instead of expanding A themselves, which removes 23 of the
+ * 39 Keccak-f of a Saber decapsulation.  Results equal the plain calls for
+ * the same keys.  a_stream and pk of tmvp_genmatrix_batch must be device
+ * memory (TMVP_EINVAL otherwise). */
+size_t tmvp_genmatrix_bytes(tmvp_param_set set);
+int tmvp_genmatrix_batch(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *a_stream,
+                         const uint8_t *pk, size_t pk_stride, void *stream);
+int tmvp_kem_enc_batch_a(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *ct, uint8_t *ss,
+                         const uint8_t *pk, const uint8_t *coins, const uint8_t *a_stream,
+                         tmvp_form form, void *stream);
+int tmvp_kem_dec_batch_a(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *ss,
+                         const uint8_t *ct, const uint8_t *sk, const uint8_t *a_stream,
+                         tmvp_form form, void *stream);
+
 /* Batched IND-CPA (indcpa_kem_* of the Saber reference API, n instances). */
 int tmvp_indcpa_keypair_batch(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *pk,
                               uint8_t *sk, const uint8_t *seeds /*[n][64]: seed_A|seed_s*/,

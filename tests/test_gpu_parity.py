@@ -231,3 +231,38 @@ def test_out_of_range_secret_is_reported(kem):
     # the CUDA-core form computes it exactly
     out = ctx.matvec(A, s, eq=13, form=T.FORM_CUDA_CORE)
     assert not out.any()
+
+
+@pytest.mark.parametrize("set_id", [0, 1, 2, 3, 4, 5])
+def test_cached_genmatrix_matches_plain_calls(kem, set_id):
+    """Encapsulation and decapsulation with each key's A expanded once
+    (tmvp_genmatrix_batch + the _a entry points) give the plain calls' bytes,
+    including the implicit rejection of a tampered ciphertext."""
+    import torch
+    T, ctx = kem
+    dev = torch.device("cuda", 0)
+    n = 333
+    z = T.sizes(set_id)
+    coins = torch.from_numpy(T.splitmix_bytes(900 + set_id, n * 96).reshape(n, 96)).to(dev)
+    ec = torch.from_numpy(T.splitmix_bytes(910 + set_id, n * 32).reshape(n, 32)).to(dev)
+    pk = torch.empty((n, z.pk_bytes), dtype=torch.uint8, device=dev)
+    sk = torch.empty((n, z.sk_bytes), dtype=torch.uint8, device=dev)
+    ctx.kem_keypair_ptr(set_id, n, pk, sk, coins)
+    a = torch.empty((n, T.genmatrix_bytes(set_id)), dtype=torch.uint8, device=dev)
+    ctx.genmatrix_ptr(set_id, n, a, pk)
+    ct1 = torch.empty((n, z.ct_bytes), dtype=torch.uint8, device=dev)
+    ss1 = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+    ct2, ss2 = torch.empty_like(ct1), torch.empty_like(ss1)
+    ctx.kem_enc_ptr(set_id, n, ct1, ss1, pk, ec)
+    ctx.kem_enc_a_ptr(set_id, n, ct2, ss2, pk, ec, a)
+    torch.cuda.synchronize()
+    assert torch.equal(ct1, ct2) and torch.equal(ss1, ss2)
+    ct1[7, 11] ^= 0x10
+    d1, d2 = torch.zeros_like(ss1), torch.zeros_like(ss1)
+    ctx.kem_dec_ptr(set_id, n, d1, ct1, sk)
+    ctx.kem_dec_a_ptr(set_id, n, d2, ct1, sk, a)
+    torch.cuda.synchronize()
+    assert torch.equal(d1, d2)
+    good = torch.ones(n, dtype=torch.bool, device=dev)
+    good[7] = False
+    assert torch.equal(d2[good], ss1[good]) and not torch.equal(d2[7], ss1[7])

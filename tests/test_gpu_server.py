@@ -86,7 +86,8 @@ def test_alone_and_in_the_mix(kem, oracle):
 def test_memory_admission_and_loadgen(kem):
     T, ctx = kem
     # a budget that holds two slots of 256 requests, while four were asked for
-    one_slot = 256 * (1472 + 1504 + 3040 + 4 + 16 * 416 + 768 + 64 + 64 + 1 + 32) + 64 * 256
+    # (per request: input, output, key, index, the key's expanded A, KEM workspace)
+    one_slot = 256 * (1472 + 1504 + 3040 + 4 + 16 * 416 + 16 * 416 + 768 + 64 + 64 + 1 + 32) + 64 * 256
     srv = T.Server(max_batch=256, slots=4, mem_budget=2 * one_slot + 1000)
     try:
         assert srv.stats()["slots"] == 2
