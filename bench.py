@@ -403,114 +403,119 @@ def _workloads(ctx, T, dev, sp, stream, args):
     batch 65536, and the serving loop under Poisson load."""
     import torch
     out = {}
+    W = set(args.workloads.split(","))
     forms = [("fp8_tc", T.FORM_FP8_TC), ("int8_tc", T.FORM_INT8_TC), ("cuda_core", T.FORM_CUDA_CORE)]
     if hasattr(T, "FORM_FP8_TCGEN05"):
         forms.insert(0, ("fp8_tcgen05", T.FORM_FP8_TCGEN05))
     # raw matrix-vector: 16384 instances of a 3x3 matrix (uniform mod 2^13) times CBD(mu=8) secrets
-    n, l = 16384, 3
-    g = torch.Generator(device="cpu").manual_seed(1234)
-    A = torch.randint(0, 1 << 13, (n, l, l, 256), generator=g, dtype=torch.int32).to(torch.int16).to(dev)
-    r = torch.randint(0, 256, (n, l, 256), generator=g, dtype=torch.int32)
-    pc = torch.tensor([bin(i).count("1") for i in range(16)], dtype=torch.int32)
-    s8 = (pc[r & 15] - pc[r >> 4]).to(torch.int8).to(dev)
-    mv = {}
-    ref = None
-    for name, f in forms:
-        o = torch.empty((n, l, 256), dtype=torch.int16, device=dev)
-        fn = lambda o=o, f=f: ctx.matvec_ptr(n, l, 13, False, o, A, s8, f, sp)
-        for _ in range(3):
-            fn()
-        ms = _event_ms(stream, fn, 10)
-        if ref is None:
-            ref = o.clone()
-        mv[name] = {"instances_per_s": n / (ms / 1e3), "ms": ms, "matches_first_form": bool(torch.equal(o, ref))}
-    if "cuda_core" in mv:
-        for name in mv:
-            mv[name]["over_cuda_core"] = mv[name]["instances_per_s"] / mv["cuda_core"]["instances_per_s"]
-    out["matvec_16384_l3"] = mv
+    if "matvec" in W:
+        n, l = 16384, 3
+        g = torch.Generator(device="cpu").manual_seed(1234)
+        A = torch.randint(0, 1 << 13, (n, l, l, 256), generator=g, dtype=torch.int32).to(torch.int16).to(dev)
+        r = torch.randint(0, 256, (n, l, 256), generator=g, dtype=torch.int32)
+        pc = torch.tensor([bin(i).count("1") for i in range(16)], dtype=torch.int32)
+        s8 = (pc[r & 15] - pc[r >> 4]).to(torch.int8).to(dev)
+        mv = {}
+        ref = None
+        for name, f in forms:
+            o = torch.empty((n, l, 256), dtype=torch.int16, device=dev)
+            fn = lambda o=o, f=f: ctx.matvec_ptr(n, l, 13, False, o, A, s8, f, sp)
+            for _ in range(3):
+                fn()
+            ms = _event_ms(stream, fn, 10)
+            if ref is None:
+                ref = o.clone()
+            mv[name] = {"instances_per_s": n / (ms / 1e3), "ms": ms, "matches_first_form": bool(torch.equal(o, ref))}
+        if "cuda_core" in mv:
+            for name in mv:
+                mv[name]["over_cuda_core"] = mv[name]["instances_per_s"] / mv["cuda_core"]["instances_per_s"]
+        out["matvec_16384_l3"] = mv
     # Sable l=3 full KEM at batch 65536
-    SABLE = 4
-    z = T.sizes(SABLE)
-    nb = 65536
-    coins = torch.from_numpy(T.splitmix_bytes(77, nb * 96).reshape(nb, 96)).to(dev)
-    ecoins = torch.from_numpy(T.splitmix_bytes(78, nb * 32).reshape(nb, 32)).to(dev)
-    pk = torch.empty((nb, z.pk_bytes), dtype=torch.uint8, device=dev)
-    sk = torch.empty((nb, z.sk_bytes), dtype=torch.uint8, device=dev)
-    ct = torch.empty((nb, z.ct_bytes), dtype=torch.uint8, device=dev)
-    ss1 = torch.empty((nb, 32), dtype=torch.uint8, device=dev)
-    ss2 = torch.empty((nb, 32), dtype=torch.uint8, device=dev)
-    sab = {}
-    for name, f in forms:
-        kp = lambda f=f: ctx.kem_keypair_ptr(SABLE, nb, pk, sk, coins, f, sp)
-        en = lambda f=f: ctx.kem_enc_ptr(SABLE, nb, ct, ss1, pk, ecoins, f, sp)
-        de = lambda f=f: ctx.kem_dec_ptr(SABLE, nb, ss2, ct, sk, f, sp)
-        for fn in (kp, en, de):
-            fn()
-        t_kp, t_en, t_de = (_event_ms(stream, fn, 3) for fn in (kp, en, de))
-        sab[name] = {"keypairs_per_s": nb / (t_kp / 1e3), "encaps_per_s": nb / (t_en / 1e3),
-                     "decaps_per_s": nb / (t_de / 1e3),
-                     "round_trips_per_s": nb / ((t_kp + t_en + t_de) / 1e3),
-                     "bit_exact_round_trip": bool(torch.equal(ss1, ss2))}
-    out["sable_l3_kem_65536"] = sab
+    if "sable" in W:
+        SABLE = 4
+        z = T.sizes(SABLE)
+        nb = 65536
+        coins = torch.from_numpy(T.splitmix_bytes(77, nb * 96).reshape(nb, 96)).to(dev)
+        ecoins = torch.from_numpy(T.splitmix_bytes(78, nb * 32).reshape(nb, 32)).to(dev)
+        pk = torch.empty((nb, z.pk_bytes), dtype=torch.uint8, device=dev)
+        sk = torch.empty((nb, z.sk_bytes), dtype=torch.uint8, device=dev)
+        ct = torch.empty((nb, z.ct_bytes), dtype=torch.uint8, device=dev)
+        ss1 = torch.empty((nb, 32), dtype=torch.uint8, device=dev)
+        ss2 = torch.empty((nb, 32), dtype=torch.uint8, device=dev)
+        sab = {}
+        for name, f in forms:
+            kp = lambda f=f: ctx.kem_keypair_ptr(SABLE, nb, pk, sk, coins, f, sp)
+            en = lambda f=f: ctx.kem_enc_ptr(SABLE, nb, ct, ss1, pk, ecoins, f, sp)
+            de = lambda f=f: ctx.kem_dec_ptr(SABLE, nb, ss2, ct, sk, f, sp)
+            for fn in (kp, en, de):
+                fn()
+            t_kp, t_en, t_de = (_event_ms(stream, fn, 3) for fn in (kp, en, de))
+            sab[name] = {"keypairs_per_s": nb / (t_kp / 1e3), "encaps_per_s": nb / (t_en / 1e3),
+                         "decaps_per_s": nb / (t_de / 1e3),
+                         "round_trips_per_s": nb / ((t_kp + t_en + t_de) / 1e3),
+                         "bit_exact_round_trip": bool(torch.equal(ss1, ss2))}
+        out["sable_l3_kem_65536"] = sab
     # mixed batch: requests of LightSaber, Saber, FireSaber and Sable interleaved, each with a
-    # count drawn uniformly from 1..8192, decapsulated by one CUDA-graph replay
-    rng = np.random.default_rng(4242)
-    sets = [0, 1, 2, 4]
-    reqs = [(sets[i % 4], int(rng.integers(1, 8193))) for i in range(24)]
-    made, outs = [], []
-    for i, (sid, cnt) in enumerate(reqs):
-        z = T.sizes(sid)
-        cc = torch.from_numpy(T.splitmix_bytes(9000 + i, cnt * 96).reshape(cnt, 96)).to(dev)
-        ee = torch.from_numpy(T.splitmix_bytes(9500 + i, cnt * 32).reshape(cnt, 32)).to(dev)
-        pk_i = torch.empty((cnt, z.pk_bytes), dtype=torch.uint8, device=dev)
-        sk_i = torch.empty((cnt, z.sk_bytes), dtype=torch.uint8, device=dev)
-        ct_i = torch.empty((cnt, z.ct_bytes), dtype=torch.uint8, device=dev)
-        ss_i = torch.empty((cnt, 32), dtype=torch.uint8, device=dev)
-        ctx.kem_keypair_ptr(sid, cnt, pk_i, sk_i, cc, T.FORM_AUTO, sp)
-        ctx.kem_enc_ptr(sid, cnt, ct_i, ss_i, pk_i, ee, T.FORM_AUTO, sp)
-        made.append((sid, cnt, sk_i, ct_i, ss_i))
-        outs.append(torch.zeros_like(ss_i))
-    total = sum(c for _, c in reqs)
-    plan = T.MixedPlan(ctx, [(sid, outs[i], ct_i, sk_i) for i, (sid, _, sk_i, ct_i, _) in enumerate(made)])
-    try:
-        ms_graph = _event_ms(stream, lambda: plan.launch(sp), 5)
-    finally:
-        plan.close()
-    exact = all(torch.equal(outs[i], made[i][4]) for i in range(len(made)))
+    if "mixed" in W:
+        # count drawn uniformly from 1..8192, decapsulated by one CUDA-graph replay
+        rng = np.random.default_rng(4242)
+        sets = [0, 1, 2, 4]
+        reqs = [(sets[i % 4], int(rng.integers(1, 8193))) for i in range(24)]
+        made, outs = [], []
+        for i, (sid, cnt) in enumerate(reqs):
+            z = T.sizes(sid)
+            cc = torch.from_numpy(T.splitmix_bytes(9000 + i, cnt * 96).reshape(cnt, 96)).to(dev)
+            ee = torch.from_numpy(T.splitmix_bytes(9500 + i, cnt * 32).reshape(cnt, 32)).to(dev)
+            pk_i = torch.empty((cnt, z.pk_bytes), dtype=torch.uint8, device=dev)
+            sk_i = torch.empty((cnt, z.sk_bytes), dtype=torch.uint8, device=dev)
+            ct_i = torch.empty((cnt, z.ct_bytes), dtype=torch.uint8, device=dev)
+            ss_i = torch.empty((cnt, 32), dtype=torch.uint8, device=dev)
+            ctx.kem_keypair_ptr(sid, cnt, pk_i, sk_i, cc, T.FORM_AUTO, sp)
+            ctx.kem_enc_ptr(sid, cnt, ct_i, ss_i, pk_i, ee, T.FORM_AUTO, sp)
+            made.append((sid, cnt, sk_i, ct_i, ss_i))
+            outs.append(torch.zeros_like(ss_i))
+        total = sum(c for _, c in reqs)
+        plan = T.MixedPlan(ctx, [(sid, outs[i], ct_i, sk_i) for i, (sid, _, sk_i, ct_i, _) in enumerate(made)])
+        try:
+            ms_graph = _event_ms(stream, lambda: plan.launch(sp), 5)
+        finally:
+            plan.close()
+        exact = all(torch.equal(outs[i], made[i][4]) for i in range(len(made)))
 
-    sep_out = [torch.empty_like(o) for o in outs]
+        sep_out = [torch.empty_like(o) for o in outs]
 
-    def per_request():
-        for i, (sid, cnt, sk_i, ct_i, _) in enumerate(made):
-            ctx.kem_dec_ptr(sid, cnt, sep_out[i], ct_i, sk_i, T.FORM_AUTO, sp)
-    ms_sep = _event_ms(stream, per_request, 3)
-    out["mixed_graph"] = {"requests": len(reqs), "instances": total, "sets": "LightSaber, Saber, FireSaber, Sable",
-                          "decaps_per_s": total / (ms_graph / 1e3), "ms": ms_graph,
-                          "per_request_calls_decaps_per_s": total / (ms_sep / 1e3),
-                          "bit_exact": bool(exact),
-                          "launch": "one CUDA graph, five launches: each stage one launch over all 24 requests"}
+        def per_request():
+            for i, (sid, cnt, sk_i, ct_i, _) in enumerate(made):
+                ctx.kem_dec_ptr(sid, cnt, sep_out[i], ct_i, sk_i, T.FORM_AUTO, sp)
+        ms_sep = _event_ms(stream, per_request, 3)
+        out["mixed_graph"] = {"requests": len(reqs), "instances": total, "sets": "LightSaber, Saber, FireSaber, Sable",
+                              "decaps_per_s": total / (ms_graph / 1e3), "ms": ms_graph,
+                              "per_request_calls_decaps_per_s": total / (ms_sep / 1e3),
+                              "bit_exact": bool(exact),
+                              "launch": "one CUDA graph, five launches: each stage one launch over all 24 requests"}
     # serving loop: Poisson arrivals over LightSaber, Saber, FireSaber and Sable
-    rate, secs = 200_000.0, 2.0
-    srv = T.Server(device=dev.index or 0, max_batch=4096, slots=4, form=T.FORM_AUTO)
-    try:
-        ids = []
-        for k, sid in enumerate((0, 1, 2, 4)):
-            kpk, ksk = ctx.kem_keypair(sid, T.splitmix_bytes(500 + k, 256 * 96).reshape(256, 96))
-            ids.append(srv.add_keys(sid, kpk, ksk))
-        # warm-up at the same load (module loading, workspace growth), then the measured run
-        srv.loadgen(rate=rate, seconds=0.25, seed=20, key_ids=np.concatenate(ids), decaps_fraction=0.5)
-        srv.reset_stats()
-        nreq = srv.loadgen(rate=rate, seconds=secs, seed=21, key_ids=np.concatenate(ids),
-                           decaps_fraction=0.5)
-        st = srv.stats()
-    finally:
-        srv.close()
-    out["serving"] = {"offered_req_per_s": rate, "seconds": secs, "requests": nreq,
-                      "throughput_req_per_s": st["throughput"], "p50_us": st["p50_us"],
-                      "p99_us": st["p99_us"], "max_us": st["max_us"], "mean_batch": st["mean_batch"],
-                      "batches": st["batches"], "slots": st["slots"], "failed": st["failed"],
-                      "mix": "encaps/decaps 50/50 over LightSaber, Saber, FireSaber, Sable; 256 keys each",
-                      "warmup_s": 0.25}
+    if "serving" in W:
+        rate, secs = 200_000.0, 2.0
+        srv = T.Server(device=dev.index or 0, max_batch=4096, slots=4, form=T.FORM_AUTO)
+        try:
+            ids = []
+            for k, sid in enumerate((0, 1, 2, 4)):
+                kpk, ksk = ctx.kem_keypair(sid, T.splitmix_bytes(500 + k, 256 * 96).reshape(256, 96))
+                ids.append(srv.add_keys(sid, kpk, ksk))
+            # warm-up at the same load (module loading, workspace growth), then the measured run
+            srv.loadgen(rate=rate, seconds=0.25, seed=20, key_ids=np.concatenate(ids), decaps_fraction=0.5)
+            srv.reset_stats()
+            nreq = srv.loadgen(rate=rate, seconds=secs, seed=21, key_ids=np.concatenate(ids),
+                               decaps_fraction=0.5)
+            st = srv.stats()
+        finally:
+            srv.close()
+        out["serving"] = {"offered_req_per_s": rate, "seconds": secs, "requests": nreq,
+                          "throughput_req_per_s": st["throughput"], "p50_us": st["p50_us"],
+                          "p99_us": st["p99_us"], "max_us": st["max_us"], "mean_batch": st["mean_batch"],
+                          "batches": st["batches"], "slots": st["slots"], "failed": st["failed"],
+                          "mix": "encaps/decaps 50/50 over LightSaber, Saber, FireSaber, Sable; 256 keys each",
+                          "warmup_s": 0.25}
     return out
 
 
@@ -546,6 +551,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the matrix-vector, Sable and serving workloads")
+    ap.add_argument("--workloads", default="matvec,sable,mixed,serving",
+                    help="extra workloads to run (comma list of matvec, sable, mixed, serving)")
     ap.add_argument("--forms", default="fp8_tc,int8_tc,cuda_core",
                     help="forms to time besides the headline (AUTO) form (comma list, or 'none')")
     args = ap.parse_args()
