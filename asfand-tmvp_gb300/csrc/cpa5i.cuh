@@ -11,8 +11,10 @@
 //   3. one thread issues the 8 l tcgen05.mma (M = 128, N = 16 / 32, K = 32;
 //      each window of the Hankel sequence serves both M halves through the
 //      negacyclic wrap) into tensor memory and commits them to an mbarrier;
-//   4. accumulators -> int32 columns (tcgen05.ld) -> the rounding / packing /
-//      compare / decode epilogue, eight coefficients at a time.
+//   4. accumulators -> registers (tcgen05.ld: every digit column of one
+//      coefficient per thread) -> the compare / decode / output epilogue
+//      (encryption and key generation: rounded 16-bit values, then packed
+//      eight coefficients at a time).
 // Same results as the runtime-shaped kernels (cpa_tc_kernel.cuh,
 // cpa_persist.cuh); the arithmetic per instance is the same.
 #pragma once
@@ -106,7 +108,8 @@ struct LayoutC {
   static constexpr int BM = H + C::L * kHankelBytes5;
   static constexpr int EXT = BM + C::L * BJ;
   static constexpr int ENG_END_OPS = EXT + C::L * 512;
-  static constexpr int ENG_BYTES = ENG_END_OPS > S::NCOLS * 1024 ? ENG_END_OPS : S::NCOLS * 1024;
+  static constexpr int ENG_BYTES = ENG_END_OPS;  // also holds the epilogue's 16-bit values (R x 512 bytes)
+  static_assert(S::R * 512 <= ENG_END_OPS, "epilogue values fit the operand region");
   static constexpr int CTO = al16c(ENG + ENG_BYTES);
   static constexpr int MSG = HAS_CT ? al16c(CTO + C::CT + 16) : CTO;
   static constexpr int SEC8 = HAS_B ? al16c(MSG + 32 + 16) : MSG;
@@ -227,7 +230,6 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
   uint32_t *sec8w = reinterpret_cast<uint32_t *>(sm + LO::SEC8);
   uint8_t *H = sm + LO::H, *Bm = sm + LO::BM;
   const uint32_t ext32 = smem_u32(sm + LO::EXT);
-  int *acc = reinterpret_cast<int *>(sm + LO::ENG);
   bool ok = true, done = false;
   if (ready) {
     // 1. secrets, straight into s_ext (s_ext[d] = -s[d + 1] for d < 255,
@@ -396,7 +398,6 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
   const int q4 = warp & 3, hsel = warp >> 2;
   const int k = 128 * hsel + 32 * q4 + lane;
   constexpr int G8 = 8 * LO::G;
-  constexpr bool FUSED = OP == kDecrypt || OP == kReenc || OP == kMatvec;
   float xacc[G8];  // digit column c of coefficient k, times 2^-9 (exact)
   if (done) {
     const uint32_t t0 = tmem + ((uint32_t)(32 * q4) << 16);
@@ -415,9 +416,30 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
 #pragma unroll
       for (int c = 0; c < S::NCOLS; c++) xacc[c] = __uint_as_float(f[c]) + __uint_as_float(g[c]);
     }
-    if constexpr (!FUSED) {
+    if constexpr (OP == kEncrypt || OP == kKeygen) {
+      // coefficient k of every output polynomial, rounded (b, b') or encoded
+      // with the message bit (c_m), as 16-bit values for the packing pass;
+      // the MMAs are done, so the operand region is free
+      constexpr uint32_t qm = (1u << C::EQ) - 1u, pm = (1u << C::EP) - 1u;
+      uint16_t *vals = reinterpret_cast<uint16_t *>(sm + LO::ENG);
 #pragma unroll
-      for (int c = 0; c < S::NCOLS; c++) acc[c * 256 + k] = __float2int_rn(xacc[c] * 512.0f);
+      for (int p = 0; p < S::R; p++) {
+        uint32_t v = 0, off = 0;
+#pragma unroll
+        for (int d = 0; d < 4; d++) {
+          if (d < S::digits(p)) {
+            v += (1u << (4 * d)) * __float_as_uint(xacc[S::col_base(p) + d] + 24576.0f);
+            off += (1u << (4 * d)) * 0x46C00000u;
+          }
+        }
+        v -= off;
+        if (p < L) {
+          vals[256 * p + k] = (uint16_t)(((v + C::H1) & qm) >> (C::EQ - C::EP));
+        } else {
+          const uint32_t mk = (sm[LO::MSG + (k >> 3)] >> (k & 7)) & 1u;
+          vals[256 * p + k] = (uint16_t)(((v + C::H1 - (mk << (C::EP - 1))) & pm) >> (C::EP - C::ET));
+        }
+      }
     }
   } else {
     // an input copy or the tensor core did not complete in time: report, and
@@ -433,46 +455,9 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
   if (warp == 0) tmem_dealloc(tmem, S::TMEM_COLS);
   if (!done) return;
 
-  // 5. epilogues on groups of eight coefficients
-  auto combine8 = [&](int p, int grp, uint32_t (&V)[4]) {
-    const int cb = p < S::RA ? p * S::DA : S::RA * S::DA + (p - S::RA) * S::DB;
-    const int D = p < S::RA ? S::DA : S::DB;
-    const int4 *base = reinterpret_cast<const int4 *>(acc + 8 * grp);
-    uint32_t v[8];
-    {
-      const int4 x0 = base[cb * 64], x1 = base[cb * 64 + 1];
-      v[0] = x0.x; v[1] = x0.y; v[2] = x0.z; v[3] = x0.w;
-      v[4] = x1.x; v[5] = x1.y; v[6] = x1.z; v[7] = x1.w;
-    }
-#pragma unroll
-    for (int d = 1; d < (S::DA > S::DB ? S::DA : S::DB); d++) {
-      if (d < D) {
-        const uint32_t wgt = 1u << (4 * d);
-        const int4 x0 = base[(cb + d) * 64], x1 = base[(cb + d) * 64 + 1];
-        v[0] += wgt * (uint32_t)x0.x; v[1] += wgt * (uint32_t)x0.y;
-        v[2] += wgt * (uint32_t)x0.z; v[3] += wgt * (uint32_t)x0.w;
-        v[4] += wgt * (uint32_t)x1.x; v[5] += wgt * (uint32_t)x1.y;
-        v[6] += wgt * (uint32_t)x1.z; v[7] += wgt * (uint32_t)x1.w;
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < 4; i++) V[i] = (v[2 * i] & 0xffffu) | (v[2 * i + 1] << 16);
-  };
+  // 5. epilogues
   constexpr uint32_t qmask = (1u << C::EQ) - 1u, pmask = (1u << C::EP) - 1u;
-  // round(x) = ((x + h1) mod q) >> (eq - ep) on two 16-bit lanes
-  auto round_lanes = [&](uint32_t x) -> uint32_t {
-    const uint32_t lo16 = (((x & 0xffffu) + C::H1) & qmask) >> (C::EQ - C::EP);
-    const uint32_t hi16 = (((x >> 16) + C::H1) & qmask) >> (C::EQ - C::EP);
-    return lo16 | (hi16 << 16);
-  };
-  // c_m = ((x + h1 - (m << (ep-1))) mod p) >> (ep - et) on two 16-bit lanes
-  auto encode_lanes = [&](uint32_t x, uint32_t mlo, uint32_t mhi) -> uint32_t {
-    const uint32_t lo16 = (((x & 0xffffu) + C::H1 - (mlo << (C::EP - 1))) & pmask) >> (C::EP - C::ET);
-    const uint32_t hi16 = (((x >> 16) + C::H1 - (mhi << (C::EP - 1))) & pmask) >> (C::EP - C::ET);
-    return lo16 | (hi16 << 16);
-  };
-
-  // sum_d 16^d acc_d of the digit columns c0.. (FUSED path): each f32
+  // sum_d 16^d acc_d of the digit columns c0..: each f32
   // accumulator holds x * 2^-9 for an exact integer |x| < 2^22, so adding
   // 1.5 * 2^14 leaves x + 0x46C00000 in its bit pattern; the offsets are
   // removed at the end
@@ -527,33 +512,25 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
 #pragma unroll
     for (int p = 0; p < L; p++) o[256 * p] = (uint16_t)(combine1(S::col_base(p), S::DA) & m);
   } else if (OP == kEncrypt) {
-    const uint8_t *msg = sm + LO::MSG;
+    // pack the 16-bit values eight at a time: b' at EP bits, c_m at ET bits
+    const uint16_t *vals = reinterpret_cast<const uint16_t *>(sm + LO::ENG);
     for (int idx = tid; idx < S::R * 32; idx += NT) {
       const int p = idx >> 5, grp = idx & 31;
-      uint32_t V[4], W[4];
-      combine8(p, grp, V);
-      if (p < L) {
-#pragma unroll
-        for (int i = 0; i < 4; i++) W[i] = round_lanes(V[i]);
-        pack8(sm + LO::OUT + (32 * p + grp) * C::EP, W, C::EP);
-      } else {
-        const uint32_t mb = msg[grp];
-#pragma unroll
-        for (int i = 0; i < 4; i++) W[i] = encode_lanes(V[i], (mb >> (2 * i)) & 1u, (mb >> (2 * i + 1)) & 1u);
-        pack8(sm + LO::OUT + L * C::POLYCOMP + grp * C::ET, W, C::ET);
-      }
+      const uint4 q = *reinterpret_cast<const uint4 *>(vals + 256 * p + 8 * grp);
+      const uint32_t W[4] = {q.x, q.y, q.z, q.w};
+      if (p < L) pack8(sm + LO::OUT + (32 * p + grp) * C::EP, W, C::EP);
+      else pack8(sm + LO::OUT + L * C::POLYCOMP + grp * C::ET, W, C::ET);
     }
     __syncthreads();
     copy16(a.ct_out + (size_t)inst * C::CT, sm + LO::OUT, C::CT);
   } else if (OP == kKeygen) {
     constexpr int bbytes = L * C::POLYCOMP;
     uint8_t *outb = sm + LO::OUT;
+    const uint16_t *vals = reinterpret_cast<const uint16_t *>(sm + LO::ENG);
     for (int idx = tid; idx < L * 32; idx += NT) {
       const int p = idx >> 5, grp = idx & 31;
-      uint32_t V[4], W[4];
-      combine8(p, grp, V);
-#pragma unroll
-      for (int i = 0; i < 4; i++) W[i] = round_lanes(V[i]);
+      const uint4 q = *reinterpret_cast<const uint4 *>(vals + 256 * p + 8 * grp);
+      const uint32_t W[4] = {q.x, q.y, q.z, q.w};
       pack8(outb + (32 * p + grp) * C::EP, W, C::EP);
     }
     // secret key: 13-bit two's complement (Saber) or 2-bit (Sable) of sec8
