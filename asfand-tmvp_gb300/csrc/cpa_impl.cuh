@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(CpaCfg<FORM, OP, L, Q>::NT) k_cpa(CpaArgs a) {
 
 template <int FORM, int OP, int L, int Q>
 inline int launch_one(const CpaArgs &a, cudaStream_t s) {
-  if constexpr (FORM == kFp8TC || FORM == kInt8TC || FORM == kFp8Tcgen05) {
+  if constexpr (FORM == kFp8TC || FORM == kInt8TC) {
     return launch_tc<FORM, OP, L, Q>(a, s);
   } else {
     using C = CpaCfg<FORM, OP, L, Q>;
@@ -335,8 +335,7 @@ template <int FORM, int OP, int L>
 inline int tc_q(const CpaArgs &a) {
   using C = CpaCfg<FORM, OP, L>;
   int wa = OP == kMatvec ? a.mv_eq : a.P.eq;
-  const int q = (tc_cols<FORM>(C::R, C::RA, wa, a.P.ep) + 7) / 8;
-  return FORM == kFp8Tcgen05 ? (q + 1) & ~1 : q;  // tcgen05: N = 16 or 32
+  return (tc_cols<FORM>(C::R, C::RA, wa, a.P.ep) + 7) / 8;
 }
 
 template <int FORM, int OP, int L>
@@ -345,11 +344,11 @@ inline int launch_q(const CpaArgs &a, cudaStream_t s) {
     return launch_one<FORM, OP, L, 1>(a, s);
   } else {
     switch (tc_q<FORM, OP, L>(a)) {
-      case 1: if constexpr (FORM != kFp8Tcgen05) return launch_one<FORM, OP, L, 1>(a, s); break;
+      case 1: return launch_one<FORM, OP, L, 1>(a, s);
       case 2: return launch_one<FORM, OP, L, 2>(a, s);
       case 3: if constexpr (FORM == kFp8TC) return launch_one<FORM, OP, L, 3>(a, s); break;
       case 4:
-        if constexpr (FORM == kFp8TC || FORM == kFp8Tcgen05) return launch_one<FORM, OP, L, 4>(a, s);
+        if constexpr (FORM == kFp8TC) return launch_one<FORM, OP, L, 4>(a, s);
         break;
     }
     return (int)cudaErrorInvalidValue;

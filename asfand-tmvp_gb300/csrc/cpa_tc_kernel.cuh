@@ -1,4 +1,6 @@
-// cpa_tc_kernel.cuh — the tensor-core IND-CPA kernel (one CTA per instance).
+// cpa_tc_kernel.cuh — the mma.sync tensor-core IND-CPA kernel (FP8_TC and
+// INT8_TC forms, one CTA per instance; the tcgen05 form has its own kernels,
+// cpa5i.cuh and cpa_persist.cuh).
 //
 // Same shape and results as the generic k_cpa template (cpa_impl.cuh), tuned
 // for the tensor-core forms, where the integer work around the MMAs dominates:
@@ -26,7 +28,6 @@ struct TcLayout {
   int eng;    // digit columns [l][Q*8][272] then Toeplitz copies [l][4][136] words;
               // int32 accumulators [Q*8][256] alias it after the MMAs
   int out;    // packed output staging (ct / pk part) for encrypt / keygen
-  int bar;    // tcgen05 form: mbarrier (8 bytes) and the TMEM base address
   int total;
 };
 
@@ -44,7 +45,7 @@ inline TcLayout tc_layout(const KemParams &P) {
   TcLayout o;
   int off = 0;
   auto take = [&](int bytes) { int r = off; off = tc_align(off + bytes + 16); return r; };
-  o.raw_a = o.raw_s = o.raw_b = o.raw_msg = o.raw_ct = o.raw_sk = o.out = o.bar = -1;
+  o.raw_a = o.raw_s = o.raw_b = o.raw_msg = o.raw_ct = o.raw_sk = o.out = -1;
   if (OP == kEncrypt || OP == kReenc || OP == kKeygen) {
     o.raw_a = take(P.gm_bytes);
     o.raw_s = take(P.gs_bytes);
@@ -57,11 +58,9 @@ inline TcLayout tc_layout(const KemParams &P) {
   if (OP == kDecrypt) o.raw_sk = take(P.indcpa_sk_bytes);
   o.sec8 = take(L * 256);
   o.senc = take(L * 256);
-  int eng = FORM == kFp8Tcgen05 ? L * (kHankelBytes + 256 * Q * 8 + 512)
-                                 : L * Q * 8 * kColStride + L * kTzBytesPerPoly;
+  int eng = L * Q * 8 * kColStride + L * kTzBytesPerPoly;
   if (Q * 8 * 256 * 4 > eng) eng = Q * 8 * 256 * 4;
   o.eng = take(eng);
-  if (FORM == kFp8Tcgen05) o.bar = take(16);
   if (OP == kEncrypt) o.out = take(P.ct_bytes);
   if (OP == kKeygen) o.out = take(L * P.polycompbytes + P.indcpa_sk_bytes);
   o.total = off;
@@ -114,19 +113,7 @@ __global__ void __launch_bounds__(128, (Q >= 4 ? 3 : 4)) k_cpa_tc(CpaArgs a, TcL
   const KemParams &P = a.P;
   const unsigned inst = blockIdx.x;
   const int tid = threadIdx.x;
-  constexpr int NU = Q * 8;                            // tcgen05: N of the MMA
-  constexpr uint32_t kTmemCols = NU <= 16 ? 32u : 64u;  // two M halves of N f32 columns
-  uint32_t mbar = 0;
-  if constexpr (FORM == kFp8Tcgen05) {
-    static_assert(NU == 16 || NU == 32, "tcgen05 form: N = 16 or 32");
-    mbar = smem_u32(sm + lo.bar);
-    if (tid < 32) tmem_alloc(smem_u32(sm + lo.bar + 8), kTmemCols);
-    if (tid == 0) {
-      mbar_init(mbar, 1);
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    tc_fence_before();
-  }
+  static_assert(FORM == kFp8TC || FORM == kInt8TC, "mma.sync forms");
 
   // 1. packed inputs to shared memory
   if (lo.raw_a >= 0) copy16(sm + lo.raw_a, a.a_stream + (size_t)inst * P.gm_bytes, P.gm_bytes);
@@ -213,28 +200,14 @@ __global__ void __launch_bounds__(128, (Q >= 4 ? 3 : 4)) k_cpa_tc(CpaArgs a, TcL
     if (!ok && a.err) atomicOr(a.err, 1);
   }
 
-  // 3. public digit columns
-  //    mma.sync forms: [l][Q*8 columns][kColStride bytes], then the Toeplitz
-  //    copies; tcgen05 form: Hankel core matrices [l][kHankelBytes], digit
-  //    columns [l][256 x N] in core-matrix order with K reversed, then s_ext
+  // 3. public digit columns [l][Q*8 columns][kColStride bytes], then the
+  //    Toeplitz copies
   uint32_t *colw = reinterpret_cast<uint32_t *>(sm + lo.eng);
   uint32_t *tz = colw + L * Q * 8 * (kColStride / 4);
-  uint8_t *umma_h = sm + lo.eng;
-  uint8_t *umma_b = umma_h + L * kHankelBytes;
-  uint32_t *umma_ext = reinterpret_cast<uint32_t *>(umma_b + L * 256 * NU);
   const int wa = OP == kMatvec ? a.mv_eq : P.eq, wb = P.ep;
   const int Da = tc_digits<FORM>(wa), Db = tc_digits<FORM>(wb);
   const int c0 = FORM == kFp8TC ? 1 : 0;
   const int ncols = c0 + C::RA * Da + (C::R - C::RA) * Db;
-  if constexpr (FORM == kFp8Tcgen05) {
-    // zero the padding columns ncols..N-1 (16 bytes = one K chunk of a column)
-    const int padc = NU - ncols;
-    for (int idx = tid; idx < L * padc * 16; idx += C::NT) {
-      const int j = idx / (padc * 16), r = idx % (padc * 16), n = ncols + r % padc, ac = r / padc;
-      *reinterpret_cast<uint4 *>(umma_b + j * 256 * NU + ac * 16 * NU + (n >> 3) * 128 + (n & 7) * 16) =
-          make_uint4(0u, 0u, 0u, 0u);
-    }
-  }
   for (int idx = tid; idx < C::R * L * 32; idx += C::NT) {
     const int grp = idx & 31, j = (idx >> 5) % L, p = idx / (32 * L);
     uint32_t X[4];
@@ -253,79 +226,11 @@ __global__ void __launch_bounds__(128, (Q >= 4 ? 3 : 4)) k_cpa_tc(CpaArgs a, TcL
     }
     const int D = p < C::RA ? Da : Db;
     const int cb = c0 + (p < C::RA ? p * Da : C::RA * Da + (p - C::RA) * Db);
-    if constexpr (FORM == kFp8Tcgen05) {
-      // coefficients 8grp..8grp+7 are rows k' = 248-8grp .. 255-8grp, reversed
-      const int kq = 31 - grp;
-      uint8_t *base = umma_b + j * 256 * NU + (kq >> 1) * 16 * NU + 8 * (kq & 1);
-      for (int d = 0; d < D; d++) {
-        const int n = cb + d;
-        uint2 v = digit8<FORM>(X, d, p < C::RA ? wa : wb);
-        *reinterpret_cast<uint2 *>(base + (n >> 3) * 128 + (n & 7) * 16) =
-            make_uint2(__byte_perm(v.y, 0, 0x0123), __byte_perm(v.x, 0, 0x0123));
-      }
-    } else {
-      uint2 *dst = reinterpret_cast<uint2 *>(colw + (j * Q * 8 + cb) * (kColStride / 4) + 2 * grp);
-      for (int d = 0; d < D; d++) dst[d * (kColStride / 8)] = digit8<FORM>(X, d);
-    }
-  }
-  if constexpr (FORM == kFp8Tcgen05) {
-    __syncthreads();  // every secret word of stage 2 is written before s_ext reads them
-    stage_ext(umma_ext, sencw, L, tid, C::NT, [](uint32_t v) { return v ^ 0x80808080u; });
+    uint2 *dst = reinterpret_cast<uint2 *>(colw + (j * Q * 8 + cb) * (kColStride / 4) + 2 * grp);
+    for (int d = 0; d < D; d++) dst[d * (kColStride / 8)] = digit8<FORM>(X, d);
   }
   __syncthreads();
 
-  if constexpr (FORM == kFp8Tcgen05) {
-    // 4'. Hankel core matrices, then the MMAs on the tensor cores
-    stage_hankel(umma_h, umma_ext, L, tid, C::NT);
-    fence_async_smem();  // generic-proxy writes -> visible to the tensor core
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(sm + lo.bar + 8);
-    if (tid == 0) {
-      // descriptors differ only in the start address field (16-byte units)
-      constexpr uint32_t idesc = umma_idesc_e4m3(NU);
-      const uint64_t ad0 = umma_desc(smem_u32(umma_h), 256, 128);
-      const uint64_t bd0 = umma_desc(smem_u32(umma_b), 16 * NU, 128);
-#pragma unroll
-      for (int j = 0; j < L; j++) {
-#pragma unroll
-        for (int ks = 0; ks < 8; ks++) {
-          const uint64_t bd = bd0 + (uint64_t)((j * 256 * NU + 2 * ks * 16 * NU) >> 4);
-#pragma unroll
-          for (int hh = 0; hh < 2; hh++) {
-            const uint64_t ad = ad0 + (uint64_t)((j * kHankelBytes + (16 * hh + 4 * ks) * 128) >> 4);
-            umma_f8(tmem + hh * NU, ad, bd, idesc, (j | ks) != 0);
-          }
-        }
-      }
-      umma_commit(mbar);
-    }
-    // one warp polls; the others wait in the barrier
-    const int warp = tid >> 5, lane = tid & 31;
-    bool done = true;
-    if (warp == 0) done = mbar_wait_bounded(mbar, 0);
-    done = __syncthreads_and(done) != 0;
-    tc_fence_after();
-    int *acc = reinterpret_cast<int *>(sm + lo.eng);
-    if (done) {
-#pragma unroll
-      for (int hh = 0; hh < 2; hh++) {
-#pragma unroll
-        for (int cc = 0; cc < NU; cc += 16) {
-          uint32_t r[16];
-          tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + hh * NU + cc, r);
-          const int row = 128 * hh + 32 * warp + lane;
-#pragma unroll
-          for (int c = 0; c < 16; c++) acc[(cc + c) * 256 + row] = __float2int_rn(__uint_as_float(r[c]));
-        }
-      }
-    } else if (tid == 0 && a.err) {
-      atomicOr(a.err, 2);  // the tensor core did not signal completion in time
-    }
-    tc_fence_before();
-    __syncthreads();
-    if (tid < 32) tmem_dealloc(tmem, kTmemCols);
-  } else {
   // 4. Toeplitz copy 0: srev word u = byte-reversed encoded word 63-u; the
   //    second half is its negation
   for (int idx = tid; idx < L * 130; idx += C::NT) {
@@ -348,12 +253,11 @@ __global__ void __launch_bounds__(128, (Q >= 4 ? 3 : 4)) k_cpa_tc(CpaArgs a, TcL
 
   // 5. MMAs -> int32 accumulators (aliasing the operands)
   tc_engine_v2<FORM, Q, 4>(tz, colw, L, ncols, reinterpret_cast<int *>(sm + lo.eng));
-  }
   __syncthreads();
   const int *acc = reinterpret_cast<const int *>(sm + lo.eng);
 
   // 6. epilogues on groups of eight coefficients
-  constexpr int WS = FORM == kFp8TC ? 3 : (FORM == kFp8Tcgen05 ? 4 : 8);  // digit weight 2^WS
+  constexpr int WS = FORM == kFp8TC ? 3 : 8;  // digit weight 2^WS
   // sum_d 2^(WS d) acc_d (- FP8 bias) for coefficients 8*grp .. 8*grp+7 of poly p
   auto combine8 = [&](int p, int grp, uint32_t (&V)[4]) {
     const int D = p < C::RA ? Da : Db;
@@ -503,23 +407,8 @@ inline int launch_tc(const CpaArgs &a, cudaStream_t s) {
   int smem = lo.total;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (e != cudaSuccess) return (int)e;
-  if (FORM == kFp8Tcgen05) {
-    // at most 512 / kTmemCols resident CTAs per SM, so every CTA's TMEM
-    // allocation succeeds at once: pad the shared memory until no more fit
-    const int cols = Q * 8 <= 16 ? 32 : 64, cap = 512 / cols;
-    for (int it = 0; it < 64; it++) {
-      e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      if (e != cudaSuccess) return (int)e;
-      int nb = 0;
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, smem);
-      if (e != cudaSuccess) return (int)e;
-      if (nb <= cap) break;
-      smem += 2048;
-    }
-  } else {
-    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return (int)e;
-  }
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return (int)e;
   fn<<<a.n, 128, smem, s>>>(a, lo);
   return (int)cudaGetLastError();
 }
