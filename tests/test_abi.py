@@ -52,3 +52,13 @@ def test_context_without_gpu_is_refused(T):
     h = ctypes.c_void_p()
     assert T.lib().tmvp_ctx_create(0, 0, ctypes.byref(h)) == T.ENOTSUP
     assert T.lib().crypto_kem_keypair(None, None) == T.ENOTSUP
+
+
+def test_genmatrix_bytes(T, oracle):
+    """One key's GenMatrix stream is the l x l 13-bit (Saber) or 11-bit (Sable)
+    polynomials GenMatrix unpacks: l * l * eq * 32 bytes; unknown sets give 0."""
+    for s in range(6):
+        p = oracle.params(s)
+        assert T.genmatrix_bytes(s) == p.l * p.l * p.eq * 32
+    assert T.genmatrix_bytes(T.SABER) == 3744
+    assert T.lib().tmvp_genmatrix_bytes(17) == 0
