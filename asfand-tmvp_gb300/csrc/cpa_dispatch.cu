@@ -18,6 +18,8 @@ TMVP_DECL_FORM(int8)
 TMVP_DECL_FORM(cc)
 TMVP_DECL_FORM(sb)
 TMVP_DECL_FORM(f8u)
+TMVP_DECL_FORM(dp2a)
+TMVP_DECL_FORM(tc4)
 #undef TMVP_DECL_FORM
 int cpa_launch_mixed_decrypt(const CpaArgs *, int, const MixTable *, cudaStream_t, int);
 int cpa_launch_mixed_encrypt(const CpaArgs *, int, const MixTable *, cudaStream_t, int);
@@ -28,7 +30,7 @@ int cpa_launch_mixed_matvec(const CpaArgs *, int, const MixTable *, cudaStream_t
 typedef int (*cpa_fn)(const CpaArgs &, cudaStream_t);
 
 int cpa_launch(int form, int op, const CpaArgs &a, void *stream) {
-  static const cpa_fn tab[6][5] = {
+  static const cpa_fn tab[8][5] = {
       {cpa_launch_cc_decrypt, cpa_launch_cc_encrypt, cpa_launch_cc_reenc, cpa_launch_cc_keygen,
        cpa_launch_cc_matvec},
       {cpa_launch_int8_decrypt, cpa_launch_int8_encrypt, cpa_launch_int8_reenc,
@@ -40,8 +42,12 @@ int cpa_launch(int form, int op, const CpaArgs &a, void *stream) {
        cpa_launch_sb_matvec},
       {cpa_launch_f8u_decrypt, cpa_launch_f8u_encrypt, cpa_launch_f8u_reenc, cpa_launch_f8u_keygen,
        cpa_launch_f8u_matvec},
+      {cpa_launch_dp2a_decrypt, cpa_launch_dp2a_encrypt, cpa_launch_dp2a_reenc, cpa_launch_dp2a_keygen,
+       cpa_launch_dp2a_matvec},
+      {cpa_launch_tc4_decrypt, cpa_launch_tc4_encrypt, cpa_launch_tc4_reenc, cpa_launch_tc4_keygen,
+       cpa_launch_tc4_matvec},
   };
-  if (form < 0 || form > 5 || op < 0 || op > 4 || !tab[form][op]) return (int)cudaErrorInvalidValue;
+  if (form < 0 || form > 7 || op < 0 || op > 4 || !tab[form][op]) return (int)cudaErrorInvalidValue;
   return tab[form][op](a, (cudaStream_t)stream);
 }
 

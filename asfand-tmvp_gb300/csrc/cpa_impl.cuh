@@ -33,9 +33,13 @@ struct CpaCfg {
   static constexpr int WARPS = 4;
   static constexpr int RP = R <= 4 ? 4 : 8;
   static constexpr bool TMVP = FORM == kCudaCore;
+  static constexpr bool DP2A = FORM == kDp2a;
+  static constexpr bool TOOM = FORM == kToomCook;
   static constexpr int NPROD = TMVP ? 3 : 1;
   static constexpr int NCOL = TMVP ? 128 : 256;
-  static constexpr int NT = TC ? 32 * WARPS : (TMVP ? 96 : 64);
+  static constexpr int NT = (TC || TOOM) ? 32 * WARPS : ((TMVP || DP2A) ? 96 : 64);
+  // largest |secret| the form multiplies exactly (larger ones set a.err)
+  static constexpr int SMAX = TC ? 7 : (DP2A ? 63 : 128);
 };
 
 struct CpaLayout {
@@ -69,6 +73,11 @@ __host__ __device__ inline CpaLayout cpa_layout(const KemParams &P) {
   if (C::TC) {
     eng = L * C::Q * 8 * kColStride + L * kTzBytesPerPoly;
     if (C::Q * 8 * 256 * 4 > eng) eng = C::Q * 8 * 256 * 4;  // int32 accumulators alias it
+  } else if (C::DP2A) {
+    eng = L * 3 * 64 * 16 + L * 3 * 64 * C::RP * 4 + 3 * C::RP * 128 * 4;
+  } else if (C::TOOM) {
+    eng = L * 7 * kToomSStride * 4 + C::R * L * 7 * kToomPStride * 4;
+    if (C::R * 7 * 128 * 4 > eng) eng = C::R * 7 * 128 * 4;  // products alias the evaluations
   } else {
     eng = L * C::NPROD * 512 * 2 + L * C::NPROD * C::NCOL * C::RP * 2 +
           (C::TMVP ? 3 * C::RP * 128 * 4 : 0);
@@ -133,7 +142,7 @@ __global__ void __launch_bounds__(CpaCfg<FORM, OP, L, Q>::NT) k_cpa(CpaArgs a) {
         int h = P.mu >> 1;
         v = __popc(x & ((1u << h) - 1u)) - __popc(x >> h);
       }
-      if (C::TC && (v > 7 || v < -7)) bad = true;
+      if (C::SMAX < 128 && (v > C::SMAX || v < -C::SMAX)) bad = true;
       sec[idx] = (int16_t)v;
     }
     if (bad && a.err) atomicOr(a.err, 1);
@@ -209,6 +218,79 @@ __global__ void __launch_bounds__(CpaCfg<FORM, OP, L, Q>::NT) k_cpa(CpaArgs a) {
       if (FORM == kFp8TC) v -= 8u * wsum * (uint32_t)accs[row];
       res[p * 256 + row] = (uint16_t)v;
     }
+  } else if (C::DP2A) {
+    uint4 *tb = reinterpret_cast<uint4 *>(sm + lo.eng);
+    uint32_t *wp = reinterpret_cast<uint32_t *>(tb + L * 3 * 64);
+    int *pp = reinterpret_cast<int *>(wp + L * 3 * 64 * C::RP);
+    // public pairs: products 0, 1, 2 take v0 + v1, v1, v0 (v0 = coefficients
+    // 0..127, v1 = 128..255)
+    for (int idx = tid; idx < L * 64 * C::RP; idx += C::NT) {
+      const int r = idx % C::RP, cp = (idx / C::RP) & 63, j = idx / (C::RP * 64);
+      uint32_t a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+      if (r < C::R) {
+        int w;
+        a0 = pub(r, j, 2 * cp, w);
+        a1 = pub(r, j, 2 * cp + 1, w);
+        b0 = pub(r, j, 2 * cp + 128, w);
+        b1 = pub(r, j, 2 * cp + 129, w);
+      }
+      wp[((j * 3 + 0) * 64 + cp) * C::RP + r] = (a0 + b0) | ((a1 + b1) << 16);
+      wp[((j * 3 + 1) * 64 + cp) * C::RP + r] = b0 | (b1 << 16);
+      wp[((j * 3 + 2) * 64 + cp) * C::RP + r] = a0 | (a1 << 16);
+    }
+    __syncthreads();  // sec complete
+    auto se = [&](int j, int i) -> int {
+      return i >= 255 ? (int)sec[j * 256 + i - 255] : -(int)sec[j * 256 + i + 1];
+    };
+    // u[k] = t_p[127 - k]: t_0 = T00, t_1 = T01 - T00, t_2 = T00 - T10
+    auto u = [&](int j, int p, int k) -> uint32_t {
+      if (k > 254) return 0u;
+      const int x = 127 - k;
+      const int v = p == 0 ? se(j, x + 255)
+                           : (p == 1 ? se(j, x + 127) - se(j, x + 255) : se(j, x + 255) - se(j, x + 383));
+      return (uint32_t)v & 0xffu;
+    };
+    for (int idx = tid; idx < L * 3 * 64; idx += C::NT) {
+      const int w = idx & 63, p = (idx >> 6) % 3, j = idx / 192;
+      uint32_t cw[4];
+#pragma unroll
+      for (int cp = 0; cp < 4; cp++) {
+        const int k = 4 * w + cp;
+        cw[cp] = u(j, p, k) | (u(j, p, k + 1) << 8) | (u(j, p, k + 2) << 16) | (u(j, p, k + 3) << 24);
+      }
+      tb[idx] = make_uint4(cw[0], cw[1], cw[2], cw[3]);
+    }
+    __syncthreads();
+    dp2a_engine<C::RP>(tb, wp, L, C::R, pp, res);
+  } else if (C::TOOM) {
+    uint32_t *sv = reinterpret_cast<uint32_t *>(sm + lo.eng);
+    uint32_t *pv = sv + L * 7 * kToomSStride;
+    // public evaluations
+    for (int idx = tid; idx < C::R * L * 64; idx += C::NT) {
+      const int i = idx & 63, j = (idx >> 6) % L, r = idx / (64 * L);
+      int w;
+      uint32_t e[7];
+      toom4_eval(pub(r, j, i, w), pub(r, j, i + 64, w), pub(r, j, i + 128, w), pub(r, j, i + 192, w), e);
+#pragma unroll
+      for (int pt = 0; pt < 7; pt++) pv[((r * L + j) * 7 + pt) * kToomPStride + i] = e[pt];
+    }
+    // zero margins of the secret evaluations
+    for (int idx = tid; idx < L * 7 * 128; idx += C::NT) {
+      const int x = idx & 127, jp = idx >> 7;
+      sv[jp * kToomSStride + (x < 64 ? x : x + 64)] = 0u;
+    }
+    __syncthreads();  // sec complete
+    for (int idx = tid; idx < L * 64; idx += C::NT) {
+      const int i = idx & 63, j = idx >> 6;
+      const int16_t *sj = sec + j * 256;
+      uint32_t e[7];
+      toom4_eval((uint32_t)(int)sj[i], (uint32_t)(int)sj[i + 64], (uint32_t)(int)sj[i + 128],
+                 (uint32_t)(int)sj[i + 192], e);
+#pragma unroll
+      for (int pt = 0; pt < 7; pt++) sv[(j * 7 + pt) * kToomSStride + 64 + i] = e[pt];
+    }
+    __syncthreads();
+    toom4_engine<C::R>(sv, pv, L, sv, res);
   } else {
     int16_t *tseq = reinterpret_cast<int16_t *>(sm + lo.eng);
     uint16_t *wv = reinterpret_cast<uint16_t *>(tseq + L * C::NPROD * 512);
@@ -340,7 +422,7 @@ inline int tc_q(const CpaArgs &a) {
 
 template <int FORM, int OP, int L>
 inline int launch_q(const CpaArgs &a, cudaStream_t s) {
-  if constexpr (FORM == kCudaCore || FORM == kSchoolbook) {
+  if constexpr (FORM == kCudaCore || FORM == kSchoolbook || FORM == kDp2a || FORM == kToomCook) {
     return launch_one<FORM, OP, L, 1>(a, s);
   } else {
     switch (tc_q<FORM, OP, L>(a)) {

@@ -77,12 +77,15 @@ enum Form : int {
   kFp8TC = 2,
   kAuto = 3,
   kSchoolbook = 4,
-  kFp8Tcgen05 = 5
+  kFp8Tcgen05 = 5,
+  kDp2a = 6,
+  kToomCook = 7
 };
 
 // A form a kernel exists for (kAuto is resolved before launch).
 __host__ __device__ constexpr bool form_valid(int f) {
-  return f == kCudaCore || f == kInt8TC || f == kFp8TC || f == kSchoolbook || f == kFp8Tcgen05;
+  return f == kCudaCore || f == kInt8TC || f == kFp8TC || f == kSchoolbook || f == kFp8Tcgen05 ||
+         f == kDp2a || f == kToomCook;
 }
 
 // Little-endian bit-stream field read from a byte array: bits

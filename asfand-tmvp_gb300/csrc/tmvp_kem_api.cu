@@ -226,13 +226,15 @@ void collect_stage_times(tmvp_ctx *c) {
 }
 
 const char *form_tag(int form, int op) {
-  static const char *names[5][5] = {
+  static const char *names[7][5] = {
       {"cpa_decrypt_cuda_core", "cpa_encrypt_cuda_core", "cpa_reenc_cuda_core", "cpa_keygen_cuda_core", "cpa_matvec_cuda_core"},
       {"cpa_decrypt_int8_tc", "cpa_encrypt_int8_tc", "cpa_reenc_int8_tc", "cpa_keygen_int8_tc", "cpa_matvec_int8_tc"},
       {"cpa_decrypt_fp8_tc", "cpa_encrypt_fp8_tc", "cpa_reenc_fp8_tc", "cpa_keygen_fp8_tc", "cpa_matvec_fp8_tc"},
       {"cpa_decrypt_schoolbook", "cpa_encrypt_schoolbook", "cpa_reenc_schoolbook", "cpa_keygen_schoolbook", "cpa_matvec_schoolbook"},
-      {"cpa_decrypt_fp8_tcgen05", "cpa_encrypt_fp8_tcgen05", "cpa_reenc_fp8_tcgen05", "cpa_keygen_fp8_tcgen05", "cpa_matvec_fp8_tcgen05"}};
-  int f = form == kSchoolbook ? 3 : (form == kFp8Tcgen05 ? 4 : form);
+      {"cpa_decrypt_fp8_tcgen05", "cpa_encrypt_fp8_tcgen05", "cpa_reenc_fp8_tcgen05", "cpa_keygen_fp8_tcgen05", "cpa_matvec_fp8_tcgen05"},
+      {"cpa_decrypt_dp2a", "cpa_encrypt_dp2a", "cpa_reenc_dp2a", "cpa_keygen_dp2a", "cpa_matvec_dp2a"},
+      {"cpa_decrypt_toom_cook", "cpa_encrypt_toom_cook", "cpa_reenc_toom_cook", "cpa_keygen_toom_cook", "cpa_matvec_toom_cook"}};
+  int f = form == kSchoolbook ? 3 : (form == kFp8Tcgen05 ? 4 : (form == kDp2a ? 5 : (form == kToomCook ? 6 : form)));
   return names[f][op];
 }
 

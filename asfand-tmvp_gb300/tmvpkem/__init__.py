@@ -18,9 +18,11 @@ from . import build as _build
 LIGHTSABER, SABER, FIRESABER, LIGHTSABLE, SABLE, FIRESABLE = range(6)
 SET_NAMES = {LIGHTSABER: "LightSaber", SABER: "Saber", FIRESABER: "FireSaber",
              LIGHTSABLE: "LightSable", SABLE: "Sable", FIRESABLE: "FireSable"}
-FORM_CUDA_CORE, FORM_INT8_TC, FORM_FP8_TC, FORM_AUTO, FORM_SCHOOLBOOK, FORM_FP8_TCGEN05 = range(6)
+(FORM_CUDA_CORE, FORM_INT8_TC, FORM_FP8_TC, FORM_AUTO, FORM_SCHOOLBOOK, FORM_FP8_TCGEN05, FORM_DP2A,
+ FORM_TOOM_COOK) = range(8)
 FORM_NAMES = {FORM_CUDA_CORE: "cuda_core", FORM_INT8_TC: "int8_tc", FORM_FP8_TC: "fp8_tc",
-              FORM_AUTO: "auto", FORM_SCHOOLBOOK: "schoolbook", FORM_FP8_TCGEN05: "fp8_tcgen05"}
+              FORM_AUTO: "auto", FORM_SCHOOLBOOK: "schoolbook", FORM_FP8_TCGEN05: "fp8_tcgen05",
+              FORM_DP2A: "dp2a", FORM_TOOM_COOK: "toom_cook"}
 
 OK, EINVAL, ENOMEM, EDEVICE, ETIMEOUT, ENOTSUP = 0, -1, -2, -3, -4, -5
 

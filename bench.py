@@ -11,8 +11,9 @@ checked against the encapsulated one, and a sample against the CPU oracle).
 One step = one tmvp_kem_dec_batch call over the whole batch with device-
 resident inputs (inputs are 222 MB, larger than the 129 MB L2, so no flush is
 needed between steps).  `value` is decaps/s of the FP8 tensor-core form;
-`forms` adds the INT8 tensor-core and CUDA-core TMVP forms timed the same
-way.  `e2e` is the same metric through the public C ABI with pinned HOST
+`forms` adds the other forms timed the same way: the mma.sync FP8 and INT8
+tensor-core forms, and the CUDA-core forms (TMVP with IMAD, TMVP with dp2a,
+Toom-Cook 4-way).  `e2e` is the same metric through the public C ABI with pinned HOST
 buffers (host-to-device copies of ct and sk and the copy of the keys back are
 inside the timed region).  `roofline` is the dominant kernel of the step,
 timed live with CUDA events on its own stream.  `cpu_baseline` is the CPU
@@ -417,7 +418,7 @@ def _workloads(ctx, T, dev, sp, stream, args):
         s8 = (pc[r & 15] - pc[r >> 4]).to(torch.int8).to(dev)
         mv = {}
         ref = None
-        for name, f in forms:
+        for name, f in forms + [("dp2a", T.FORM_DP2A), ("toom_cook", T.FORM_TOOM_COOK)]:
             o = torch.empty((n, l, 256), dtype=torch.int16, device=dev)
             fn = lambda o=o, f=f: ctx.matvec_ptr(n, l, 13, False, o, A, s8, f, sp)
             for _ in range(3):
@@ -553,7 +554,7 @@ def main():
                     help="skip the matrix-vector, Sable and serving workloads")
     ap.add_argument("--workloads", default="matvec,sable,mixed,serving",
                     help="extra workloads to run (comma list of matvec, sable, mixed, serving)")
-    ap.add_argument("--forms", default="fp8_tc,int8_tc,cuda_core",
+    ap.add_argument("--forms", default="fp8_tc,int8_tc,cuda_core,dp2a,toom_cook",
                     help="forms to time besides the headline (AUTO) form (comma list, or 'none')")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -59,14 +59,23 @@ typedef enum {
  *   SCHOOLBOOK    plain negacyclic schoolbook on CUDA cores (reference mode 2)
  *   FP8_TCGEN05   TMVP on the 5th-generation tensor cores (tcgen05.mma,
  *                 operands in shared memory, accumulator in tensor memory):
- *                 e4m3 secrets x radix-16 digits, f32 accumulate, exact */
+ *                 e4m3 secrets x radix-16 digits, f32 accumulate, exact
+ *   DP2A          TMVP on CUDA cores with dp2a (two 16-bit x 8-bit products
+ *                 per instruction), the DPSaber form of the reference's unused
+ *                 DoDP4Av7 kernels (SABER poly.cu:32-224); secrets |s| <= 63
+ *   TOOM_COOK     Toom-Cook 4-way on CUDA cores (the reference's pol_mul,
+ *                 TMVP_SABLE pack.cu:505-732): seven 64x64 products per
+ *                 polynomial pair, accumulated over the module index before
+ *                 one interpolation */
 typedef enum {
   TMVP_FORM_CUDA_CORE = 0,
   TMVP_FORM_INT8_TC = 1,
   TMVP_FORM_FP8_TC = 2,
   TMVP_FORM_AUTO = 3,
   TMVP_FORM_SCHOOLBOOK = 4,
-  TMVP_FORM_FP8_TCGEN05 = 5
+  TMVP_FORM_FP8_TCGEN05 = 5,
+  TMVP_FORM_DP2A = 6,
+  TMVP_FORM_TOOM_COOK = 7
 } tmvp_form;
 
 enum {

@@ -50,6 +50,7 @@ def lib():
         L.orc_unpack_bits.argtypes = [P, P, ctypes.c_int, ctypes.c_int]
         L.orc_polmul_schoolbook.argtypes = [P, P, P]
         L.orc_polmul_tmvp2.argtypes = [P, P, P]
+        L.orc_polmul_toom4.argtypes = [P, P, P]
         L.orc_matvec_batch.argtypes = [ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        P, P, P, ctypes.c_int]
         L.orc_indcpa_keypair.argtypes = [ctypes.c_int, P, P, P, P]
@@ -136,7 +137,8 @@ def polmul(a: np.ndarray, b: np.ndarray, method: str = "schoolbook") -> np.ndarr
     a = np.ascontiguousarray(a, dtype=np.uint16)
     b = np.ascontiguousarray(b, dtype=np.uint16)
     r = np.zeros(256, np.uint16)
-    fn = lib().orc_polmul_schoolbook if method == "schoolbook" else lib().orc_polmul_tmvp2
+    fn = {"schoolbook": lib().orc_polmul_schoolbook, "tmvp2": lib().orc_polmul_tmvp2,
+          "toom4": lib().orc_polmul_toom4}[method]
     fn(_p(r), _p(a), _p(b))
     return r
 

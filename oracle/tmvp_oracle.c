@@ -300,6 +300,69 @@ void orc_polmul_tmvp2(uint16_t r[256], const uint16_t a[256], const uint16_t b[2
 #undef TOEP
 }
 
+/* Toom-Cook 4-way: TMVP_SABLE pack.cu:505-732 (toom_cook_4way, pol_mul)
+ * evaluates the four 64-coefficient quarters of each operand at the seven
+ * points 0, 1, -1, 1/2, -1/2, 2 and infinity (the half points scaled by 8),
+ * multiplies pointwise (there with two levels of Karatsuba, here with
+ * schoolbook) and interpolates.  This restatement works mod 2^32: the
+ * interpolation's exact divisions by 2 and 4 are shifts and those by 3, 9 and
+ * 15 are products with their inverses mod 2^32, which leaves every
+ * coefficient correct mod 2^29, so the low 16 bits are those of the schoolbook
+ * product.  The interpolation is the one derived in toom4_interp. */
+static void toom4_eval(uint32_t e[7][64], const uint16_t a[256]) {
+  for (int i = 0; i < 64; i++) {
+    uint32_t a0 = a[i], a1 = a[64 + i], a2 = a[128 + i], a3 = a[192 + i];
+    e[0][i] = a0;
+    e[1][i] = a0 + a1 + a2 + a3;
+    e[2][i] = a0 - a1 + a2 - a3;
+    e[3][i] = 8 * a0 + 4 * a1 + 2 * a2 + a3;
+    e[4][i] = 8 * a0 - 4 * a1 + 2 * a2 - a3;
+    e[5][i] = a0 + 2 * a1 + 4 * a2 + 8 * a3;
+    e[6][i] = a3;
+  }
+}
+
+/* w[k] = the product at point k (order 0, 1, -1, 64 c(1/2), 64 c(-1/2), 2,
+ * infinity) -> c[k] = coefficient k of c(y) = sum_k c_k y^k, y = x^64.
+ *   E1 = (w1+w2)/2 = c0+c2+c4+c6        O1 = (w1-w2)/2 = c1+c3+c5
+ *   Eh = (w3+w4)/2 = 64c0+16c2+4c4+c6   V = (w3-w4)/4 = 16c1+4c3+c5
+ *   S = E1-c0-c6 = c2+c4                T = (Eh-64c0-c6)/4 = 4c2+c4
+ *   c2 = (T-S)/3, c4 = S-c2
+ *   U = (w5-c0-4c2-16c4-64c6)/2 = c1+4c3+16c5
+ *   D = (V-U)/15 = c1-c5                Sm = (V+U-8 O1)/9 = c1+c5
+ *   c1 = (Sm+D)/2, c5 = Sm-c1, c3 = O1-Sm */
+static void toom4_interp(uint32_t c[7], const uint32_t w[7]) {
+  const uint32_t inv3 = 0xAAAAAAABu, inv9 = 0x38E38E39u, inv15 = 0xEEEEEEEFu;
+  uint32_t c0 = w[0], c6 = w[6];
+  uint32_t e1 = (w[1] + w[2]) >> 1, o1 = (w[1] - w[2]) >> 1;
+  uint32_t eh = (w[3] + w[4]) >> 1, v = (w[3] - w[4]) >> 2;
+  uint32_t sv = e1 - c0 - c6, t = (eh - 64 * c0 - c6) >> 2;
+  uint32_t c2 = (t - sv) * inv3, c4 = sv - c2;
+  uint32_t u = (w[5] - c0 - 4 * c2 - 16 * c4 - 64 * c6) >> 1;
+  uint32_t d = (v - u) * inv15, sm = (v + u - 8 * o1) * inv9;
+  uint32_t c1 = (sm + d) >> 1;
+  c[0] = c0; c[1] = c1; c[2] = c2; c[3] = o1 - sm; c[4] = c4; c[5] = sm - c1; c[6] = c6;
+}
+
+void orc_polmul_toom4(uint16_t r[256], const uint16_t a[256], const uint16_t b[256]) {
+  uint32_t ea[7][64], eb[7][64], w[7][128], full[512];
+  toom4_eval(ea, a);
+  toom4_eval(eb, b);
+  for (int k = 0; k < 7; k++) {
+    for (int i = 0; i < 128; i++) w[k][i] = 0;
+    for (int i = 0; i < 64; i++)
+      for (int m = 0; m < 64; m++) w[k][i + m] += ea[k][i] * eb[k][m];
+  }
+  for (int i = 0; i < 512; i++) full[i] = 0;
+  for (int i = 0; i < 128; i++) {
+    uint32_t wi[7], ci[7];
+    for (int k = 0; k < 7; k++) wi[k] = w[k][i];
+    toom4_interp(ci, wi);
+    for (int k = 0; k < 7; k++) full[64 * k + i] += ci[k];
+  }
+  for (int i = 0; i < 256; i++) r[i] = (uint16_t)(full[i] - full[i + 256]);
+}
+
 /* ------------------------------------------------------------------------ */
 /* Raw matrix-vector product (the TMVP benchmark shape).                     */
 /* ------------------------------------------------------------------------ */

@@ -69,6 +69,7 @@ void orc_unpack_bits(uint16_t *out, const uint8_t *in, int n, int w);
 /* Negacyclic products in Z_{2^16}[x]/(x^256+1). */
 void orc_polmul_schoolbook(uint16_t r[256], const uint16_t a[256], const uint16_t b[256]);
 void orc_polmul_tmvp2(uint16_t r[256], const uint16_t a[256], const uint16_t b[256]);
+void orc_polmul_toom4(uint16_t r[256], const uint16_t a[256], const uint16_t b[256]);
 
 /* Raw matrix-vector product: out[i] = sum_j A[i][j]*s[j] (transpose=0) or
  * sum_j A[j][i]*s[j] (transpose=1), reduced mod 2^eq.  s is int8 per

@@ -8,7 +8,7 @@ from conftest import golden
 
 pytestmark = pytest.mark.gpu
 
-ALL_FORMS = [0, 1, 2, 4, 5]  # cuda_core, int8_tc, fp8_tc, schoolbook, fp8_tcgen05
+ALL_FORMS = [0, 1, 2, 4, 5, 6, 7]  # cuda_core, int8_tc, fp8_tc, schoolbook, fp8_tcgen05, dp2a, toom_cook
 SETS = range(6)
 
 
@@ -50,14 +50,30 @@ def test_matvec_extremes(kem, oracle, form):
     assert np.array_equal(got, oracle.matvec(A, s, eq=eq, nthreads=4))
 
 
-@pytest.mark.parametrize("form", [0, 4])
+@pytest.mark.parametrize("form", [0, 4, 7])
 def test_matvec_wide_secrets_cuda_core(kem, oracle, form):
-    """The CUDA-core forms take any int8 secret."""
+    """The IMAD CUDA-core forms (TMVP, schoolbook, Toom-Cook) take any int8
+    secret."""
     T, ctx = kem
     rng = np.random.default_rng(6)
     A = rng.integers(0, 1 << 13, (8, 3, 3, 256), dtype=np.uint16)
     s = rng.integers(-128, 128, (8, 3, 256)).astype(np.int8)
     assert np.array_equal(ctx.matvec(A, s, eq=13, form=form), oracle.matvec(A, s, eq=13, nthreads=4))
+
+
+def test_matvec_dp2a_limits(kem, oracle):
+    """dp2a multiplies signed bytes of the TMVP operands (differences of two
+    secret coefficients), exact for |s| <= 63: the largest secrets with the
+    largest public values of every width."""
+    T, ctx = kem
+    rng = np.random.default_rng(7)
+    for eq in (13, 11, 10):
+        A = rng.integers(0, 1 << eq, (10, 4, 4, 256), dtype=np.uint16)
+        A[:4] = (1 << eq) - 1
+        s = np.where(rng.integers(0, 2, (10, 4, 256)) == 1, 63, -63).astype(np.int8)
+        s[5:] = rng.integers(-63, 64, (5, 4, 256))
+        got = ctx.matvec(A, s, eq=eq, form=T.FORM_DP2A)
+        assert np.array_equal(got, oracle.matvec(A, s, eq=eq, nthreads=4))
 
 
 @pytest.mark.parametrize("form", ALL_FORMS)
@@ -113,7 +129,7 @@ def test_reference_golden(kem, name, set_id, form):
     assert rej[0].tobytes() == g["rej_ss"].tobytes()
 
 
-@pytest.mark.parametrize("form", [0, 2, 5])
+@pytest.mark.parametrize("form", [0, 2, 5, 6, 7])
 @pytest.mark.parametrize("set_id", [1, 4])
 def test_indcpa_parity(kem, oracle, set_id, form):
     T, ctx = kem
@@ -224,13 +240,17 @@ def test_out_of_range_secret_is_reported(kem):
     A = np.zeros((2, 3, 3, 256), np.uint16)
     s = np.zeros((2, 3, 256), np.int8)
     s[1, 0, 7] = 100
-    for form in (T.FORM_FP8_TC, T.FORM_INT8_TC, T.FORM_FP8_TCGEN05):
+    for form in (T.FORM_FP8_TC, T.FORM_INT8_TC, T.FORM_FP8_TCGEN05, T.FORM_DP2A):
         with pytest.raises(T.TmvpError) as e:
             ctx.matvec(A, s, eq=13, form=form)
         assert e.value.code == T.EINVAL
-    # the CUDA-core form computes it exactly
-    out = ctx.matvec(A, s, eq=13, form=T.FORM_CUDA_CORE)
-    assert not out.any()
+    s[1, 0, 7] = -64
+    with pytest.raises(T.TmvpError):
+        ctx.matvec(A, s, eq=13, form=T.FORM_DP2A)
+    # the IMAD CUDA-core forms compute it exactly
+    for form in (T.FORM_CUDA_CORE, T.FORM_TOOM_COOK):
+        out = ctx.matvec(A, s, eq=13, form=form)
+        assert not out.any()
 
 
 @pytest.mark.parametrize("set_id", [0, 1, 2, 3, 4, 5])

@@ -40,7 +40,7 @@ def test_million_round_trips(kem, oracle):
     assert total >= 1_000_000
 
 
-@pytest.mark.parametrize("form", [0, 1, 2, 5])
+@pytest.mark.parametrize("form", [0, 1, 2, 5, 6, 7])
 def test_matvec_benchmark_size(kem, oracle, form):
     """16384 instances of a 3x3 matrix (uniform mod 2^13) times CBD(mu=8) secrets."""
     import torch

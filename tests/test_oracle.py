@@ -104,6 +104,19 @@ def test_tmvp2_equals_schoolbook(oracle):
     assert r[0] == 65535 and not r[1:].any()
 
 
+def test_toom4_equals_schoolbook(oracle):
+    """The Toom-Cook 4-way restatement (mod 2^32 evaluation and interpolation)
+    gives the schoolbook product mod 2^16 for any 16-bit operands, including
+    the extremes that maximise every evaluation."""
+    rng = np.random.default_rng(4)
+    cases = [(rng.integers(0, 65536, 256, dtype=np.uint16), rng.integers(0, 65536, 256, dtype=np.uint16))
+             for _ in range(10)]
+    cases.append((np.full(256, 65535, np.uint16), np.full(256, 65535, np.uint16)))
+    cases.append((np.full(256, 8191, np.uint16), (-rng.integers(0, 6, 256)).astype(np.uint16)))
+    for a, b in cases:
+        assert np.array_equal(oracle.polmul(a, b), oracle.polmul(a, b, "toom4"))
+
+
 @pytest.mark.parametrize("w", [1, 2, 3, 4, 5, 6, 9, 10, 11, 13])
 def test_pack_roundtrip(oracle, w):
     v = np.random.default_rng(w).integers(0, 1 << w, 256, dtype=np.uint16)
