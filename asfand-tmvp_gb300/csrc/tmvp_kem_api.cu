@@ -59,6 +59,7 @@ struct tmvp_ctx {
   cudaStream_t side = nullptr;          // GenMatrix and H(c) beside the decryption (highest priority)
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   size_t host_chunk = 16384;                       // chunk of host-input decapsulation (0: none)
+  int host_ramp = 2;                               // first chunks host_chunk >> ramp, >> ramp-1, ...
   size_t dev_chunk = 32768;                        // chunk of device-input decapsulation (0: none)
   static constexpr int kLanes = 4;                 // streams for chunk chains
   cudaStream_t lane[kLanes] = {};
@@ -540,6 +541,13 @@ int tmvp_ctx_set_host_chunk(tmvp_ctx *c, size_t n) {
   return set_err(TMVP_OK);
 }
 
+int tmvp_ctx_set_host_ramp(tmvp_ctx *c, int steps) {
+  if (!c || steps < 0 || steps > 4) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->host_ramp = steps;
+  return set_err(TMVP_OK);
+}
+
 int tmvp_ctx_set_dev_chunk(tmvp_ctx *c, size_t n) {
   if (!c || (n != 0 && n < 1024)) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(c->mu);
@@ -770,7 +778,11 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
     // host inputs: chunk k's copies (one copy stream, five input slots) run
     // ahead of the kernels, and chunk k's chain runs on lane k mod 4 (as in
     // dec_lanes, each lane with its own scratch and Keccak-front stream), so
-    // consecutive chunks' chains overlap
+    // consecutive chunks' chains overlap.  The kernels are slower than the
+    // host link, so the call lasts about (first chunk's copy) + (the kernels
+    // of the whole batch): the first host_ramp chunks are host_chunk >>
+    // host_ramp, >> host_ramp - 1, ..., which starts the kernels early while
+    // later chunks stay large enough to fill the GPU.
     constexpr int NL = tmvp_ctx::kLanes, NS = tmvp_ctx::kSlots;
     const size_t cn = c->host_chunk;
     const size_t inb = up(cn * P.ct_bytes) + up(cn * P.sk_bytes);
@@ -786,7 +798,8 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
     TRY_CUDA(cudaEventRecord(c->fork_ev, s));
     for (int l = 0; l < tmvp_ctx::kLanes; l++) TRY_CUDA(cudaStreamWaitEvent(c->lane[l], c->fork_ev, 0));
     for (size_t off = 0, k = 0, m = 0; off < n; off += m, k++) {
-      m = std::min(cn, n - off);
+      const size_t ck = k < (size_t)c->host_ramp ? std::max<size_t>(cn >> (c->host_ramp - k), 256) : cn;
+      m = std::min(ck, n - off);
       const int sl = (int)(k % NS), ln = (int)(k % NL);
       cudaStream_t ls = c->lane[ln];
       uint8_t *ct_k = bct.host ? slot_in[sl] : bct.dev + off * P.ct_bytes;

@@ -116,6 +116,7 @@ def lib(build_if_missing: bool = False):
         getattr(L, nm).restype = None
     L.tmvp_ctx_reserve.argtypes = [P, S]
     L.tmvp_ctx_set_host_chunk.argtypes = [P, S]
+    L.tmvp_ctx_set_host_ramp.argtypes = [P, ctypes.c_int]
     L.tmvp_ctx_set_dev_chunk.argtypes = [P, S]
     L.tmvp_kem_dec_batch_noalloc.argtypes = [I, S, P, P, P, I, P]
     L.tmvp_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]
@@ -339,6 +340,10 @@ class Context:
 
     def set_host_chunk(self, n: int):
         _check(lib().tmvp_ctx_set_host_chunk(self.h, n), "tmvp_ctx_set_host_chunk")
+
+    def set_host_ramp(self, steps: int):
+        """First chunks of a host-buffer decapsulation: host_chunk >> steps, ..."""
+        _check(lib().tmvp_ctx_set_host_ramp(self.h, steps), "tmvp_ctx_set_host_ramp")
 
     def set_dev_chunk(self, n: int):
         """Chunk size of device-buffer decapsulation chains (0: one chain)."""

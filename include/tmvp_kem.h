@@ -179,10 +179,17 @@ int tmvp_matvec_batch(tmvp_ctx *ctx, size_t n, int l, int eq, int transpose, uin
  * allocate).  Fails with TMVP_ENOMEM above the context's budget. */
 int tmvp_ctx_reserve(tmvp_ctx *ctx, size_t bytes);
 /* Batched decapsulation with host-resident ct / sk copies and processes them
- * in chunks of n instances (two copy streams), so that copies overlap the
- * kernels of the previous chunk; 0 = one copy, then the kernels.  Default
- * 16384; n must be 0 or >= 1024. */
+ * in chunks of n instances (one copy stream running ahead of the kernels), so
+ * that copies overlap the kernels of earlier chunks; 0 = one copy, then the
+ * kernels.  Default 16384; n must be 0 or >= 1024.  Results do not depend
+ * on it. */
 int tmvp_ctx_set_host_chunk(tmvp_ctx *ctx, size_t n);
+/* The first `steps` chunks of such a call are n >> steps, n >> (steps - 1),
+ * ..., n >> 1 instances (at least 256), so that the kernels start after a
+ * short first copy; 0 = all chunks n.  Default 2; 0 <= steps <= 4.  Results
+ * do not depend on it.  No counterpart in the reference (its calls are
+ * synchronous, with the whole batch copied first). */
+int tmvp_ctx_set_host_ramp(tmvp_ctx *ctx, int steps);
 /* Batched decapsulation with device-resident buffers splits batches larger
  * than n into chunks whose decryption / G / re-encryption / final-key chains
  * run on four of the context's streams (joined back into the caller's), so

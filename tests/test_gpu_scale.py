@@ -136,3 +136,39 @@ def test_chunked_device_decapsulation(kem, chunk):
         ctx.set_dev_chunk(32768)
     assert torch.equal(out[:n - 5], ss[:n - 5]) and torch.equal(out[n - 4:], ss[n - 4:])
     assert not torch.equal(out[n - 5], ss[n - 5])
+
+
+@pytest.mark.parametrize("chunk,ramp", [(1024, 4), (4096, 2), (16384, 0), (16384, 3), (0, 0)])
+def test_chunked_host_decapsulation(kem, chunk, ramp):
+    """Host buffers run as copy-ahead chunks (ramped first chunks, five input
+    slots, four lanes); every schedule, including more chunks than slots and
+    a ragged last chunk, gives the encapsulation's keys and rejects a
+    tampered ciphertext in the last chunk."""
+    import torch
+    T, ctx = kem
+    dev = torch.device("cuda", 0)
+    n = 40000
+    z = T.sizes(T.SABER)
+    coins = torch.from_numpy(T.splitmix_bytes(43, n * 96).reshape(n, 96)).to(dev)
+    ec = torch.from_numpy(T.splitmix_bytes(44, n * 32).reshape(n, 32)).to(dev)
+    pk = torch.empty((n, z.pk_bytes), dtype=torch.uint8, device=dev)
+    sk = torch.empty((n, z.sk_bytes), dtype=torch.uint8, device=dev)
+    ct = torch.empty((n, z.ct_bytes), dtype=torch.uint8, device=dev)
+    ss = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+    ctx.kem_keypair_ptr(T.SABER, n, pk, sk, coins)
+    ctx.kem_enc_ptr(T.SABER, n, ct, ss, pk, ec)
+    ct[n - 3, 7] ^= 1
+    torch.cuda.synchronize()
+    ct_h, sk_h = ct.cpu().pin_memory(), sk.cpu().pin_memory()
+    out = torch.zeros((n, 32), dtype=torch.uint8).pin_memory()
+    try:
+        ctx.set_host_chunk(chunk)
+        ctx.set_host_ramp(ramp)
+        ctx.kem_dec_ptr(T.SABER, n, out, ct_h, sk_h)
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_host_chunk(16384)
+        ctx.set_host_ramp(2)
+    ss_h = ss.cpu()
+    assert torch.equal(out[:n - 3], ss_h[:n - 3]) and torch.equal(out[n - 2:], ss_h[n - 2:])
+    assert not torch.equal(out[n - 3], ss_h[n - 3])
