@@ -58,8 +58,9 @@ struct tmvp_ctx {
   uint64_t launches = 0;
   cudaStream_t side = nullptr;          // GenMatrix and H(c) beside the decryption (highest priority)
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  cudaEvent_t gm_ev = nullptr;                     // whole-batch GenMatrix of a host-input call
   size_t host_chunk = 16384;                       // chunk of host-input decapsulation (0: none)
-  int host_ramp = 2;                               // first chunks host_chunk >> ramp, >> ramp-1, ...
+  int host_ramp = 1;                               // first chunks host_chunk >> ramp, >> ramp-1, ...
   size_t dev_chunk = 32768;                        // chunk of device-input decapsulation (0: none)
   static constexpr int kLanes = 4;                 // streams for chunk chains
   cudaStream_t lane[kLanes] = {};
@@ -143,6 +144,18 @@ bool is_device_ptr(const void *p, int device) {
   }
   return (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) &&
          at.device == device;
+}
+
+// Device address of host memory that kernels may read in place (pinned and
+// mapped into the device's address space), or nullptr.
+const uint8_t *mapped_host_ptr(const void *p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  return (const uint8_t *)at.devicePointer;
 }
 
 Buf classify(const void *p, size_t bytes, int device) {
@@ -325,7 +338,8 @@ DecScratch dec_scratch(const KemParams &P, size_t n, Arena &A) {
 // s; the re-encryption and the final key wait for it.
 int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const uint8_t *ct,
                  const uint8_t *sk, int form, cudaStream_t s, const DecScratch &w, bool fork = true,
-                 cudaStream_t side = nullptr, const uint8_t *a_cached = nullptr) {
+                 cudaStream_t side = nullptr, const uint8_t *a_cached = nullptr,
+                 cudaEvent_t a_ready = nullptr) {
   int r;
   if (!side) side = c->side;
   if (fork) {
@@ -356,6 +370,7 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   }
   c->launches++;
   TRY_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));  // join: GenMatrix
+  if (a_ready) TRY_CUDA(cudaStreamWaitEvent(s, a_ready, 0));  // a_cached written on another stream
   CpaArgs b{};
   b.P = P;
   b.n = (int)n;
@@ -477,6 +492,7 @@ int tmvp_ctx_create(int device, size_t mem_budget, tmvp_ctx **out) {
       cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, pri_high) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->gm_ev, cudaEventDisableTiming) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->copy[0], cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->copy[1], cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
@@ -516,6 +532,7 @@ void tmvp_ctx_destroy(tmvp_ctx *c) {
     if (c->side) cudaStreamDestroy(c->side);
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->join_ev) cudaEventDestroy(c->join_ev);
+    if (c->gm_ev) cudaEventDestroy(c->gm_ev);
     for (int i = 0; i < tmvp_ctx::kLanes; i++) {
       if (c->lane[i]) cudaStreamDestroy(c->lane[i]);
       if (c->lane_side[i]) cudaStreamDestroy(c->lane_side[i]);
@@ -787,8 +804,22 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
     const size_t cn = c->host_chunk;
     const size_t inb = up(cn * P.ct_bytes) + up(cn * P.sk_bytes);
     size_t need = NL * dec_ws_bytes(P, cn) + NS * inb + (bss.host ? NL * up(cn * 32) : 0);
+    // GenMatrix needs only the 32-byte seed of each key.  Where the kernels
+    // can read sk in place (device memory, or pinned host memory mapped into
+    // the device's address space, with 8-byte-aligned seeds), GenMatrix of
+    // the whole batch runs first, at full occupancy while ct and sk stream
+    // in, and each chunk's chain is the cached-A chain (H(c), decryption, G,
+    // re-encryption, final key).  Otherwise each chunk expands its own.
+    const size_t seed_off = P.indcpa_sk_bytes + (size_t)P.l * P.polycompbytes;
+    const uint8_t *sk_seed = bsk.host ? mapped_host_ptr(bsk.user) : bsk.dev;
+    if (sk_seed && (((uintptr_t)sk_seed | seed_off | P.sk_bytes) & 7) != 0) sk_seed = nullptr;
+    if (sk_seed && ensure_ws(c, need + up(n * P.gm_bytes)) == TMVP_OK)
+      need += up(n * P.gm_bytes);
+    else
+      sk_seed = nullptr;
     if ((r = ensure_ws(c, need))) return set_err(r);
     Arena A{c->ws};
+    uint8_t *a_full = sk_seed ? A.take(n * P.gm_bytes) : nullptr;
     DecScratch w[NL];
     uint8_t *slot_in[NS], *ss_stage[NL] = {};
     for (int l = 0; l < NL; l++) w[l] = dec_scratch(P, cn, A);
@@ -797,6 +828,16 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
       for (int l = 0; l < NL; l++) ss_stage[l] = A.take(cn * 32);
     TRY_CUDA(cudaEventRecord(c->fork_ev, s));
     for (int l = 0; l < tmvp_ctx::kLanes; l++) TRY_CUDA(cudaStreamWaitEvent(c->lane[l], c->fork_ev, 0));
+    if (a_full) {
+      TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+      {
+        StageTimer tm_(c, "genmatrix", c->side);
+        k_genmatrix<<<blocks_for(n, kHashBlock), kHashBlock, 0, c->side>>>(P, sk_seed + P.indcpa_sk_bytes,
+                                                                           P.sk_bytes, a_full, (int)n);
+      }
+      c->launches++;
+      TRY_CUDA(cudaEventRecord(c->gm_ev, c->side));
+    }
     for (size_t off = 0, k = 0, m = 0; off < n; off += m, k++) {
       const size_t ck = k < (size_t)c->host_ramp ? std::max<size_t>(cn >> (c->host_ramp - k), 256) : cn;
       m = std::min(ck, n - off);
@@ -820,7 +861,8 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
       TRY_CUDA(cudaEventRecord(c->ev_loaded[sl][0], c->copy[0]));
       TRY_CUDA(cudaStreamWaitEvent(ls, c->ev_loaded[sl][0], 0));
       uint8_t *ss_k = bss.host ? ss_stage[ln] : bss.dev + off * 32;
-      if ((r = dec_pipeline(c, P, m, ss_k, ct_k, sk_k, form, ls, w[ln], true, c->lane_side[ln])))
+      if ((r = dec_pipeline(c, P, m, ss_k, ct_k, sk_k, form, ls, w[ln], true, c->lane_side[ln],
+                            a_full ? a_full + off * P.gm_bytes : nullptr, a_full ? c->gm_ev : nullptr)))
         return set_err(r);
       TRY_CUDA(cudaEventRecord(c->ev_free[sl], ls));
       if (bss.host)

@@ -385,7 +385,7 @@ def _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws):
         if best is None or statistics.mean(e2e_ms) < statistics.mean(best[0]):
             best = (e2e_ms, e2e_exact, f"{chunk}/{ramp}")
     ctx.set_host_chunk(16384)
-    ctx.set_host_ramp(2)
+    ctx.set_host_ramp(1)
     e2e_ms, e2e_exact, chunk = best
     return e2e_ms, e2e_exact, ws * n / (statistics.mean(e2e_ms) / 1e3), (chunk, sweep)
 

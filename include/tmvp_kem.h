@@ -186,7 +186,7 @@ int tmvp_ctx_reserve(tmvp_ctx *ctx, size_t bytes);
 int tmvp_ctx_set_host_chunk(tmvp_ctx *ctx, size_t n);
 /* The first `steps` chunks of such a call are n >> steps, n >> (steps - 1),
  * ..., n >> 1 instances (at least 256), so that the kernels start after a
- * short first copy; 0 = all chunks n.  Default 2; 0 <= steps <= 4.  Results
+ * short first copy; 0 = all chunks n.  Default 1; 0 <= steps <= 4.  Results
  * do not depend on it.  No counterpart in the reference (its calls are
  * synchronous, with the whole batch copied first). */
 int tmvp_ctx_set_host_ramp(tmvp_ctx *ctx, int steps);

@@ -138,12 +138,15 @@ def test_chunked_device_decapsulation(kem, chunk):
     assert not torch.equal(out[n - 5], ss[n - 5])
 
 
-@pytest.mark.parametrize("chunk,ramp", [(1024, 4), (4096, 2), (16384, 0), (16384, 3), (0, 0)])
-def test_chunked_host_decapsulation(kem, chunk, ramp):
+@pytest.mark.parametrize("chunk,ramp,pinned", [(1024, 4, True), (4096, 2, True), (16384, 0, True),
+                                               (16384, 3, True), (0, 0, True), (4096, 2, False)])
+def test_chunked_host_decapsulation(kem, chunk, ramp, pinned):
     """Host buffers run as copy-ahead chunks (ramped first chunks, five input
-    slots, four lanes); every schedule, including more chunks than slots and
-    a ragged last chunk, gives the encapsulation's keys and rejects a
-    tampered ciphertext in the last chunk."""
+    slots, four lanes; with pinned buffers GenMatrix of the whole batch runs
+    first from the seeds read in place, with pageable ones each chunk expands
+    its own); every schedule, including more chunks than slots and a ragged
+    last chunk, gives the encapsulation's keys and rejects a tampered
+    ciphertext in the last chunk."""
     import torch
     T, ctx = kem
     dev = torch.device("cuda", 0)
@@ -159,8 +162,10 @@ def test_chunked_host_decapsulation(kem, chunk, ramp):
     ctx.kem_enc_ptr(T.SABER, n, ct, ss, pk, ec)
     ct[n - 3, 7] ^= 1
     torch.cuda.synchronize()
-    ct_h, sk_h = ct.cpu().pin_memory(), sk.cpu().pin_memory()
-    out = torch.zeros((n, 32), dtype=torch.uint8).pin_memory()
+    ct_h, sk_h = ct.cpu(), sk.cpu()
+    out = torch.zeros((n, 32), dtype=torch.uint8)
+    if pinned:
+        ct_h, sk_h, out = ct_h.pin_memory(), sk_h.pin_memory(), out.pin_memory()
     try:
         ctx.set_host_chunk(chunk)
         ctx.set_host_ramp(ramp)
@@ -168,7 +173,7 @@ def test_chunked_host_decapsulation(kem, chunk, ramp):
         torch.cuda.synchronize()
     finally:
         ctx.set_host_chunk(16384)
-        ctx.set_host_ramp(2)
+        ctx.set_host_ramp(1)
     ss_h = ss.cpu()
     assert torch.equal(out[:n - 3], ss_h[:n - 3]) and torch.equal(out[n - 2:], ss_h[n - 2:])
     assert not torch.equal(out[n - 3], ss_h[n - 3])
