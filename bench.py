@@ -72,7 +72,9 @@ def _dist():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 25 ms, each sample
+    stamped with the host clock, so that the ones taken inside the timed
+    region can be told apart."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -80,7 +82,7 @@ class ClockSampler:
 
     def __init__(self, gpu_id: str | None):
         self.rows, self.proc = [], None
-        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "25"]
         if gpu_id:
             cmd += ["-i", gpu_id]
         try:
@@ -94,9 +96,16 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) == 7:
-                self.rows.append(parts)
+                self.rows.append((time.perf_counter(), parts))
 
-    def stop(self):
+    def wait_started(self, timeout: float = 3.0):
+        """Block until the first sample arrived (nvidia-smi takes a while to start)."""
+        t_end = time.perf_counter() + timeout
+        while self.proc and not self.rows and time.perf_counter() < t_end:
+            time.sleep(0.01)
+
+    def stop(self, t0: float | None = None, t1: float | None = None):
+        """Stats over the samples stamped in [t0, t1] (all samples if none fell there)."""
         if self.proc:
             self.proc.terminate()
             try:
@@ -105,12 +114,15 @@ class ClockSampler:
                 self.proc.kill()
         if not self.rows:
             return None
-        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        inside = [r for t, r in self.rows if t0 is not None and t0 <= t <= t1]
+        rows = inside or [r for _, r in self.rows]
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i] == "Active"})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i] == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows), "samples_in_timed_region": len(inside),
+                "samples_total": len(self.rows)}
 
 
 def cpu_decaps_rate(n: int, nthreads: int, seed: int = 99):
@@ -202,6 +214,8 @@ def run_ours(args):
     # launch shapes for this workload, picked by the library's autotuner
     tuned = {} if args.no_tune else {"saber": ctx.autotune(SABER, n)}
 
+    window = [None, None]  # host clock around the timed region
+
     def timed(form, steps, stage_timing=False):
         for _ in range(args.warmup):
             ctx.kem_dec_ptr(SABER, n, ss, ct, sk, form, sp)
@@ -211,11 +225,13 @@ def run_ours(args):
         l0 = ctx.launches
         barrier()
         torch.cuda.synchronize()
+        window[0] = time.perf_counter()
         ev[0].record(stream)
         for k in range(steps):
             ctx.kem_dec_ptr(SABER, n, ss, ct, sk, form, sp)
             ev[k + 1].record(stream)
         torch.cuda.synchronize()
+        window[1] = time.perf_counter()
         barrier()
         launches = ctx.launches - l0
         per = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
@@ -232,8 +248,9 @@ def run_ours(args):
     except Exception:
         pass
     sampler = ClockSampler(gpu_id)
+    sampler.wait_started()
     total_ms, per_ms, launches, stages, exact_main = timed(T.FORM_AUTO, args.steps, stage_timing=True)
-    clocks = sampler.stop()
+    clocks = sampler.stop(window[0], window[1])
     if ws > 1:
         import torch.distributed as dist
         t = torch.tensor([total_ms], device=dev)
@@ -544,7 +561,7 @@ def _ncu_traffic(kernel: str):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=BATCH)
