@@ -122,7 +122,12 @@ int ensure_ws(tmvp_ctx *c, size_t bytes) {
     c->ws = nullptr;
     c->ws_cap = 0;
   }
-  TRY_CUDA(cudaMalloc(&c->ws, cap));
+  cudaError_t e = cudaMalloc(&c->ws, cap);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // report it here, not from the next call's error check
+    c->ws = nullptr;
+    return cuda_err(e);
+  }
   c->ws_cap = cap;
   return TMVP_OK;
 }
@@ -311,6 +316,9 @@ struct Guard {
 // context's host_chunk instances, default below), so that the copy of one
 // chunk overlaps the kernels of the previous one.
 constexpr size_t kHostChunk = 16384;
+// Largest whole-batch GenMatrix buffer a host-input decapsulation expands
+// ahead of its chunks (1M Saber instances take 3.6 GiB).
+constexpr size_t kGmFirstBytes = size_t(4) << 30;
 
 // Intermediate buffers of one decapsulation pass over n instances.
 struct DecScratch {
@@ -813,10 +821,13 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
     const size_t seed_off = P.indcpa_sk_bytes + (size_t)P.l * P.polycompbytes;
     const uint8_t *sk_seed = bsk.host ? mapped_host_ptr(bsk.user) : bsk.dev;
     if (sk_seed && (((uintptr_t)sk_seed | seed_off | P.sk_bytes) & 7) != 0) sk_seed = nullptr;
-    if (sk_seed && ensure_ws(c, need + up(n * P.gm_bytes)) == TMVP_OK)
+    // (up to kGmFirstBytes of GenMatrix streams; larger batches, or a
+    // workspace that cannot grow, keep the per-chunk GenMatrix)
+    if (sk_seed && up(n * P.gm_bytes) <= kGmFirstBytes && ensure_ws(c, need + up(n * P.gm_bytes)) == TMVP_OK) {
       need += up(n * P.gm_bytes);
-    else
+    } else {
       sk_seed = nullptr;
+    }
     if ((r = ensure_ws(c, need))) return set_err(r);
     Arena A{c->ws};
     uint8_t *a_full = sk_seed ? A.take(n * P.gm_bytes) : nullptr;

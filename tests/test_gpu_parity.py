@@ -286,3 +286,21 @@ def test_cached_genmatrix_matches_plain_calls(kem, set_id):
     good = torch.ones(n, dtype=torch.bool, device=dev)
     good[7] = False
     assert torch.equal(d2[good], ss1[good]) and not torch.equal(d2[7], ss1[7])
+
+
+def test_failed_workspace_allocation_leaves_context_usable(kem, oracle):
+    """A workspace request the GPU cannot hold (2 TiB, refused by cudaMalloc
+    without allocating anything) returns ENOMEM, and the next calls on the
+    same context succeed and match the oracle: the failed allocation is
+    reported once, not again by a later call."""
+    import ctypes
+    T, ctx = kem
+    rc = T.lib().tmvp_ctx_reserve(ctx.h, ctypes.c_size_t(1 << 41))
+    assert rc == T.ENOMEM
+    n = 4
+    coins = _coins(91, n, 96)
+    pk, sk = ctx.kem_keypair(T.SABER, coins)
+    opk, osk = oracle.kem_keypair_batch(T.SABER, coins)
+    assert np.array_equal(pk, opk) and np.array_equal(sk, osk)
+    ct, ss = ctx.kem_enc(T.SABER, pk, _coins(92, n, 32))
+    assert np.array_equal(ctx.kem_dec(T.SABER, ct, sk), ss)
