@@ -142,8 +142,10 @@ int alloc_slot(Slot &s, int device, int mb) {
       cudaMalloc(&s.d_out, (size_t)mb * (kMaxCt + 32)) != cudaSuccess ||
       cudaMalloc(&s.d_key, (size_t)mb * kMaxSk) != cudaSuccess ||
       cudaMalloc(&s.d_idx, (size_t)mb * 4) != cudaSuccess ||
-      cudaMalloc(&s.d_a, (size_t)mb * kMaxGm) != cudaSuccess)
+      cudaMalloc(&s.d_a, (size_t)mb * kMaxGm) != cudaSuccess) {
+    cudaGetLastError();  // reported here, not by a later call's error check
     return TMVP_ENOMEM;
+  }
   s.batch.reserve(mb);
   return TMVP_OK;
 }
@@ -380,6 +382,7 @@ int tmvp_server_add_keys(tmvp_server *S, tmvp_param_set set, size_t n, const uin
         cudaMalloc(&na, cap * P.gm_bytes) != cudaSuccess) {
       if (npk) cudaFree(npk);
       if (nsk) cudaFree(nsk);
+      cudaGetLastError();  // reported here, not by a later call's error check
       cudaSetDevice(prev);
       return TMVP_ENOMEM;
     }

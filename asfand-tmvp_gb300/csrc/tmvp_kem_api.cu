@@ -1454,7 +1454,10 @@ struct DevBufs {
   }
   uint8_t *get(size_t bytes) {
     void *p = nullptr;
-    if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+      cudaGetLastError();  // the caller reports TMVP_ENOMEM
+      return nullptr;
+    }
     ptrs.push_back(p);
     return static_cast<uint8_t *>(p);
   }
