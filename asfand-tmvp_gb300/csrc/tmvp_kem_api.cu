@@ -1238,13 +1238,18 @@ int mixed_check(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr) {
 
 // Device bytes of the group tables of one pass: two CPA tables (decryption,
 // re-encryption) and the Keccak-stage table.
+// Group tables of a mixed pass: per parameter set, one decryption and one
+// re-encryption table of that set's groups, then the hash groups.
+constexpr int kNumSets = 6;
 size_t mixed_tab_bytes(size_t ng) {
-  return 2 * up(mix_table_bytes()) + up(ng * sizeof(HashGroup));
+  return 2 * kNumSets * up(mix_table_bytes()) + up(ng * sizeof(HashGroup));
 }
 
-// Enqueues one mixed decapsulation pass on s: every stage is one launch over
-// all groups (GenMatrix, then H(c), on the side stream; decryption, G,
-// re-encryption and the final key on s).  ws: mixed_ws_bytes of device
+// Enqueues one mixed decapsulation pass on s: the Keccak stages are one
+// launch over all groups (GenMatrix and H(c) on the side stream; G and the
+// final key on s), the decryption and the re-encryption one launch per
+// parameter set present, each sized for its set and shaped as the autotuner
+// chose for it.  ws: mixed_ws_bytes of device
 // memory; tabs: mixed_tab_bytes of device memory for the group tables, which
 // are built into host_tabs and, if upload_tabs, copied on s.  Makes no
 // allocation and no host synchronisation, so it can be captured into a graph.
@@ -1254,8 +1259,6 @@ int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws,
   std::vector<HashGroup> hg(ng);
   Arena A{ws};
   int total = 0;
-  bool persist_dec = true, persist_re = true;
-  int shape_dec = 0, shape_re = 0;
   for (size_t g = 0; g < ng; g++) {
     KemParams P;
     make_params(gr[g].set, &P);
@@ -1298,36 +1301,50 @@ int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws,
     b.ct = gr[g].ct;
     b.fail = h.fail;
     b.err = c->d_err;
-    // the persistent kernel only where the autotuner chose it for every set
-    const int sd = persist_ctas_per_sm(kDecrypt, P.set), sr = persist_ctas_per_sm(kReenc, P.set);
-    persist_dec = persist_dec && sd >= 0;
-    persist_re = persist_re && sr >= 0;
-    shape_dec = std::max(shape_dec, sd);
-    shape_re = std::max(shape_re, sr);
+  }
+  // the groups of each parameter set, for the per-set IND-CPA launches
+  std::vector<CpaArgs> sa[kNumSets], sb[kNumSets];
+  for (size_t g = 0; g < ng; g++) {
+    sa[ga[g].P.set].push_back(ga[g]);
+    sb[gb[g].P.set].push_back(gb[g]);
   }
   const size_t tb = up(mix_table_bytes());
   host_tabs.assign(mixed_tab_bytes(ng), 0);
-  mix_table_build(host_tabs.data(), ga.data(), (int)ng);
-  mix_table_build(host_tabs.data() + tb, gb.data(), (int)ng);
-  std::memcpy(host_tabs.data() + 2 * tb, hg.data(), ng * sizeof(HashGroup));
+  for (int st = 0; st < kNumSets; st++) {
+    if (sa[st].empty()) continue;
+    mix_table_build(host_tabs.data() + st * tb, sa[st].data(), (int)sa[st].size());
+    mix_table_build(host_tabs.data() + (kNumSets + st) * tb, sb[st].data(), (int)sb[st].size());
+  }
+  std::memcpy(host_tabs.data() + 2 * kNumSets * tb, hg.data(), ng * sizeof(HashGroup));
   // (pageable source: the call returns once the bytes are staged)
   if (upload_tabs) TRY_CUDA(cudaMemcpyAsync(tabs, host_tabs.data(), host_tabs.size(), cudaMemcpyHostToDevice, s));
-  const MixTable *tdec = reinterpret_cast<const MixTable *>(tabs);
-  const MixTable *tre = reinterpret_cast<const MixTable *>(tabs + tb);
-  const HashGroup *th = reinterpret_cast<const HashGroup *>(tabs + 2 * tb);
+  auto tdec = [&](int st) { return reinterpret_cast<const MixTable *>(tabs + st * tb); };
+  auto tre = [&](int st) { return reinterpret_cast<const MixTable *>(tabs + (kNumSets + st) * tb); };
+  const HashGroup *th = reinterpret_cast<const HashGroup *>(tabs + 2 * kNumSets * tb);
   const unsigned nb = blocks_for((size_t)total, kHashBlock);
   TRY_CUDA(cudaEventRecord(c->fork_ev, s));
   TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
   // GenMatrix and H(c) of every group in one launch (2 total sponges)
   k_mix_front<<<blocks_for(2 * (size_t)total, kHashBlock), kHashBlock, 0, c->side>>>(th, (int)ng, total, 0);
   TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
-  if (cpa_launch_mixed(kDecrypt, ga.data(), (int)ng, tdec, s, persist_dec ? shape_dec : -1) != 0)
-    return TMVP_EDEVICE;
+  int nsets = 0;
+  for (int st = 0; st < kNumSets; st++) {
+    if (sa[st].empty()) continue;
+    nsets++;
+    if (cpa_launch_mixed(kDecrypt, sa[st].data(), (int)sa[st].size(), tdec(st), s,
+                         persist_ctas_per_sm(kDecrypt, st)) != 0)
+      return TMVP_EDEVICE;
+  }
   k_mix_g<<<nb, kHashBlock, 0, s>>>(th, (int)ng, total);
   TRY_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));  // GenMatrix
-  if (cpa_launch_mixed(kReenc, gb.data(), (int)ng, tre, s, persist_re ? shape_re : -1) != 0) return TMVP_EDEVICE;
+  for (int st = 0; st < kNumSets; st++) {
+    if (sb[st].empty()) continue;
+    if (cpa_launch_mixed(kReenc, sb[st].data(), (int)sb[st].size(), tre(st), s,
+                         persist_ctas_per_sm(kReenc, st)) != 0)
+      return TMVP_EDEVICE;
+  }
   k_mix_final<<<nb, kHashBlock, 0, s>>>(th, (int)ng, total);
-  c->launches += 5;
+  c->launches += 3 + 2 * nsets;
   TRY_CUDA(cudaGetLastError());
   return TMVP_OK;
 }

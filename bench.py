@@ -514,7 +514,8 @@ def _workloads(ctx, T, dev, sp, stream, args):
                               "decaps_per_s": total / (ms_graph / 1e3), "ms": ms_graph,
                               "per_request_calls_decaps_per_s": total / (ms_sep / 1e3),
                               "bit_exact": bool(exact),
-                              "launch": "one CUDA graph, five launches: each stage one launch over all 24 requests"}
+                              "launch": "one CUDA graph: the Keccak stages one launch over all 24 requests, "
+                                        "decryption and re-encryption one launch per parameter set"}
     # serving loop: Poisson arrivals over LightSaber, Saber, FireSaber and Sable
     if "serving" in W:
         rate, secs = 200_000.0, 2.0

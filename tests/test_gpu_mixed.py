@@ -1,7 +1,8 @@
-"""Mixed-parameter decapsulation and launch shapes: one persistent launch per
-IND-CPA step over groups of different parameter sets, and its CUDA-graph
-plan, give the same keys as per-set batches (which the parity tests pin to
-the oracle); every launch shape, and the autotuner's choice, stay bit-exact."""
+"""Mixed-parameter decapsulation and launch shapes: a pass over groups of
+different parameter sets (Keccak stages one launch over all groups, each
+IND-CPA step one launch per set present), and its CUDA-graph plan, give the
+same keys as per-set batches (which the parity tests pin to the oracle);
+every launch shape, and the autotuner's choice, stay bit-exact."""
 import numpy as np
 import pytest
 
