@@ -203,7 +203,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
     mbar_init(mbar_mma, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     const uint32_t d = smem_u32(sm);
-    mbar_expect_tx(mbar_in, LO::IN_BYTES);
+    mbar_expect_tx(mbar_in, LO::IN_BYTES + (a.stall_inputs ? 16 : 0));
     if (LO::HAS_AS) {
       bulk_g2s(d + LO::A, a.a_stream + (size_t)inst * C::GM, C::GM, mbar_in);
       bulk_g2s(d + LO::SS, a.s_stream + (size_t)inst * C::GS, C::GS, mbar_in);

@@ -44,6 +44,10 @@ struct CpaArgs {
   uint16_t *mv_out;
   int mv_eq, mv_transpose;
   int *err;           // set when a secret coefficient is outside the form's range
+  // tcgen05 per-instance kernel only, for tmvp_selftest_bounded_wait: the
+  // input barrier expects 16 bytes more than the copies bring, so its
+  // bounded wait runs out (nothing else changes; the copies all land)
+  int stall_inputs;
 };
 
 // Launch over a.n instances on `stream`.  Returns a CUDA error code (0 on

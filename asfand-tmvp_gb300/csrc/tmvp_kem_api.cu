@@ -1378,6 +1378,35 @@ int tmvp_ctx_sync_status(tmvp_ctx *c, void *stream) {
   return set_err(finish(c, (cudaStream_t)stream, true));
 }
 
+int tmvp_selftest_bounded_wait(tmvp_ctx *c, void *stream) {
+  if (!c) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  cudaStream_t st = (cudaStream_t)stream;
+  int r = finish(c, st, true);  // an earlier call's status is that call's, not this test's
+  if (r != TMVP_OK && r != TMVP_EINVAL && r != TMVP_ETIMEOUT) return set_err(r);
+  // one l = 2 matrix-vector instance on the tcgen05 per-instance kernel
+  const size_t a_bytes = 2 * 2 * 256 * 2, s_bytes = 2 * 256, o_bytes = 2 * 256 * 2;
+  if ((r = ensure_ws(c, up(a_bytes) + up(s_bytes) + up(o_bytes)))) return set_err(r);
+  Arena A{c->ws};
+  uint8_t *dA = A.take(a_bytes), *dS = A.take(s_bytes), *dO = A.take(o_bytes);
+  TRY_CUDA(cudaMemsetAsync(dA, 0, a_bytes, st));
+  TRY_CUDA(cudaMemsetAsync(dS, 0, s_bytes, st));
+  KemParams P{};
+  P.l = 2;
+  P.eq = 13;
+  CpaArgs a{};
+  a.P = P;
+  a.n = 1;
+  a.mv_A = (const uint16_t *)dA;
+  a.mv_s = (const int8_t *)dS;
+  a.mv_out = (uint16_t *)dO;
+  a.mv_eq = 13;
+  a.stall_inputs = 1;
+  if ((r = run_cpa(c, kFp8Tcgen05, kMatvec, a, st))) return set_err(r);
+  return set_err(finish(c, st, true));
+}
+
 int tmvp_kem_dec_mixed(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, void *stream) {
   int r = mixed_check(c, ng, gr);
   if (r) return set_err(r);

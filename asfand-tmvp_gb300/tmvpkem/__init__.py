@@ -117,6 +117,7 @@ def lib(build_if_missing: bool = False):
     L.tmvp_ctx_reserve.argtypes = [P, S]
     L.tmvp_ctx_set_host_chunk.argtypes = [P, S]
     L.tmvp_ctx_set_host_ramp.argtypes = [P, ctypes.c_int]
+    L.tmvp_selftest_bounded_wait.argtypes = [P, P]
     L.tmvp_ctx_set_dev_chunk.argtypes = [P, S]
     L.tmvp_kem_dec_batch_noalloc.argtypes = [I, S, P, P, P, I, P]
     L.tmvp_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]

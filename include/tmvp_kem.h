@@ -280,6 +280,14 @@ int tmvp_autotune(tmvp_ctx *ctx, tmvp_param_set set, size_t n, int *shapes);
  * a bounded device wait gave up, TMVP_OK otherwise.  For work launched without
  * a host synchronisation (device buffers, graphs). */
 int tmvp_ctx_sync_status(tmvp_ctx *ctx, void *stream);
+/* Failure-detection self-test: launches one tcgen05 matrix-vector instance
+ * whose input barrier is told to expect 16 bytes more than its copies bring,
+ * so the kernel's bounded wait (about two seconds, then a second bounded
+ * wait for anything still in flight) gives up, frees its tensor memory and
+ * reports.  Returns TMVP_ETIMEOUT when that path works as designed (after
+ * about four seconds); the context stays usable.  No counterpart in the
+ * reference, which has no device-side waits. */
+int tmvp_selftest_bounded_wait(tmvp_ctx *ctx, void *stream);
 
 /* ---------------------------------------------------------------------------
  * Mixed-parameter decapsulation.  No counterpart in the reference (one

@@ -304,3 +304,23 @@ def test_failed_workspace_allocation_leaves_context_usable(kem, oracle):
     assert np.array_equal(pk, opk) and np.array_equal(sk, osk)
     ct, ss = ctx.kem_enc(T.SABER, pk, _coins(92, n, 32))
     assert np.array_equal(ctx.kem_dec(T.SABER, ct, sk), ss)
+
+
+def test_bounded_wait_reports_timeout(kem, oracle):
+    """Failure detection without a fault: the self-test launch's input wait
+    can never complete, so the kernel's bounded wait gives up after about two
+    seconds (and a second bounded wait for anything in flight), frees its
+    tensor memory and reports TMVP_ETIMEOUT; the context and the GPU stay
+    usable for the next call."""
+    import time
+    T, ctx = kem
+    t0 = time.perf_counter()
+    rc = T.lib().tmvp_selftest_bounded_wait(ctx.h, None)
+    dt = time.perf_counter() - t0
+    assert rc == T.ETIMEOUT
+    assert 1.5 < dt < 60, dt
+    rng = np.random.default_rng(11)
+    A = rng.integers(0, 1 << 13, (16, 3, 3, 256), dtype=np.uint16)
+    s = rng.integers(-5, 6, (16, 3, 256)).astype(np.int8)
+    got = ctx.matvec(A, s, eq=13, form=T.FORM_FP8_TCGEN05)
+    assert np.array_equal(got, oracle.matvec(A, s, eq=13, nthreads=4))
