@@ -14,6 +14,7 @@
 // (TMVP-Saber/SABER-GPU/src/cuda_kernel.cu:25-479) and SABLE_enc / SABLE_dec
 // (TMVP_SABLE/src/SABLE_indcpa.cu:24-610).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cerrno>
@@ -212,12 +213,23 @@ int stage_index(tmvp_ctx *c, const char *name) {
 }
 
 // Brackets one kernel launch with events when the context's timing is on.
+// NVTX range around the enqueue of one stage or one API call: Nsight tools
+// attribute the launches inside it, and ncu selects them with --nvtx-include.
+// Without an attached tool a push / pop costs a few nanoseconds.
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 struct StageTimer {
+  NvtxRange nv;
   tmvp_ctx *c;
   cudaStream_t s;
   int idx = -1;
   cudaEvent_t a = nullptr, b = nullptr;
-  StageTimer(tmvp_ctx *cc, const char *name, cudaStream_t ss) : c(cc), s(ss) {
+  StageTimer(tmvp_ctx *cc, const char *name, cudaStream_t ss) : nv(name), c(cc), s(ss) {
     if (!c->timing) return;
     idx = stage_index(c, name);
     a = pool_event(c);
@@ -620,6 +632,7 @@ uint64_t tmvp_ctx_launch_count(const tmvp_ctx *c) { return c ? c->launches : 0; 
 
 int tmvp_kem_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *pk, uint8_t *sk,
                            const uint8_t *coins, tmvp_form form, void *stream) {
+  NvtxRange nv_("tmvp_kem_keypair_batch");
   KemParams P;
   int r = check_common(c, set, n, form, &P);
   if (r) return set_err(r);
@@ -727,6 +740,7 @@ extern "C" {
 
 int tmvp_kem_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, uint8_t *ss,
                        const uint8_t *pk, const uint8_t *coins, tmvp_form form, void *stream) {
+  NvtxRange nv_("tmvp_kem_enc_batch");
   return enc_batch(c, set, n, ct, ss, pk, coins, nullptr, form, stream);
 }
 
@@ -737,6 +751,7 @@ size_t tmvp_genmatrix_bytes(tmvp_param_set set) {
 
 int tmvp_genmatrix_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *a_stream, const uint8_t *pk,
                          size_t pk_stride, void *stream) {
+  NvtxRange nv_("tmvp_genmatrix_batch");
   KemParams P;
   if (!c || !make_params(set, &P) || n > (size_t)INT_MAX) return set_err(TMVP_EINVAL);
   if (n == 0) return set_err(TMVP_OK);
@@ -754,6 +769,7 @@ int tmvp_genmatrix_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *a_s
 int tmvp_kem_enc_batch_a(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, uint8_t *ss,
                          const uint8_t *pk, const uint8_t *coins, const uint8_t *a_stream, tmvp_form form,
                          void *stream) {
+  NvtxRange nv_("tmvp_kem_enc_batch_a");
   KemParams P;
   if (!c || !make_params(set, &P) || !a_stream) return set_err(TMVP_EINVAL);
   if (n && classify(a_stream, n * P.gm_bytes, c->device).host) return set_err(TMVP_EINVAL);
@@ -762,6 +778,7 @@ int tmvp_kem_enc_batch_a(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct,
 
 int tmvp_kem_dec_batch_a(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, const uint8_t *ct,
                          const uint8_t *sk, const uint8_t *a_stream, tmvp_form form, void *stream) {
+  NvtxRange nv_("tmvp_kem_dec_batch_a");
   KemParams P;
   int r = check_common(c, set, n, form, &P);
   if (r) return set_err(r);
@@ -789,6 +806,7 @@ int tmvp_kem_dec_batch_a(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss,
 
 int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, const uint8_t *ct,
                        const uint8_t *sk, tmvp_form form, void *stream) {
+  NvtxRange nv_("tmvp_kem_dec_batch");
   KemParams P;
   int r = check_common(c, set, n, form, &P);
   if (r) return set_err(r);
@@ -904,6 +922,7 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
 
 int tmvp_indcpa_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *pk, uint8_t *sk,
                               const uint8_t *seeds, tmvp_form form, void *stream) {
+  NvtxRange nv_("tmvp_indcpa_keypair_batch");
   KemParams P;
   int r = check_common(c, set, n, form, &P);
   if (r) return set_err(r);
@@ -951,6 +970,7 @@ int tmvp_indcpa_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t
 int tmvp_indcpa_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, const uint8_t *m,
                           const uint8_t *noiseseed, const uint8_t *pk, tmvp_form form,
                           void *stream) {
+  NvtxRange nv_("tmvp_indcpa_enc_batch");
   KemParams P;
   int r = check_common(c, set, n, form, &P);
   if (r) return set_err(r);
@@ -996,6 +1016,7 @@ int tmvp_indcpa_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct
 
 int tmvp_indcpa_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *m, const uint8_t *sk,
                           const uint8_t *ct, tmvp_form form, void *stream) {
+  NvtxRange nv_("tmvp_indcpa_dec_batch");
   KemParams P;
   int r = check_common(c, set, n, form, &P);
   if (r) return set_err(r);
@@ -1032,6 +1053,7 @@ int tmvp_indcpa_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *m,
 
 int tmvp_matvec_batch(tmvp_ctx *c, size_t n, int l, int eq, int transpose, uint16_t *out,
                       const uint16_t *A_, const int8_t *s_, tmvp_form form, void *stream) {
+  NvtxRange nv_("tmvp_matvec_batch");
   if (!c || l < 2 || l > 4 || eq < 2 || eq > 13 || n > (size_t)INT_MAX) return set_err(TMVP_EINVAL);
   if (n == 0) return set_err(TMVP_OK);
   if (!out || !A_ || !s_) return set_err(TMVP_EINVAL);
@@ -1379,6 +1401,7 @@ int tmvp_ctx_sync_status(tmvp_ctx *c, void *stream) {
 }
 
 int tmvp_selftest_bounded_wait(tmvp_ctx *c, void *stream) {
+  NvtxRange nv_("tmvp_selftest_bounded_wait");
   if (!c) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(c->mu);
   Guard g(c);
@@ -1408,6 +1431,7 @@ int tmvp_selftest_bounded_wait(tmvp_ctx *c, void *stream) {
 }
 
 int tmvp_kem_dec_mixed(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, void *stream) {
+  NvtxRange nv_("tmvp_kem_dec_mixed");
   int r = mixed_check(c, ng, gr);
   if (r) return set_err(r);
   std::lock_guard<std::mutex> lk(c->mu);
@@ -1460,6 +1484,7 @@ int tmvp_mixed_plan_create(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, tmv
 }
 
 int tmvp_mixed_plan_launch(tmvp_mixed_plan *p, void *stream) {
+  NvtxRange nv_("tmvp_mixed_plan_launch");
   if (!p) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(p->c->mu);
   Guard g(p->c);
