@@ -43,6 +43,11 @@ def test_invalid_arguments(T):
     assert T.lib().tmvp_kem_dec_batch(None, 1, 1, None, None, None, 0, None) == T.EINVAL
     assert T.lib().tmvp_strerror(T.ENOMEM).decode().startswith("device workspace")
     assert T.lib().tmvp_ref_batch(0) == 1 and T.lib().tmvp_ref_batch(1) == 512
+    # context settings and the self-test refuse a null context before any CUDA call
+    assert T.lib().tmvp_ctx_set_host_ramp(None, 1) == T.EINVAL
+    assert T.lib().tmvp_ctx_set_host_chunk(None, 16384) == T.EINVAL
+    assert T.lib().tmvp_ctx_set_dev_chunk(None, 32768) == T.EINVAL
+    assert T.lib().tmvp_selftest_bounded_wait(None, None) == T.EINVAL
 
 
 def test_context_without_gpu_is_refused(T):
