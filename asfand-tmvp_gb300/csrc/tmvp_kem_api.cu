@@ -35,6 +35,11 @@
 #include "hash_kernels.cuh"
 #include "kem_common.cuh"
 
+namespace tmvp {
+// tensor-core issue-cost diagnostic (diag_umma.cu)
+int diag_umma_rate(int kind, int n, int ctas_per_sm, int iters, int *err, double *out, cudaStream_t s);
+}  // namespace tmvp
+
 using namespace tmvp;
 
 static thread_local int g_last_error = TMVP_OK;
@@ -1398,6 +1403,20 @@ int tmvp_ctx_sync_status(tmvp_ctx *c, void *stream) {
   std::lock_guard<std::mutex> lk(c->mu);
   Guard g(c);
   return set_err(finish(c, (cudaStream_t)stream, true));
+}
+
+int tmvp_diag_umma_rate(tmvp_ctx *c, int kind, int n, int ctas_per_sm, int iters, double *out) {
+  if (!c || !out) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  NvtxRange nv_("tmvp_diag_umma_rate");
+  const int e = tmvp::diag_umma_rate(kind, n, ctas_per_sm, iters, c->d_err, out, c->side);
+  c->launches++;
+  if (e == (int)cudaErrorInvalidValue) return set_err(TMVP_EINVAL);
+  const int r = finish(c, c->side, true);
+  if (e == (int)cudaErrorLaunchTimeout) return set_err(TMVP_ETIMEOUT);
+  if (e) return set_err(cuda_err((cudaError_t)e));
+  return set_err(r);
 }
 
 int tmvp_selftest_bounded_wait(tmvp_ctx *c, void *stream) {

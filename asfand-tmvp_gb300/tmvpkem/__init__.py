@@ -118,6 +118,7 @@ def lib(build_if_missing: bool = False):
     L.tmvp_ctx_set_host_chunk.argtypes = [P, S]
     L.tmvp_ctx_set_host_ramp.argtypes = [P, ctypes.c_int]
     L.tmvp_selftest_bounded_wait.argtypes = [P, P]
+    L.tmvp_diag_umma_rate.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
     L.tmvp_ctx_set_dev_chunk.argtypes = [P, S]
     L.tmvp_kem_dec_batch_noalloc.argtypes = [I, S, P, P, P, I, P]
     L.tmvp_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]
@@ -341,6 +342,12 @@ class Context:
 
     def set_host_chunk(self, n: int):
         _check(lib().tmvp_ctx_set_host_chunk(self.h, n), "tmvp_ctx_set_host_chunk")
+
+    def umma_rate(self, kind: int, n: int, ctas_per_sm: int = 4, iters: int = 4096):
+        """(cycles per MMA of one CTA, of the SM) for tcgen05 kind 0 = f8f6f4, 1 = f16."""
+        out = (ctypes.c_double * 2)()
+        _check(lib().tmvp_diag_umma_rate(self.h, kind, n, ctas_per_sm, iters, out), "tmvp_diag_umma_rate")
+        return out[0], out[1]
 
     def set_host_ramp(self, steps: int):
         """First chunks of a host-buffer decapsulation: host_chunk >> steps, ..."""

@@ -516,6 +516,17 @@ def _workloads(ctx, T, dev, sp, stream, args):
                               "bit_exact": bool(exact),
                               "launch": "one CUDA graph: the Keccak stages one launch over all 24 requests, "
                                         "decryption and re-encryption one launch per parameter set"}
+    # tensor-core issue cost of the two exact kinds the IND-CPA kernels could use
+    if "mma_rates" in W:
+        rates = {}
+        for kind, name in ((0, "f8f6f4_e4m3_K32"), (1, "f16_K16")):
+            rates[name] = {}
+            for ncol in (16, 32, 64, 128, 256):
+                ctas = max(1, min(4, 512 // max(32, ncol)))
+                cta, per_sm = ctx.umma_rate(kind, ncol, ctas_per_sm=ctas, iters=4096)
+                rates[name][str(ncol)] = {"sm_cycles_per_mma": per_sm, "ctas_per_sm": ctas,
+                                          "k_elements": 32 if kind == 0 else 16}
+        out["tcgen05_mma_cycles"] = rates
     # serving loop: Poisson arrivals over LightSaber, Saber, FireSaber and Sable
     if "serving" in W:
         rate, secs = 200_000.0, 2.0
@@ -574,8 +585,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the matrix-vector, Sable and serving workloads")
-    ap.add_argument("--workloads", default="matvec,sable,mixed,serving",
-                    help="extra workloads to run (comma list of matvec, sable, mixed, serving)")
+    ap.add_argument("--workloads", default="matvec,sable,mixed,mma_rates,serving",
+                    help="extra workloads to run (comma list of matvec, sable, mixed, mma_rates, serving)")
     ap.add_argument("--forms", default="fp8_tc,int8_tc,cuda_core,dp2a,toom_cook",
                     help="forms to time besides the headline (AUTO) form (comma list, or 'none')")
     args = ap.parse_args()

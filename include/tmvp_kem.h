@@ -288,6 +288,13 @@ int tmvp_ctx_sync_status(tmvp_ctx *ctx, void *stream);
  * about four seconds); the context stays usable.  No counterpart in the
  * reference, which has no device-side waits. */
 int tmvp_selftest_bounded_wait(tmvp_ctx *ctx, void *stream);
+/* Tensor-core issue cost of the exact kinds available to the IND-CPA kernels:
+ * kind 0 = tcgen05.mma kind::f8f6f4 (e4m3, K = 32), kind 1 = kind::f16 (f16,
+ * K = 16), M = 128, N = n (16, 32, 64, 128 or 256).  ctas_per_sm CTAs on
+ * every SM each issue `iters` MMAs back to back; out[0] = median cycles per
+ * MMA of one CTA (issue to completion), out[1] = out[0] / ctas_per_sm, the
+ * SM's cycles per MMA.  A diagnostic with no counterpart in the reference. */
+int tmvp_diag_umma_rate(tmvp_ctx *ctx, int kind, int n, int ctas_per_sm, int iters, double *out);
 
 /* ---------------------------------------------------------------------------
  * Mixed-parameter decapsulation.  No counterpart in the reference (one
