@@ -48,9 +48,9 @@ SABER = 1
 CT_BYTES, SK_BYTES, PK_BYTES = 1088, 2304, 992
 # schoolbook-equivalent work of one negacyclic 256 x 256 product
 POLY_OPS = 2 * 256 * 256
-# SM cycles per tcgen05.mma kind::f8f6f4 with M = 128, N <= 32, K = 32 when several CTAs per SM
-# issue back to back (measured on GB300); N = 256 takes 129
-MMA_CYCLES = 38
+# SM cycles per tcgen05.mma kind::f8f6f4 with M = 128, N = 32, K = 32 when 4 CTAs per SM issue
+# back to back (measured on GB300 by the mma_rates workload); N = 256 takes 128
+MMA_CYCLES = 39.8
 # tcgen05.mma per Saber re-encryption: 3 secret polynomials x 8 Hankel windows,
 # each N = 32 over two K steps (the negacyclic wrap serves both M halves)
 REENC_MMAS = 24
