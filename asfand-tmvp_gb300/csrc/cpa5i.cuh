@@ -205,7 +205,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
     const uint32_t d = smem_u32(sm);
     mbar_expect_tx(mbar_in, LO::IN_BYTES + (a.stall_inputs ? 16 : 0));
     if (LO::HAS_AS) {
-      bulk_g2s(d + LO::A, a.a_stream + (size_t)inst * C::GM, C::GM, mbar_in);
+      bulk_g2s(d + LO::A, a.a_stream + (a.key_shared ? 0 : (size_t)inst * C::GM), C::GM, mbar_in);
       bulk_g2s(d + LO::SS, a.s_stream + (size_t)inst * C::GS, C::GS, mbar_in);
     }
     if (LO::HAS_B) {
@@ -213,7 +213,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
       bulk_g2s(d + LO::MSG, a.msg + (size_t)inst * a.msg_stride, 32, mbar_in);
     }
     if (LO::HAS_CT) bulk_g2s(d + LO::CTO, a.ct + (size_t)inst * C::CT, C::CT, mbar_in);
-    if (LO::HAS_SK) bulk_g2s(d + LO::SKO, a.sk + (size_t)inst * C::SK, C::INDCPA_SK, mbar_in);
+    if (LO::HAS_SK) bulk_g2s(d + LO::SKO, a.sk + (a.key_shared ? 0 : (size_t)inst * C::SK), C::INDCPA_SK, mbar_in);
     if (LO::HAS_MV) {
       bulk_g2s(d + LO::A, reinterpret_cast<const uint8_t *>(a.mv_A) + (size_t)inst * LO::MV_A, LO::MV_A, mbar_in);
       bulk_g2s(d + LO::SS, reinterpret_cast<const uint8_t *>(a.mv_s) + (size_t)inst * LO::MV_S, LO::MV_S, mbar_in);
@@ -487,7 +487,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
     const uint32_t bits = __ballot_sync(0xffffffffu, ((t >> (C::EP - 1)) & 1u) != 0u);
     uint8_t *mo = a.m_out + (size_t)inst * a.m_out_stride;
     if (lane < 4) mo[4 * (4 * hsel + q4) + lane] = (uint8_t)(bits >> (8 * lane));
-    if (a.copy_hpk && warp == 0) mo[32 + lane] = a.sk[(size_t)inst * C::SK + C::SK - 64 + lane];
+    if (a.copy_hpk && warp == 0) mo[32 + lane] = a.sk[(a.key_shared ? 0 : (size_t)inst * C::SK) + C::SK - 64 + lane];
   } else if constexpr (OP == kReenc) {
     // round coefficient k of b' and encode that of v', compare with the ciphertext
     const uint32_t mk = (sm[LO::MSG + (k >> 3)] >> (k & 7)) & 1u;

@@ -11,7 +11,8 @@
 namespace tmvp {
 int cpa_launch_f8u_decrypt(const CpaArgs &a, cudaStream_t s) {
   const int mode = persist_ctas_per_sm(kDecrypt, a.P.set);
-  if (mode < 0) return launch_cpa5i_set<kDecrypt>(a, s);  // one CTA per instance
+  // one CTA per instance (always for a shared key, which only that kernel reads)
+  if (mode < 0 || a.key_shared) return launch_cpa5i_set<kDecrypt>(a, s);
   return launch_persist<kDecrypt>(&a, 1, nullptr, s, mode);
 }
 int cpa_launch_mixed_decrypt(const CpaArgs *g, int ng, const MixTable *dev_tab, cudaStream_t s, int ctas_per_sm) {

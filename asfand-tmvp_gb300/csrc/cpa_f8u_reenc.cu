@@ -9,7 +9,8 @@
 namespace tmvp {
 int cpa_launch_f8u_reenc(const CpaArgs &a, cudaStream_t s) {
   const int mode = persist_ctas_per_sm(kReenc, a.P.set);
-  if (mode < 0) return launch_cpa5i_set<kReenc>(a, s);  // one CTA per instance
+  // one CTA per instance (always for a shared key, which only that kernel reads)
+  if (mode < 0 || a.key_shared) return launch_cpa5i_set<kReenc>(a, s);
   return launch_persist<kReenc>(&a, 1, nullptr, s, mode);
 }
 int cpa_launch_mixed_reenc(const CpaArgs *g, int ng, const MixTable *dev_tab, cudaStream_t s, int ctas_per_sm) {

@@ -399,6 +399,7 @@ __global__ void __launch_bounds__(CpaCfg<FORM, OP, L, Q>::NT) k_cpa(CpaArgs a) {
 
 template <int FORM, int OP, int L, int Q>
 inline int launch_one(const CpaArgs &a, cudaStream_t s) {
+  if (a.key_shared) return (int)cudaErrorInvalidValue;  // per-instance keys only in these forms
   if constexpr (FORM == kFp8TC || FORM == kInt8TC) {
     return launch_tc<FORM, OP, L, Q>(a, s);
   } else {

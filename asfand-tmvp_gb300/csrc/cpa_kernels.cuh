@@ -48,6 +48,9 @@ struct CpaArgs {
   // input barrier expects 16 bytes more than the copies bring, so its
   // bounded wait runs out (nothing else changes; the copies all land)
   int stall_inputs;
+  // tcgen05 per-instance kernel only: sk (decryption) and a_stream
+  // (re-encryption) hold one key for every instance (stride 0)
+  int key_shared;
 };
 
 // Launch over a.n instances on `stream`.  Returns a CUDA error code (0 on

@@ -143,16 +143,17 @@ __global__ void __launch_bounds__(128) k_dec_front(KemParams P, const uint8_t *s
 // Final key derivation.  Encapsulation (cuda_kernel.cu:185-186):
 // K = H(kr[0:32] || H(c)); hc, when given, holds H(c) already.  Decapsulation (cuda_kernel.cu:445-450, with the
 // FO selection done as specified): K = H((fail ? z : kr[0:32]) || H(c)), the
-// selection made with a mask so that it does not branch on `fail`.
+// selection made with a mask so that it does not branch on `fail`.  sk of
+// instance t at sk + t * sk_stride (0: one key for every instance).
 __device__ __forceinline__ void final_key_one(const KemParams &P, const uint8_t *ct, const uint8_t *hc,
                                               const uint8_t *kr, const uint8_t *fail, const uint8_t *sk,
-                                              uint8_t *ss, size_t t) {
+                                              size_t sk_stride, uint8_t *ss, size_t t) {
   uint64_t buf[8], k[4];
   load_words(buf, kr + t * 64, 4);
   if (fail) {
     uint64_t mask = 0ull - (uint64_t)(fail[t] != 0);
     uint64_t z[4];
-    load_words(z, sk + t * P.sk_bytes + P.sk_bytes - 32, 4);
+    load_words(z, sk + t * sk_stride + P.sk_bytes - 32, 4);
 #pragma unroll
     for (int w = 0; w < 4; w++) buf[w] ^= mask & (buf[w] ^ z[w]);
   }
@@ -169,9 +170,9 @@ __device__ __forceinline__ void final_key_one(const KemParams &P, const uint8_t 
 __global__ void __launch_bounds__(128) k_final_key(KemParams P, const uint8_t *ct,
                                                     const uint8_t *hc, const uint8_t *kr,
                                                     const uint8_t *fail, const uint8_t *sk,
-                                                    uint8_t *ss, int n) {
+                                                    size_t sk_stride, uint8_t *ss, int n) {
   size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < (size_t)n) final_key_one(P, ct, hc, kr, fail, sk, ss, t);
+  if (t < (size_t)n) final_key_one(P, ct, hc, kr, fail, sk, sk_stride, ss, t);
 }
 
 // ---- mixed-parameter decapsulation: one launch per stage over a group table
@@ -215,7 +216,7 @@ __global__ void __launch_bounds__(128) k_mix_final(const HashGroup *T, int ng, i
   const int gi = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   if (gi >= total) return;
   const HashGroup &G = T[hash_group(T, ng, gi)];
-  final_key_one(G.P, G.ct, G.hc, G.kr, G.fail, G.sk, G.ss, (size_t)(gi - G.first));
+  final_key_one(G.P, G.ct, G.hc, G.kr, G.fail, G.sk, (size_t)G.P.sk_bytes, G.ss, (size_t)(gi - G.first));
 }
 
 // Key-generation tail: sk[SK-64 : SK-32] = H(pk), sk[SK-32 : SK] = z.
@@ -244,6 +245,17 @@ __global__ void k_sha3_256_batch(const uint8_t *in, int inbytes, uint8_t *out, i
   uint64_t *o = reinterpret_cast<uint64_t *>(out + t * 32);
 #pragma unroll
   for (int w = 0; w < 4; w++) o[w] = h[w];
+}
+
+// dst[i * words + w] = src[w] for i < n (16-byte words): one key's bytes and
+// its expanded A repeated per instance, for the one-key decapsulation.  Blocks
+// take instances, threads the words of one (coalesced stores; the source
+// stays in L1).
+__global__ void __launch_bounds__(256) k_replicate16(uint4 *dst, const uint4 *src, int words, size_t n) {
+  for (size_t i = blockIdx.x; i < n; i += gridDim.x) {
+    uint4 *d = dst + i * (size_t)words;
+    for (int w = threadIdx.x; w < words; w += blockDim.x) d[w] = src[w];
+  }
 }
 
 }  // namespace tmvp

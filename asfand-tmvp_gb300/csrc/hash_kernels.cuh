@@ -27,8 +27,9 @@ __global__ void k_enc_front(KemParams P, const uint8_t *pk, const uint8_t *coins
                             uint8_t *kr, uint8_t *s_stream, uint8_t *a_stream, int n);
 __global__ void k_dec_g(KemParams P, const uint8_t *mbuf, uint8_t *kr, uint8_t *s_stream, int n);
 __global__ void k_genmatrix(KemParams P, const uint8_t *pk, size_t pk_stride, uint8_t *a_stream, int n);
+__global__ void k_replicate16(uint4 *dst, const uint4 *src, int words, size_t n);
 __global__ void k_final_key(KemParams P, const uint8_t *ct, const uint8_t *hc, const uint8_t *kr,
-                            const uint8_t *fail, const uint8_t *sk, uint8_t *ss, int n);
+                            const uint8_t *fail, const uint8_t *sk, size_t sk_stride, uint8_t *ss, int n);
 __global__ void k_dec_front(KemParams P, const uint8_t *sk, const uint8_t *ct, uint8_t *a_stream,
                             uint8_t *hc, int n, int part);
 __global__ void k_kp_final(KemParams P, const uint8_t *pk, uint8_t *sk, const uint8_t *coins,

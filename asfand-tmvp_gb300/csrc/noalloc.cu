@@ -141,6 +141,6 @@ extern "C" int tmvp_kem_dec_batch_noalloc(tmvp_param_set set, size_t n, uint8_t 
   b.fail = fail;
   b.err = err;
   if (cpa_launch(f, kReenc, b, s) != 0) return TMVP_EDEVICE;
-  k_final_key<<<nblocks(n), 128, 0, s>>>(P, ct, hc, kr, fail, sk, ss, (int)n);
+  k_final_key<<<nblocks(n), 128, 0, s>>>(P, ct, hc, kr, fail, sk, (size_t)P.sk_bytes, ss, (int)n);
   return cudaGetLastError() == cudaSuccess ? TMVP_OK : TMVP_EDEVICE;
 }

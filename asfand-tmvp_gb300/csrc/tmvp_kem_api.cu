@@ -364,7 +364,7 @@ DecScratch dec_scratch(const KemParams &P, size_t n, Arena &A) {
 int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const uint8_t *ct,
                  const uint8_t *sk, int form, cudaStream_t s, const DecScratch &w, bool fork = true,
                  cudaStream_t side = nullptr, const uint8_t *a_cached = nullptr,
-                 cudaEvent_t a_ready = nullptr) {
+                 cudaEvent_t a_ready = nullptr, bool key_shared = false) {
   int r;
   if (!side) side = c->side;
   if (fork) {
@@ -388,6 +388,7 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   a.m_out = w.mbuf;
   a.m_out_stride = 64;
   a.copy_hpk = 1;
+  a.key_shared = key_shared ? 1 : 0;
   if ((r = run_cpa(c, form, kDecrypt, a, s))) return r;
   {
     StageTimer tm_(c, "dec_g", s);
@@ -402,8 +403,9 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   b.a_stream = a_cached ? a_cached : w.a_stream;
   b.s_stream = w.s_stream;
   b.pk = sk;
-  b.pk_stride = P.sk_bytes;
+  b.pk_stride = key_shared ? 0 : P.sk_bytes;
   b.pk_off = P.indcpa_sk_bytes;
+  b.key_shared = key_shared ? 1 : 0;
   b.msg = w.mbuf;
   b.msg_stride = 64;
   b.ct = ct;
@@ -411,7 +413,8 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   if ((r = run_cpa(c, form, kReenc, b, s))) return r;
   {
     StageTimer tm_(c, "final_key", s);
-    k_final_key<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, ct, w.hc, w.kr, w.fail, sk, ss, (int)n);
+    k_final_key<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, ct, w.hc, w.kr, w.fail, sk,
+                                                                 key_shared ? 0 : (size_t)P.sk_bytes, ss, (int)n);
   }
   c->launches++;
   return TMVP_OK;
@@ -733,7 +736,8 @@ int enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, uint8_t *s
   if ((r = run_cpa(c, form, kEncrypt, a, s))) return set_err(r);
   {
     StageTimer tm_(c, "final_key", s);
-    k_final_key<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, bct.dev, nullptr, kr, nullptr, nullptr, bss.dev, (int)n);
+    k_final_key<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, bct.dev, nullptr, kr, nullptr, nullptr, 0,
+                                                                 bss.dev, (int)n);
   }
   c->launches++;
   if ((r = download(bct, s)) || (r = download(bss, s))) return set_err(r);
@@ -804,6 +808,64 @@ int tmvp_kem_dec_batch_a(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss,
   stage_assign(bsk, A);
   if ((r = upload(bct, s)) || (r = upload(bsk, s))) return set_err(r);
   if ((r = dec_pipeline(c, P, n, bss.dev, bct.dev, bsk.dev, form, s, w, true, nullptr, a_stream)))
+    return set_err(r);
+  if ((r = download(bss, s))) return set_err(r);
+  return set_err(finish(c, s, bss.host));
+}
+
+int tmvp_kem_dec_batch_onekey(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, const uint8_t *ct,
+                              const uint8_t *sk, tmvp_form form, void *stream) {
+  NvtxRange nv_("tmvp_kem_dec_batch_onekey");
+  KemParams P;
+  int r = check_common(c, set, n, form, &P);
+  if (r) return set_err(r);
+  if (n == 0) return set_err(TMVP_OK);
+  if (!ss || !ct || !sk) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  cudaStream_t s = (cudaStream_t)stream;
+  Buf bss = classify(ss, n * 32, c->device), bct = classify(ct, n * P.ct_bytes, c->device),
+      bsk = classify(sk, P.sk_bytes, c->device);
+  // The key's GenMatrix runs once, then the cached-A chain (H(c),
+  // decryption, G, re-encryption, final key).  The tcgen05 per-instance
+  // kernels and the final key read the one key and its expanded A in place
+  // (stride 0); the other forms and launch shapes get them repeated per
+  // instance.
+  const bool shared = resolve_form(form) == kFp8Tcgen05;
+  size_t need = dec_ws_bytes(P, n) + up(P.gm_bytes) + stage_bytes(bss) + stage_bytes(bct) + stage_bytes(bsk) +
+                (shared ? 0 : up(n * P.sk_bytes) + up(n * P.gm_bytes));
+  if ((r = ensure_ws(c, need))) return set_err(r);
+  Arena A{c->ws};
+  DecScratch w = dec_scratch(P, n, A);
+  uint8_t *a_one = A.take(P.gm_bytes);
+  uint8_t *sk_rep = shared ? nullptr : A.take(n * P.sk_bytes), *a_rep = shared ? nullptr : A.take(n * P.gm_bytes);
+  stage_assign(bss, A);
+  stage_assign(bct, A);
+  stage_assign(bsk, A);
+  if ((r = upload(bct, s)) || (r = upload(bsk, s))) return set_err(r);
+  // the key's GenMatrix is one sponge of 23 Keccak-f, a latency of ~0.1 ms:
+  // it runs on a side stream beside H(c), the decryption and G, and only the
+  // re-encryption waits for it
+  const unsigned grid = (unsigned)std::min<size_t>(n, 152 * 16);
+  cudaStream_t gs = c->lane_side[0];
+  TRY_CUDA(cudaEventRecord(c->fork_ev, s));
+  TRY_CUDA(cudaStreamWaitEvent(gs, c->fork_ev, 0));
+  {
+    StageTimer tm_(c, "genmatrix", gs);
+    k_genmatrix<<<1, kHashBlock, 0, gs>>>(P, bsk.dev + P.indcpa_sk_bytes, 0, a_one, 1);
+    if (!shared)
+      k_replicate16<<<grid, 256, 0, gs>>>(reinterpret_cast<uint4 *>(a_rep), reinterpret_cast<const uint4 *>(a_one),
+                                          P.gm_bytes / 16, n);
+  }
+  TRY_CUDA(cudaEventRecord(c->gm_ev, gs));
+  if (!shared) {
+    StageTimer tm_(c, "replicate_key", s);
+    k_replicate16<<<grid, 256, 0, s>>>(reinterpret_cast<uint4 *>(sk_rep), reinterpret_cast<const uint4 *>(bsk.dev),
+                                       P.sk_bytes / 16, n);
+  }
+  c->launches += shared ? 1 : 3;
+  if ((r = dec_pipeline(c, P, n, bss.dev, bct.dev, shared ? bsk.dev : sk_rep, form, s, w, true, nullptr,
+                        shared ? a_one : a_rep, c->gm_ev, shared)))
     return set_err(r);
   if ((r = download(bss, s))) return set_err(r);
   return set_err(finish(c, s, bss.host));

@@ -95,6 +95,7 @@ def lib(build_if_missing: bool = False):
     L.tmvp_genmatrix_batch.argtypes = [P, I, S, P, P, S, P]
     L.tmvp_kem_enc_batch_a.argtypes = [P, I, S, P, P, P, P, P, I, P]
     L.tmvp_kem_dec_batch_a.argtypes = [P, I, S, P, P, P, P, I, P]
+    L.tmvp_kem_dec_batch_onekey.argtypes = [P, I, S, P, P, P, I, P]
     L.tmvp_indcpa_keypair_batch.argtypes = [P, I, S, P, P, P, I, P]
     L.tmvp_indcpa_enc_batch.argtypes = [P, I, S, P, P, P, P, I, P]
     L.tmvp_indcpa_dec_batch.argtypes = [P, I, S, P, P, P, I, P]
@@ -331,6 +332,11 @@ class Context:
         _check(lib().tmvp_kem_dec_batch_a(self.h, set_id, n, _ptr(ss), _ptr(ct), _ptr(sk), _ptr(a_stream),
                                           form, stream), "tmvp_kem_dec_batch_a")
 
+    def kem_dec_onekey_ptr(self, set_id, n, ss, ct, sk_one, form=FORM_AUTO, stream=None):
+        """n ciphertexts decapsulated under one secret key sk_one (sk_bytes)."""
+        _check(lib().tmvp_kem_dec_batch_onekey(self.h, set_id, n, _ptr(ss), _ptr(ct), _ptr(sk_one), form,
+                                               stream), "tmvp_kem_dec_batch_onekey")
+
     def matvec_ptr(self, n, l, eq, transpose, out, A, s, form=FORM_AUTO, stream=None):
         _check(lib().tmvp_matvec_batch(self.h, n, l, eq, int(transpose), _ptr(out), _ptr(A),
                                        _ptr(s), form, stream), "tmvp_matvec_batch")
@@ -392,6 +398,15 @@ class Context:
         n = ct.shape[0]
         ss = np.zeros((n, 32), np.uint8)
         self.kem_dec_ptr(set_id, n, ss, ct, sk, form)
+        return ss
+
+    def kem_dec_onekey(self, set_id, ct, sk_one, form=FORM_AUTO):
+        z = sizes(set_id)
+        ct = _u8(ct).reshape(-1, z.ct_bytes)
+        sk_one = _u8(sk_one).reshape(z.sk_bytes)
+        n = ct.shape[0]
+        ss = np.zeros((n, 32), np.uint8)
+        self.kem_dec_onekey_ptr(set_id, n, ss, ct, sk_one, form)
         return ss
 
     def indcpa_keypair(self, set_id, seeds, form=FORM_AUTO):

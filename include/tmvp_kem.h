@@ -156,6 +156,16 @@ int tmvp_kem_enc_batch_a(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *c
 int tmvp_kem_dec_batch_a(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *ss,
                          const uint8_t *ct, const uint8_t *sk, const uint8_t *a_stream,
                          tmvp_form form, void *stream);
+/* Decapsulation of n ciphertexts under ONE secret key (sk: sk_bytes, host or
+ * device; ct, ss as in tmvp_kem_dec_batch): a server holding one long-term
+ * key.  The key's GenMatrix runs once, then the cached-A chain, so a call
+ * costs 16 instead of 39 Keccak-f per ciphertext.  Same bytes as
+ * tmvp_kem_dec_batch with sk repeated n times.  The reference's saber_dec
+ * and SABLE_dec also decapsulate their whole batch under one key
+ * (TMVP-Saber/SABER-GPU/src/cuda_kernel.cu:320-321, TMVP_SABLE/src/
+ * SABLE_indcpa.cu:402-408), through per-instance buffers. */
+int tmvp_kem_dec_batch_onekey(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *ss, const uint8_t *ct,
+                              const uint8_t *sk, tmvp_form form, void *stream);
 
 /* Batched IND-CPA (indcpa_kem_* of the Saber reference API, n instances). */
 int tmvp_indcpa_keypair_batch(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *pk,

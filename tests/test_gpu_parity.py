@@ -324,3 +324,36 @@ def test_bounded_wait_reports_timeout(kem, oracle):
     s = rng.integers(-5, 6, (16, 3, 256)).astype(np.int8)
     got = ctx.matvec(A, s, eq=13, form=T.FORM_FP8_TCGEN05)
     assert np.array_equal(got, oracle.matvec(A, s, eq=13, nthreads=4))
+
+
+@pytest.mark.parametrize("set_id", [0, 1, 2, 3, 4, 5])
+def test_onekey_decapsulation(kem, oracle, set_id):
+    """Ciphertexts under one secret key (tmvp_kem_dec_batch_onekey): the same
+    keys as the per-instance call with sk repeated, the encapsulated keys, the
+    oracle's on a sample, and implicit rejection of a tampered ciphertext."""
+    T, ctx = kem
+    n = 1500
+    pk, sk = ctx.kem_keypair(set_id, _coins(61 + set_id, 1, 96))
+    ct, ss = ctx.kem_enc(set_id, np.repeat(pk, n, axis=0), _coins(71 + set_id, n, 32))
+    ct[9, 11] ^= 2
+    got = ctx.kem_dec_onekey(set_id, ct, sk[0])
+    assert np.array_equal(got, ctx.kem_dec(set_id, ct, np.repeat(sk, n, axis=0)))
+    good = np.ones(n, bool)
+    good[9] = False
+    assert np.array_equal(got[good], ss[good]) and not np.array_equal(got[9], ss[9])
+    oss, fail = oracle.kem_dec_batch(set_id, ct[:12], np.repeat(sk, 12, axis=0), nthreads=4)
+    assert np.array_equal(got[:12], oss) and fail[9] and not fail[:9].any()
+
+
+@pytest.mark.parametrize("form", [0, 1, 2, 6])
+def test_onekey_decapsulation_other_forms(kem, form):
+    """The forms other than tcgen05 run the one-key call on the key repeated
+    per instance, with the same bytes."""
+    T, ctx = kem
+    n = 700
+    pk, sk = ctx.kem_keypair(T.SABER, _coins(81, 1, 96))
+    ct, ss = ctx.kem_enc(T.SABER, np.repeat(pk, n, axis=0), _coins(82, n, 32))
+    ct[3, 0] ^= 1
+    got = ctx.kem_dec_onekey(T.SABER, ct, sk[0], form=form)
+    assert np.array_equal(got, ctx.kem_dec_onekey(T.SABER, ct, sk[0]))
+    assert np.array_equal(got[4:], ss[4:]) and not np.array_equal(got[3], ss[3])
