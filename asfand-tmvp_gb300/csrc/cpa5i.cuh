@@ -45,8 +45,11 @@ template <int OP, int SET>
 struct ShapeC {
   using C = SetC<SET>;
   static constexpr int L = C::L;
-  static constexpr int R = OP == kDecrypt ? 1 : (OP == kKeygen || OP == kMatvec ? L : L + 1);
-  static constexpr int RA = OP == kDecrypt ? 0 : L;
+  // kDecryptK: R ciphertexts per CTA, as many as fill 16 digit columns
+  static constexpr int R = OP == kDecrypt    ? 1
+                           : OP == kDecryptK ? 16 / r16_digits(C::EP)
+                                             : (OP == kKeygen || OP == kMatvec ? L : L + 1);
+  static constexpr int RA = (OP == kDecrypt || OP == kDecryptK) ? 0 : L;
   static constexpr int WA = C::EQ, WB = C::EP;
   static constexpr int DA = r16_digits(WA), DB = r16_digits(WB);
   static constexpr int NCOLS = RA * DA + (R - RA) * DB;
@@ -86,8 +89,12 @@ struct LayoutC {
   using S = ShapeC<OP, SET>;
   static constexpr bool HAS_AS = OP == kEncrypt || OP == kReenc || OP == kKeygen;
   static constexpr bool HAS_B = OP == kEncrypt || OP == kReenc;
-  static constexpr bool HAS_CT = OP == kReenc || OP == kDecrypt;
-  static constexpr bool HAS_SK = OP == kDecrypt;
+  static constexpr bool HAS_CT = OP == kReenc || OP == kDecrypt || OP == kDecryptK;
+  static constexpr bool HAS_SK = OP == kDecrypt || OP == kDecryptK;
+  // ciphertexts per CTA and their stride in shared memory (16 bytes of
+  // slack after each for the field readers)
+  static constexpr int NCT = OP == kDecryptK ? S::R : 1;
+  static constexpr int CTS = al16c(C::CT + 16);
   // matvec: A as 16-bit coefficients (l x l x 512 bytes) inside H, int8 secrets after it
   static constexpr bool HAS_MV = OP == kMatvec;
   static constexpr int MV_A = C::L * C::L * 512, MV_S = C::L * 256;
@@ -111,7 +118,7 @@ struct LayoutC {
   static constexpr int ENG_BYTES = ENG_END_OPS;  // also holds the epilogue's 16-bit values (R x 512 bytes)
   static_assert(S::R * 512 <= ENG_END_OPS, "epilogue values fit the operand region");
   static constexpr int CTO = al16c(ENG + ENG_BYTES);
-  static constexpr int MSG = HAS_CT ? al16c(CTO + C::CT + 16) : CTO;
+  static constexpr int MSG = HAS_CT ? al16c(CTO + NCT * CTS) : CTO;
   static constexpr int SEC8 = HAS_B ? al16c(MSG + 32 + 16) : MSG;
   static constexpr int OUT = OP == kKeygen ? al16c(SEC8 + C::L * 256) : SEC8;
   static constexpr int OUT_BYTES = OP == kEncrypt ? C::CT + 16
@@ -195,6 +202,10 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t mbar_in = smem_u32(sm + LO::BAR), mbar_mma = mbar_in + 8;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + LO::BAR + 16);
+  // kDecryptK: this CTA's ciphertexts inst0 .. inst0 + nvalid - 1 (one key)
+  constexpr bool DECK = OP == kDecryptK, IS_DEC = OP == kDecrypt || DECK;
+  const size_t inst0 = DECK ? (size_t)inst * LO::NCT : (size_t)inst;
+  const int nvalid = DECK ? min(LO::NCT, a.n - (int)inst0) : 1;
 
   // 0. tensor memory, barriers, and the input copies (one thread)
   if (warp == 0) tmem_alloc(smem_u32(tmem_slot), S::TMEM_COLS);
@@ -203,7 +214,8 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
     mbar_init(mbar_mma, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     const uint32_t d = smem_u32(sm);
-    mbar_expect_tx(mbar_in, LO::IN_BYTES + (a.stall_inputs ? 16 : 0));
+    const uint32_t in_bytes = DECK ? (uint32_t)(C::INDCPA_SK + nvalid * C::CT) : (uint32_t)LO::IN_BYTES;
+    mbar_expect_tx(mbar_in, in_bytes + (a.stall_inputs ? 16 : 0));
     if (LO::HAS_AS) {
       bulk_g2s(d + LO::A, a.a_stream + (a.key_shared ? 0 : (size_t)inst * C::GM), C::GM, mbar_in);
       bulk_g2s(d + LO::SS, a.s_stream + (size_t)inst * C::GS, C::GS, mbar_in);
@@ -212,8 +224,13 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
       bulk_g2s(d + LO::B, a.pk + (size_t)inst * a.pk_stride + a.pk_off, C::L * C::POLYCOMP, mbar_in);
       bulk_g2s(d + LO::MSG, a.msg + (size_t)inst * a.msg_stride, 32, mbar_in);
     }
-    if (LO::HAS_CT) bulk_g2s(d + LO::CTO, a.ct + (size_t)inst * C::CT, C::CT, mbar_in);
-    if (LO::HAS_SK) bulk_g2s(d + LO::SKO, a.sk + (a.key_shared ? 0 : (size_t)inst * C::SK), C::INDCPA_SK, mbar_in);
+    if (DECK) {
+      for (int r = 0; r < nvalid; r++) bulk_g2s(d + LO::CTO + r * LO::CTS, a.ct + (inst0 + r) * C::CT, C::CT, mbar_in);
+    } else if (LO::HAS_CT) {
+      bulk_g2s(d + LO::CTO, a.ct + (size_t)inst * C::CT, C::CT, mbar_in);
+    }
+    if (LO::HAS_SK)
+      bulk_g2s(d + LO::SKO, a.sk + ((a.key_shared || DECK) ? 0 : (size_t)inst * C::SK), C::INDCPA_SK, mbar_in);
     if (LO::HAS_MV) {
       bulk_g2s(d + LO::A, reinterpret_cast<const uint8_t *>(a.mv_A) + (size_t)inst * LO::MV_A, LO::MV_A, mbar_in);
       bulk_g2s(d + LO::SS, reinterpret_cast<const uint8_t *>(a.mv_s) + (size_t)inst * LO::MV_S, LO::MV_S, mbar_in);
@@ -242,7 +259,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
     if (sj >= 0 && sj < L) {
       const int j = sj, g = lane;
       uint32_t sb[2];
-      if (OP == kDecrypt && !C::SABLE) {
+      if (IS_DEC && !C::SABLE) {
         // 13-bit two's complement (SABER pack.cu:53-84)
         constexpr uint32_t m = ((1u << C::EQ) - 1u) * 0x10001u;
         uint32_t X[4];
@@ -259,7 +276,7 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
           const int w = 64 * j + 2 * g + h;
           if (OP == kMatvec) {
             sb[h] = lds32(smem_u32(sm + LO::SS) + 4 * w);  // four int8 coefficients
-          } else if (OP == kDecrypt) {
+          } else if (IS_DEC) {
             // 2-bit two's complement (SABLE pack.cu:371-376): one byte = 4 coefficients
             const uint32_t x = sm[LO::SKO + w];
             const uint32_t spread = (x & 3u) | ((x & 0xcu) << 6) | ((x & 0x30u) << 12) | ((x & 0xc0u) << 18);
@@ -338,6 +355,22 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
             const uint2 v = raw_digits8<S::WA>(X, d);
             const int n = p * S::DA + d;
             sts64(bl + j * LO::BJ + (n >> 3) * 128 + (n & 7) * 16, v.x, v.y);
+          }
+        }
+      }
+    } else if constexpr (DECK) {
+      // warp r makes ciphertext r's b'_j for every j (zero columns past the batch)
+      if (warp < S::R) {
+#pragma unroll
+        for (int j = 0; j < L; j++) {
+          if (warp < nvalid) {
+            item(std::integral_constant<int, S::WB>{}, LO::CTO + warp * LO::CTS + 32 * j * S::WB, warp * S::DB, j);
+          } else {
+#pragma unroll
+            for (int d0 = 0; d0 < S::DB; d0++) {
+              const int n = warp * S::DB + d0;
+              sts64(bl + j * LO::BJ + (n >> 3) * 128 + (n & 7) * 16, 0u, 0u);
+            }
           }
         }
       }
@@ -488,6 +521,19 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
     uint8_t *mo = a.m_out + (size_t)inst * a.m_out_stride;
     if (lane < 4) mo[4 * (4 * hsel + q4) + lane] = (uint8_t)(bits >> (8 * lane));
     if (a.copy_hpk && warp == 0) mo[32 + lane] = a.sk[(a.key_shared ? 0 : (size_t)inst * C::SK) + C::SK - 64 + lane];
+  } else if constexpr (DECK) {
+    // ciphertext r of the CTA: decode as above from its own columns and c_m
+#pragma unroll
+    for (int r = 0; r < S::R; r++) {
+      if (r >= nvalid) break;
+      const uint32_t v = combine1(r * S::DB, S::DB);
+      const uint32_t cm = field(LO::CTO + r * LO::CTS + L * C::POLYCOMP, k * C::ET, C::ET);
+      const uint32_t t = (v + C::H2 - (cm << (C::EP - C::ET))) & pmask;
+      const uint32_t bits = __ballot_sync(0xffffffffu, ((t >> (C::EP - 1)) & 1u) != 0u);
+      uint8_t *mo = a.m_out + (inst0 + r) * a.m_out_stride;
+      if (lane < 4) mo[4 * (4 * hsel + q4) + lane] = (uint8_t)(bits >> (8 * lane));
+      if (a.copy_hpk && warp == 0) mo[32 + lane] = a.sk[C::SK - 64 + lane];
+    }
   } else if constexpr (OP == kReenc) {
     // round coefficient k of b' and encode that of v', compare with the ciphertext
     const uint32_t mk = (sm[LO::MSG + (k >> 3)] >> (k & 7)) & 1u;
@@ -659,7 +705,7 @@ inline int launch_cpa5i(const CpaArgs &a, cudaStream_t s) {
     if (nb <= cap) break;
     smem += 2048;
   }
-  fn<<<a.n, kI5Threads, smem, s>>>(a);
+  fn<<<OP == kDecryptK ? (a.n + S::R - 1) / S::R : a.n, kI5Threads, smem, s>>>(a);
   return (int)cudaGetLastError();
 }
 

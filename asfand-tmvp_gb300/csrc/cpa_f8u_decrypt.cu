@@ -21,6 +21,10 @@ int cpa_launch_mixed_decrypt(const CpaArgs *g, int ng, const MixTable *dev_tab, 
   return launch_persist<kDecrypt>(g, ng, dev_tab, s, ctas_per_sm);
 }
 
+int cpa_launch_decrypt_onekey(const CpaArgs &a, void *s) {
+  return launch_cpa5i_set<kDecryptK>(a, (cudaStream_t)s);
+}
+
 size_t mix_table_bytes() { return sizeof(MixTable); }
 
 void mix_table_build(void *host_dst, const CpaArgs *g, int ng) {

@@ -16,6 +16,10 @@
 namespace tmvp {
 
 enum CpaOp : int { kDecrypt = 0, kEncrypt = 1, kReenc = 2, kKeygen = 3, kMatvec = 4 };
+// Decryption of several ciphertexts under one key per CTA (tcgen05 form
+// only; not in the per-op dispatch tables): the key's secret is staged once
+// and the ciphertexts' b' digit columns share every MMA.
+constexpr int kDecryptK = 5;
 
 struct CpaArgs {
   KemParams P;
@@ -56,6 +60,10 @@ struct CpaArgs {
 // Launch over a.n instances on `stream`.  Returns a CUDA error code (0 on
 // success).
 int cpa_launch(int form, int op, const CpaArgs &a, void *stream);
+
+// kDecryptK over a.n ciphertexts, all under the key at a.sk (a.key_shared
+// is implied): ceil(n / per-CTA count) CTAs.
+int cpa_launch_decrypt_onekey(const CpaArgs &a, void *stream);
 
 // tcgen05 form only: one persistent launch over `ngroups` (<= kMixMaxGroups)
 // groups of instances, each with its own parameter set and buffers.  groups:

@@ -389,7 +389,16 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   a.m_out_stride = 64;
   a.copy_hpk = 1;
   a.key_shared = key_shared ? 1 : 0;
-  if ((r = run_cpa(c, form, kDecrypt, a, s))) return r;
+  if (key_shared && resolve_form(form) == kFp8Tcgen05) {
+    // one key: several ciphertexts per CTA share its staged secret and MMAs
+    StageTimer tm_(c, "cpa_decrypt_onekey_fp8_tcgen05", s);
+    a.err = c->d_err;
+    const int e = cpa_launch_decrypt_onekey(a, s);
+    c->launches++;
+    if (e) return TMVP_EDEVICE;
+  } else if ((r = run_cpa(c, form, kDecrypt, a, s))) {
+    return r;
+  }
   {
     StageTimer tm_(c, "dec_g", s);
     k_dec_g<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, w.mbuf, w.kr, w.s_stream, (int)n);

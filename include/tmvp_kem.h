@@ -158,8 +158,9 @@ int tmvp_kem_dec_batch_a(tmvp_ctx *ctx, tmvp_param_set set, size_t n, uint8_t *s
                          tmvp_form form, void *stream);
 /* Decapsulation of n ciphertexts under ONE secret key (sk: sk_bytes, host or
  * device; ct, ss as in tmvp_kem_dec_batch): a server holding one long-term
- * key.  The key's GenMatrix runs once, then the cached-A chain, so a call
- * costs 16 instead of 39 Keccak-f per ciphertext.  Same bytes as
+ * key.  The key's GenMatrix runs once, then the cached-A chain (16 instead
+ * of 39 Keccak-f per ciphertext), and with the tcgen05 form one CTA decrypts
+ * 5 or 8 ciphertexts against the key's staged secret.  Same bytes as
  * tmvp_kem_dec_batch with sk repeated n times.  The reference's saber_dec
  * and SABLE_dec also decapsulate their whole batch under one key
  * (TMVP-Saber/SABER-GPU/src/cuda_kernel.cu:320-321, TMVP_SABLE/src/

@@ -357,3 +357,17 @@ def test_onekey_decapsulation_other_forms(kem, form):
     got = ctx.kem_dec_onekey(T.SABER, ct, sk[0], form=form)
     assert np.array_equal(got, ctx.kem_dec_onekey(T.SABER, ct, sk[0]))
     assert np.array_equal(got[4:], ss[4:]) and not np.array_equal(got[3], ss[3])
+
+
+@pytest.mark.parametrize("set_id,n", [(1, 1), (1, 7), (1, 1501), (4, 9), (4, 1503), (2, 11), (3, 6)])
+def test_onekey_decapsulation_ragged(kem, set_id, n):
+    """Batches that leave the last CTA of the one-key decryption partly
+    empty (5 ciphertexts per CTA for 10-bit b', 8 for 9-bit) give the
+    per-instance call's bytes."""
+    T, ctx = kem
+    pk, sk = ctx.kem_keypair(set_id, _coins(91 + n, 1, 96))
+    ct, ss = ctx.kem_enc(set_id, np.repeat(pk, n, axis=0), _coins(92 + n, n, 32))
+    ct[n - 1, 1] ^= 4
+    got = ctx.kem_dec_onekey(set_id, ct, sk[0])
+    assert np.array_equal(got, ctx.kem_dec(set_id, ct, np.repeat(sk, n, axis=0)))
+    assert np.array_equal(got[:n - 1], ss[:n - 1]) and not np.array_equal(got[n - 1], ss[n - 1])
