@@ -1,5 +1,7 @@
-// cpa_impl.cuh — the IND-CPA kernel template (one CTA per instance) shared by
-// the per-form translation units cpa_fp8.cu, cpa_int8.cu and cpa_cc.cu.
+// cpa_impl.cuh — the IND-CPA kernel template (one CTA per instance) of the
+// mma.sync and CUDA-core forms, instantiated per (form, op) in the
+// translation units cpa_fp8_*.cu, cpa_int8_*.cu, cpa_cc_*.cu, cpa_sb_*.cu,
+// cpa_dp2a.cu and cpa_tc4.cu.
 //
 // Per instance:
 //   1. 16-byte copies of the packed inputs into shared memory;

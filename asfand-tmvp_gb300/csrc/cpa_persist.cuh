@@ -374,7 +374,8 @@ __device__ __forceinline__ void drain5(const Shape5 &S, uint32_t tmem, int *acc)
 // Epilogue of one instance (worker warps; contains worker barriers): recombines
 // the radix-16 digit columns of acc and rounds / encodes / packs / compares /
 // decodes eight coefficients at a time (the same arithmetic as the
-// per-instance kernel, SABER poly.cu:15-16, pack.cu, verify.cu).
+// per-instance kernel, SABER poly.cu:15-16, pack.cu:7-212, the compare of
+// verify_gpu at pack.cu:225-241).
 template <int OP>
 __device__ __forceinline__ void epi5(const CpaArgs &a, const Shape5 &S, int inst, const uint8_t *raw,
                                      const RawOff &ro, const int *acc, const int8_t *s8, uint8_t *outb) {
