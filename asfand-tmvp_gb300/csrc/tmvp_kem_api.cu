@@ -835,6 +835,58 @@ int tmvp_kem_dec_batch_onekey(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t
   cudaStream_t s = (cudaStream_t)stream;
   Buf bss = classify(ss, n * 32, c->device), bct = classify(ct, n * P.ct_bytes, c->device),
       bsk = classify(sk, P.sk_bytes, c->device);
+  if (bct.host && c->host_chunk && n > c->host_chunk && resolve_form(form) == kFp8Tcgen05) {
+    // host ciphertexts: copy-ahead chunks over the four lanes as in
+    // tmvp_kem_dec_batch, every chunk's chain reading the one key and its
+    // expanded A (made once, on the side stream) in place
+    constexpr int NL = tmvp_ctx::kLanes, NS = tmvp_ctx::kSlots;
+    const size_t cn = c->host_chunk;
+    size_t need = NL * dec_ws_bytes(P, cn) + NS * up(cn * P.ct_bytes) + (bss.host ? NL * up(cn * 32) : 0) +
+                  up(P.gm_bytes) + stage_bytes(bsk);
+    if ((r = ensure_ws(c, need))) return set_err(r);
+    Arena A{c->ws};
+    DecScratch w[NL];
+    uint8_t *slot_ct[NS], *ss_stage[NL] = {};
+    for (int l = 0; l < NL; l++) w[l] = dec_scratch(P, cn, A);
+    for (int k = 0; k < NS; k++) slot_ct[k] = A.take(cn * P.ct_bytes);
+    if (bss.host)
+      for (int l = 0; l < NL; l++) ss_stage[l] = A.take(cn * 32);
+    uint8_t *a_one = A.take(P.gm_bytes);
+    stage_assign(bsk, A);
+    if ((r = upload(bsk, s))) return set_err(r);
+    TRY_CUDA(cudaEventRecord(c->fork_ev, s));
+    for (int l = 0; l < NL; l++) TRY_CUDA(cudaStreamWaitEvent(c->lane[l], c->fork_ev, 0));
+    TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+    {
+      StageTimer tm_(c, "genmatrix", c->side);
+      k_genmatrix<<<1, kHashBlock, 0, c->side>>>(P, bsk.dev + P.indcpa_sk_bytes, 0, a_one, 1);
+    }
+    c->launches++;
+    TRY_CUDA(cudaEventRecord(c->gm_ev, c->side));
+    for (size_t off = 0, k = 0, m = 0; off < n; off += m, k++) {
+      const size_t ck = k < (size_t)c->host_ramp ? std::max<size_t>(cn >> (c->host_ramp - k), 256) : cn;
+      m = std::min(ck, n - off);
+      const int sl = (int)(k % NS), ln = (int)(k % NL);
+      cudaStream_t ls = c->lane[ln];
+      if (k >= (size_t)NS) TRY_CUDA(cudaStreamWaitEvent(c->copy[0], c->ev_free[sl], 0));
+      TRY_CUDA(cudaMemcpyAsync(slot_ct[sl], (const uint8_t *)bct.user + off * P.ct_bytes, m * P.ct_bytes,
+                               cudaMemcpyDefault, c->copy[0]));
+      TRY_CUDA(cudaEventRecord(c->ev_loaded[sl][0], c->copy[0]));
+      TRY_CUDA(cudaStreamWaitEvent(ls, c->ev_loaded[sl][0], 0));
+      uint8_t *ss_k = bss.host ? ss_stage[ln] : bss.dev + off * 32;
+      if ((r = dec_pipeline(c, P, m, ss_k, slot_ct[sl], bsk.dev, form, ls, w[ln], true, c->lane_side[ln], a_one,
+                            c->gm_ev, true)))
+        return set_err(r);
+      TRY_CUDA(cudaEventRecord(c->ev_free[sl], ls));
+      if (bss.host)
+        TRY_CUDA(cudaMemcpyAsync((uint8_t *)bss.user + off * 32, ss_k, m * 32, cudaMemcpyDefault, ls));
+    }
+    for (int l = 0; l < NL; l++) {
+      TRY_CUDA(cudaEventRecord(c->lane_ev[l], c->lane[l]));
+      TRY_CUDA(cudaStreamWaitEvent(s, c->lane_ev[l], 0));
+    }
+    return set_err(finish(c, s, bss.host));
+  }
   // The key's GenMatrix runs once, then the cached-A chain (H(c),
   // decryption, G, re-encryption, final key).  The tcgen05 per-instance
   // kernels and the final key read the one key and its expanded A in place

@@ -177,3 +177,41 @@ def test_chunked_host_decapsulation(kem, chunk, ramp, pinned):
     ss_h = ss.cpu()
     assert torch.equal(out[:n - 3], ss_h[:n - 3]) and torch.equal(out[n - 2:], ss_h[n - 2:])
     assert not torch.equal(out[n - 3], ss_h[n - 3])
+
+
+@pytest.mark.parametrize("chunk,ramp,pinned", [(4096, 2, True), (16384, 1, True), (8192, 0, False)])
+def test_chunked_host_onekey_decapsulation(kem, chunk, ramp, pinned):
+    """Host ciphertexts under one key run as copy-ahead chunks; the keys equal
+    the device-buffer call's, with a tampered ciphertext in the last chunk
+    rejected."""
+    import torch
+    T, ctx = kem
+    dev = torch.device("cuda", 0)
+    n = 40000
+    z = T.sizes(T.SABER)
+    coins = torch.from_numpy(T.splitmix_bytes(45, 96).reshape(1, 96)).to(dev)
+    pk = torch.empty((1, z.pk_bytes), dtype=torch.uint8, device=dev)
+    sk = torch.empty((1, z.sk_bytes), dtype=torch.uint8, device=dev)
+    ctx.kem_keypair_ptr(T.SABER, 1, pk, sk, coins)
+    ec = torch.from_numpy(T.splitmix_bytes(46, n * 32).reshape(n, 32)).to(dev)
+    ct = torch.empty((n, z.ct_bytes), dtype=torch.uint8, device=dev)
+    ss = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+    ctx.kem_enc_ptr(T.SABER, n, ct, ss, pk.expand(n, -1).contiguous(), ec)
+    ct[n - 2, 3] ^= 8
+    ref = torch.empty_like(ss)
+    ctx.kem_dec_onekey_ptr(T.SABER, n, ref, ct, sk[0])
+    torch.cuda.synchronize()
+    ct_h, out = ct.cpu(), torch.zeros((n, 32), dtype=torch.uint8)
+    if pinned:
+        ct_h, out = ct_h.pin_memory(), out.pin_memory()
+    try:
+        ctx.set_host_chunk(chunk)
+        ctx.set_host_ramp(ramp)
+        ctx.kem_dec_onekey_ptr(T.SABER, n, out, ct_h, sk[0])
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_host_chunk(16384)
+        ctx.set_host_ramp(1)
+    assert torch.equal(out, ref.cpu())
+    ss_h = ss.cpu()
+    assert torch.equal(out[:n - 2], ss_h[:n - 2]) and not torch.equal(out[n - 2], ss_h[n - 2])
