@@ -101,6 +101,7 @@ struct tmvp_server {
   // statistics
   std::vector<float> lat_us;
   uint64_t submitted = 0, completed = 0, batches = 0, batched_reqs = 0, failed = 0;
+  std::atomic<uint64_t> one_key_batches{0};  // counted by launch_batch, outside the lock
   Clock::time_point t_reset = Clock::now();
 };
 
@@ -162,8 +163,21 @@ void launch_batch(tmvp_server *S, Slot &s) {
   }
   int e = 0;
   e |= cudaMemcpyAsync(s.d_in, s.h_in, (size_t)n * inb, cudaMemcpyHostToDevice, s.st);
-  e |= cudaMemcpyAsync(s.d_idx, s.h_idx, (size_t)n * 4, cudaMemcpyHostToDevice, s.st);
   const KeyTable &K = S->keys[s.set];
+  // a decapsulation batch under one key (a server's long-term key) reads
+  // that key in place and shares its secret across ciphertexts
+  bool one_key = s.op == TMVP_OP_DECAPS && n > 1;
+  for (int i = 1; one_key && i < n; i++) one_key = s.h_idx[i] == s.h_idx[0];
+  if (one_key) {
+    const int rc = tmvp_kem_dec_batch_onekey(s.ctx, (tmvp_param_set)s.set, n, s.d_out, s.d_in,
+                                             K.sk + (size_t)s.h_idx[0] * P.sk_bytes, (tmvp_form)S->cfg.form, s.st);
+    e |= cudaMemcpyAsync(s.h_out, s.d_out, (size_t)n * 32, cudaMemcpyDeviceToHost, s.st);
+    e |= cudaEventRecord(s.ev, s.st);
+    s.err = (rc != TMVP_OK || e != 0) ? 1 : 0;
+    S->one_key_batches.fetch_add(1, std::memory_order_relaxed);
+    return;
+  }
+  e |= cudaMemcpyAsync(s.d_idx, s.h_idx, (size_t)n * 4, cudaMemcpyHostToDevice, s.st);
   const int kb = s.op == TMVP_OP_DECAPS ? P.sk_bytes : P.pk_bytes;
   size_t words = (size_t)n * (kb >> 4);
   k_gather16<<<(unsigned)((words + 255) / 256), 256, 0, s.st>>>(
@@ -465,6 +479,7 @@ int tmvp_server_get_stats(tmvp_server *S, tmvp_server_stats *o) {
   o->mean_batch = S->batches ? (double)S->batched_reqs / S->batches : 0.0;
   o->slots = (int)S->slots.size();
   o->failed = S->failed;
+  o->one_key_batches = S->one_key_batches.load(std::memory_order_relaxed);
   o->elapsed_s = std::chrono::duration<double>(Clock::now() - S->t_reset).count();
   o->throughput = o->elapsed_s > 0 ? S->completed / o->elapsed_s : 0.0;
   if (!S->lat_us.empty()) {
@@ -486,6 +501,7 @@ void tmvp_server_reset_stats(tmvp_server *S) {
   std::lock_guard<std::mutex> lk(S->mu);
   S->lat_us.clear();
   S->submitted = S->completed = S->batches = S->batched_reqs = S->failed = 0;
+  S->one_key_batches.store(0, std::memory_order_relaxed);
   S->t_reset = Clock::now();
 }
 

@@ -211,7 +211,7 @@ class ServerStats(ctypes.Structure):
                 ("batches", ctypes.c_uint64), ("mean_batch", ctypes.c_double),
                 ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double), ("max_us", ctypes.c_double),
                 ("elapsed_s", ctypes.c_double), ("throughput", ctypes.c_double), ("slots", ctypes.c_int),
-                ("failed", ctypes.c_uint64)]
+                ("failed", ctypes.c_uint64), ("one_key_batches", ctypes.c_uint64)]
 
 
 OP_ENCAPS, OP_DECAPS = 0, 1

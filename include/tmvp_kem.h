@@ -241,6 +241,8 @@ typedef struct {
   int slots;                     /* slots admitted by the budget */
   uint64_t failed;               /* requests of batches whose launch failed
                                     (their outputs are not written) */
+  uint64_t one_key_batches;      /* decapsulation batches whose requests all
+                                    used one key (tmvp_kem_dec_batch_onekey) */
 } tmvp_server_stats;
 enum { TMVP_OP_ENCAPS = 0, TMVP_OP_DECAPS = 1 };
 int tmvp_server_create(const tmvp_server_config *cfg, tmvp_server **out);

@@ -102,3 +102,40 @@ def test_memory_admission_and_loadgen(kem):
         assert st["p99_us"] >= st["p50_us"] > 0
     finally:
         srv.close()
+
+
+def test_one_key_batches(kem, oracle):
+    """A server with one key per set: decapsulation batches whose requests all
+    use that key take the one-key path, with the same bytes as the
+    encapsulations and the oracle; a tampered ciphertext is rejected."""
+    T, ctx = kem
+    srv = T.Server(max_batch=256, slots=2)
+    try:
+        keys, ids = {}, {}
+        for s in (1, 4):
+            pk, sk = _keys(T, ctx, s, 1, 300 + s)
+            keys[s] = (pk, sk)
+            ids[s] = srv.add_keys(s, pk, sk)
+        reqs = []
+        for i in range(1200):
+            s = (1, 4)[i % 2]
+            c, kk = ctx.kem_enc(s, keys[s][0][0], T.splitmix_bytes(40_000 + i, 32))
+            c = c[0].copy()
+            if i == 601:
+                c[5] ^= 1
+            reqs.append((s, c, kk[0], np.zeros(32, np.uint8)))
+        srv.reset_stats()
+        for s, c, _, out in reqs:
+            srv.submit(T.OP_DECAPS, ids[s][0], c, out)
+        srv.drain()
+        st = srv.stats()
+        assert st["completed"] == len(reqs) and st["failed"] == 0
+        assert st["one_key_batches"] >= 1
+        for i, (s, c, kk, out) in enumerate(reqs):
+            if i == 601:
+                okk, fail = oracle.kem_dec(s, c, keys[s][1][0])
+                assert fail and out.tobytes() == okk and not np.array_equal(out, kk)
+            else:
+                assert np.array_equal(out, kk)
+    finally:
+        srv.close()
