@@ -543,6 +543,26 @@ def _workloads(ctx, T, dev, sp, stream, args):
                               "bit_exact": bool(exact),
                               "launch": "one CUDA graph: the Keccak stages one launch over all 24 requests, "
                                         "decryption and re-encryption one launch per parameter set"}
+    # every parameter set: decapsulations per second at batch 65536 (AUTO form)
+    if "sets" in W:
+        names = ["LightSaber", "Saber", "FireSaber", "LightSable", "Sable", "FireSable"]
+        nb = 65536
+        per_set = {}
+        for sid, name in enumerate(names):
+            z = T.sizes(sid)
+            coins = torch.from_numpy(T.splitmix_bytes(500 + sid, nb * 96).reshape(nb, 96)).to(dev)
+            ecoins = torch.from_numpy(T.splitmix_bytes(600 + sid, nb * 32).reshape(nb, 32)).to(dev)
+            pk = torch.empty((nb, z.pk_bytes), dtype=torch.uint8, device=dev)
+            sk = torch.empty((nb, z.sk_bytes), dtype=torch.uint8, device=dev)
+            ct = torch.empty((nb, z.ct_bytes), dtype=torch.uint8, device=dev)
+            ss1 = torch.empty((nb, 32), dtype=torch.uint8, device=dev)
+            ss2 = torch.empty((nb, 32), dtype=torch.uint8, device=dev)
+            ctx.kem_keypair_ptr(sid, nb, pk, sk, coins, T.FORM_AUTO, sp)
+            ctx.kem_enc_ptr(sid, nb, ct, ss1, pk, ecoins, T.FORM_AUTO, sp)
+            ms = _event_ms(stream, lambda: ctx.kem_dec_ptr(sid, nb, ss2, ct, sk, T.FORM_AUTO, sp), 10)
+            per_set[name] = {"decaps_per_s": nb / (ms / 1e3), "ms": ms, "bit_exact": bool(torch.equal(ss1, ss2))}
+            del pk, sk, ct, ss1, ss2, coins, ecoins
+        out["decaps_65536_by_set"] = per_set
     # tensor-core issue cost of the two exact kinds the IND-CPA kernels could use
     if "mma_rates" in W:
         rates = {}
@@ -612,8 +632,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the matrix-vector, Sable and serving workloads")
-    ap.add_argument("--workloads", default="matvec,sable,mixed,mma_rates,serving",
-                    help="extra workloads to run (comma list of matvec, sable, mixed, mma_rates, serving)")
+    ap.add_argument("--workloads", default="matvec,sable,sets,mixed,mma_rates,serving",
+                    help="extra workloads to run (comma list of matvec, sable, sets, mixed, mma_rates, serving)")
     ap.add_argument("--forms", default="fp8_tc,int8_tc,cuda_core,dp2a,toom_cook",
                     help="forms to time besides the headline (AUTO) form (comma list, or 'none')")
     args = ap.parse_args()
