@@ -1408,6 +1408,26 @@ int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws,
   std::vector<CpaArgs> ga(ng), gb(ng);
   std::vector<HashGroup> hg(ng);
   Arena A{ws};
+  // The Keccak launches take the groups in the table's order: the longest
+  // GenMatrix sponges first (l x l polynomials: FireSaber 40 Keccak-f, Saber
+  // 23, Sable 19, LightSaber 10), so that they do not finish alone at the
+  // end of the front launch.  Any order gives the same bytes.
+  std::vector<int> order(ng);
+  for (size_t g = 0; g < ng; g++) order[g] = (int)g;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    KemParams px, py;
+    make_params(gr[x].set, &px);
+    make_params(gr[y].set, &py);
+    return px.gm_bytes > py.gm_bytes;
+  });
+  std::vector<int> first_of(ng);
+  {
+    int t = 0;
+    for (int k = 0; k < (int)ng; k++) {
+      first_of[order[k]] = t;
+      t += (int)gr[order[k]].n;
+    }
+  }
   int total = 0;
   for (size_t g = 0; g < ng; g++) {
     KemParams P;
@@ -1415,7 +1435,7 @@ int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws,
     const size_t n = gr[g].n;
     HashGroup &h = hg[g];
     h.P = P;
-    h.first = total;
+    h.first = first_of[g];
     h.n = (int)n;
     h.sk = gr[g].sk;
     h.ct = gr[g].ct;
@@ -1465,7 +1485,10 @@ int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws,
     mix_table_build(host_tabs.data() + st * tb, sa[st].data(), (int)sa[st].size());
     mix_table_build(host_tabs.data() + (kNumSets + st) * tb, sb[st].data(), (int)sb[st].size());
   }
-  std::memcpy(host_tabs.data() + 2 * kNumSets * tb, hg.data(), ng * sizeof(HashGroup));
+  // the hash-group table in Keccak order (ascending first, as the group search needs)
+  std::vector<HashGroup> hg_sorted(ng);
+  for (size_t k = 0; k < ng; k++) hg_sorted[k] = hg[order[k]];
+  std::memcpy(host_tabs.data() + 2 * kNumSets * tb, hg_sorted.data(), ng * sizeof(HashGroup));
   // (pageable source: the call returns once the bytes are staged)
   if (upload_tabs) TRY_CUDA(cudaMemcpyAsync(tabs, host_tabs.data(), host_tabs.size(), cudaMemcpyHostToDevice, s));
   auto tdec = [&](int st) { return reinterpret_cast<const MixTable *>(tabs + st * tb); };
@@ -1477,22 +1500,33 @@ int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws,
   // GenMatrix and H(c) of every group in one launch (2 total sponges)
   k_mix_front<<<blocks_for(2 * (size_t)total, kHashBlock), kHashBlock, 0, c->side>>>(th, (int)ng, total, 0);
   TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
+  // the per-set IND-CPA launches of a step run side by side on the context's
+  // lanes (forked from s and joined back), so one set's last wave overlaps
+  // the next set's launch
   int nsets = 0;
-  for (int st = 0; st < kNumSets; st++) {
-    if (sa[st].empty()) continue;
-    nsets++;
-    if (cpa_launch_mixed(kDecrypt, sa[st].data(), (int)sa[st].size(), tdec(st), s,
-                         persist_ctas_per_sm(kDecrypt, st)) != 0)
-      return TMVP_EDEVICE;
-  }
+  auto per_set = [&](int op, std::vector<CpaArgs> *groups, auto table) -> int {
+    TRY_CUDA(cudaEventRecord(c->fork_ev, s));
+    int li = 0;
+    for (int st = 0; st < kNumSets; st++) {
+      if (groups[st].empty()) continue;
+      cudaStream_t ls = c->lane[li % tmvp_ctx::kLanes];
+      TRY_CUDA(cudaStreamWaitEvent(ls, c->fork_ev, 0));
+      if (cpa_launch_mixed(op, groups[st].data(), (int)groups[st].size(), table(st), ls,
+                           persist_ctas_per_sm(op, st)) != 0)
+        return TMVP_EDEVICE;
+      TRY_CUDA(cudaEventRecord(c->lane_ev[li % tmvp_ctx::kLanes], ls));
+      li++;
+    }
+    for (int i = 0; i < std::min(li, tmvp_ctx::kLanes); i++) TRY_CUDA(cudaStreamWaitEvent(s, c->lane_ev[i], 0));
+    return li;
+  };
+  int r1 = per_set(kDecrypt, sa, tdec);
+  if (r1 < 0) return r1;
+  nsets = r1;
   k_mix_g<<<nb, kHashBlock, 0, s>>>(th, (int)ng, total);
   TRY_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));  // GenMatrix
-  for (int st = 0; st < kNumSets; st++) {
-    if (sb[st].empty()) continue;
-    if (cpa_launch_mixed(kReenc, sb[st].data(), (int)sb[st].size(), tre(st), s,
-                         persist_ctas_per_sm(kReenc, st)) != 0)
-      return TMVP_EDEVICE;
-  }
+  int r2 = per_set(kReenc, sb, tre);
+  if (r2 < 0) return r2;
   k_mix_final<<<nb, kHashBlock, 0, s>>>(th, (int)ng, total);
   c->launches += 3 + 2 * nsets;
   TRY_CUDA(cudaGetLastError());
