@@ -228,17 +228,24 @@ __global__ void __launch_bounds__(CpaCfg<FORM, OP, L, Q>::NT) k_cpa(CpaArgs a) {
     // 0..127, v1 = 128..255)
     for (int idx = tid; idx < L * 64 * C::RP; idx += C::NT) {
       const int r = idx % C::RP, cp = (idx / C::RP) & 63, j = idx / (C::RP * 64);
-      uint32_t a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+      uint32_t va = 0, vb = 0;  // (v0[c], v0[c+1]) and (v1[c], v1[c+1]), c = 2 cp
       if (r < C::R) {
-        int w;
-        a0 = pub(r, j, 2 * cp, w);
-        a1 = pub(r, j, 2 * cp + 1, w);
-        b0 = pub(r, j, 2 * cp + 128, w);
-        b1 = pub(r, j, 2 * cp + 129, w);
+        if constexpr (OP == kMatvec) {
+          const int ij = a.mv_transpose ? (j * L + r) : (r * L + j);
+          const uint32_t *A32 = reinterpret_cast<const uint32_t *>(a.mv_A + inst * (size_t)(L * L * 256) + ij * 256);
+          const uint32_t m = ((1u << a.mv_eq) - 1u) * 0x10001u;
+          va = A32[cp] & m;
+          vb = A32[64 + cp] & m;
+        } else {
+          int w;
+          va = pub(r, j, 2 * cp, w) | (pub(r, j, 2 * cp + 1, w) << 16);
+          vb = pub(r, j, 2 * cp + 128, w) | (pub(r, j, 2 * cp + 129, w) << 16);
+        }
       }
-      wp[((j * 3 + 0) * 64 + cp) * C::RP + r] = (a0 + b0) | ((a1 + b1) << 16);
-      wp[((j * 3 + 1) * 64 + cp) * C::RP + r] = b0 | (b1 << 16);
-      wp[((j * 3 + 2) * 64 + cp) * C::RP + r] = a0 | (a1 << 16);
+      // halves below 2^14: the sum of the packed words adds them lane by lane
+      wp[((j * 3 + 0) * 64 + cp) * C::RP + r] = va + vb;
+      wp[((j * 3 + 1) * 64 + cp) * C::RP + r] = vb;
+      wp[((j * 3 + 2) * 64 + cp) * C::RP + r] = va;
     }
     __syncthreads();  // sec complete
     auto se = [&](int j, int i) -> int {
@@ -252,15 +259,22 @@ __global__ void __launch_bounds__(CpaCfg<FORM, OP, L, Q>::NT) k_cpa(CpaArgs a) {
                            : (p == 1 ? se(j, x + 127) - se(j, x + 255) : se(j, x + 255) - se(j, x + 383));
       return (uint32_t)v & 0xffu;
     };
+    // every byte u[k] once (k < 260, in the recombination scratch, free until
+    // the engine's end), then the four byte-shifted copies of word w by
+    // funnel shifts of words w and w + 1
+    constexpr int UB = 260;
+    uint8_t *ub = reinterpret_cast<uint8_t *>(pp);
+    static_assert(L * 3 * UB <= 3 * C::RP * 128 * 4, "byte sequences fit the recombination scratch");
+    for (int idx = tid; idx < L * 3 * UB; idx += C::NT) {
+      const int k = idx % UB, jp = idx / UB;
+      ub[idx] = (uint8_t)u(jp / 3, jp % 3, k);
+    }
+    __syncthreads();
     for (int idx = tid; idx < L * 3 * 64; idx += C::NT) {
-      const int w = idx & 63, p = (idx >> 6) % 3, j = idx / 192;
-      uint32_t cw[4];
-#pragma unroll
-      for (int cp = 0; cp < 4; cp++) {
-        const int k = 4 * w + cp;
-        cw[cp] = u(j, p, k) | (u(j, p, k + 1) << 8) | (u(j, p, k + 2) << 16) | (u(j, p, k + 3) << 24);
-      }
-      tb[idx] = make_uint4(cw[0], cw[1], cw[2], cw[3]);
+      const int w = idx & 63, jp = idx >> 6;
+      const uint32_t *u32 = reinterpret_cast<const uint32_t *>(ub + jp * UB);
+      const uint32_t lo = u32[w], hi = u32[w + 1];
+      tb[idx] = make_uint4(lo, __funnelshift_r(lo, hi, 8), __funnelshift_r(lo, hi, 16), __funnelshift_r(lo, hi, 24));
     }
     __syncthreads();
     dp2a_engine<C::RP>(tb, wp, L, C::R, pp, res);
