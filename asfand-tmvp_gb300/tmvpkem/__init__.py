@@ -121,7 +121,7 @@ def lib(build_if_missing: bool = False):
     L.tmvp_selftest_bounded_wait.argtypes = [P, P]
     L.tmvp_diag_umma_rate.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
     L.tmvp_ctx_set_dev_chunk.argtypes = [P, S]
-    L.tmvp_kem_dec_batch_noalloc.argtypes = [I, S, P, P, P, I, P]
+    L.tmvp_kem_dec_batch_noalloc.argtypes = [I, S, P, P, P, I, P, P]
     L.tmvp_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]
     L.tmvp_server_destroy.argtypes = [P]
     L.tmvp_server_destroy.restype = None

@@ -348,15 +348,22 @@ void tmvp_mixed_plan_destroy(tmvp_mixed_plan *plan);
  * parameter set), which every GPU that loads the library holds until the
  * process exits.  n <= TMVP_NOALLOC_MAX_BATCH
  * (larger n returns TMVP_EINVAL and launches nothing); ss, ct and sk must be
- * 16-byte-aligned device memory of the current GPU.  The first call on a
- * device looks up the array's address with that device current: make it
- * before any stream capture.  All calls share the array, which keeps the last
- * call's contents, so calls that overlap on the GPU race; issue them in order
- * on one stream.  The call is asynchronous on `stream` and calls no
- * cudaMalloc, cudaFree or allocating library routine. */
+ * 16-byte-aligned device memory of the current GPU.
+ * The return value covers the arguments and the launches only.  Errors that
+ * the GPU finds (a secret outside a tensor-core form's exact range, a bounded
+ * device wait that gave up) arrive in *status: when the stream reaches the
+ * end of the call the GPU writes TMVP_OK, TMVP_EINVAL or TMVP_ETIMEOUT there.
+ * status is a 4-byte-aligned int in device memory of the current GPU or in
+ * host memory mapped into it (cudaHostAlloc); NULL drops the report.
+ * The first call on a device (and the first after its context was replaced,
+ * e.g. by cudaDeviceReset) looks up the array's address with that device
+ * current: make it before any stream capture.  All calls share the array,
+ * which keeps the last call's contents, so calls that overlap on the GPU
+ * race; issue them in order on one stream.  The call is asynchronous on
+ * `stream` and calls no cudaMalloc, cudaFree or allocating library routine. */
 #define TMVP_NOALLOC_MAX_BATCH 1024
 int tmvp_kem_dec_batch_noalloc(tmvp_param_set set, size_t n, uint8_t *ss, const uint8_t *ct,
-                               const uint8_t *sk, tmvp_form form, void *stream);
+                               const uint8_t *sk, tmvp_form form, int *status, void *stream);
 
 /* NIST-style single-instance API for the default parameter set (Saber unless
  * changed).  Randomness comes from the randombytes hook (default: the

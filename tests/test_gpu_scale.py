@@ -73,10 +73,11 @@ def test_matvec_benchmark_size(kem, oracle, form):
     assert np.array_equal(summ.astype(np.uint16), got)
 
 
-def test_chunked_host_decapsulation(kem):
+def test_mixed_residency_host_decapsulation(kem):
     """Host inputs larger than one chunk (16384) go through the overlapped
     copy / compute path; the keys equal the device-buffer path's, including a
-    ragged last chunk and host outputs."""
+    ragged last chunk, host outputs, and mixed residency (host ciphertexts
+    with device keys and a device output)."""
     import torch
     T, ctx = kem
     dev = torch.device("cuda", 0)
