@@ -11,23 +11,23 @@
 // The product s * v is the negacyclic Toeplitz matrix T(s) times v, with
 // T(s)[r][c] = s_ext[r - c + 255], s_ext[255 + d] = s[d] (d >= 0) and
 // -s[d + 256] (d < 0), as in convertnegacyclictest (poly.cu:1116-1129).
-// Nothing here materialises T(s): the tensor-core engines read each 4-byte
+// Nothing here materialises T(s): the mma.sync engines read each 4-byte
 // fragment word straight out of the reversed sequence srev[k] =
 // s_ext[510 - k] (four byte-shifted copies keep every word aligned), and the
 // CUDA-core engine slides a register window along the same sequence.
 //
-// Three engines:
-//   * tc_engine<kFp8TC>: mma.sync m16n8k32 e4m3 x e4m3 -> f32.  Secrets are
-//     exact in e4m3 (|s| <= 8); public coefficients are centred and split into
-//     balanced radix-32 digits (|d| <= 16, exact in e4m3).  Every partial sum
-//     is an integer below 2^24 in magnitude, so the f32 accumulator is exact.
-//   * tc_engine<kInt8TC>: mma.sync m16n8k32 s8 x u8 -> s32 with the public
-//     coefficient split into 8-bit limbs.
+// The engines here:
+//   * the mma.sync instructions of the FP8_TC and INT8_TC forms (the engine
+//     itself is tc_engine_v2 in cpa_tc.cuh: e4m3 secrets against radix-8
+//     public digits biased by 8, with a column of ones for the bias
+//     correction; or s8 secrets against u8 limbs);
 //   * cc_engine: one-level 2-way TMVP on CUDA cores (the reference's
 //     submatrix_cuda / matvecp_cuda / matvecout_cuda split,
 //     poly.cu:1295-1392): P1 = T00 (v0+v1), P2 = (T01-T00) v1,
 //     P3 = (T00-T10) v0, r_lo = P1+P2, r_hi = P1-P3; or, for the schoolbook
-//     form, the full 256x256 product.
+//     form, the full 256x256 product;
+//   * dp2a_engine and toom4_engine: the DP2A and Toom-Cook 4-way CUDA-core
+//     forms.
 #pragma once
 #include <cstdint>
 
@@ -36,101 +36,13 @@
 namespace tmvp {
 
 // ---------------------------------------------------------------------------
-// Tensor-core column layout
+// Tensor-core (mma.sync) operand strides and instructions, used by the
+// FP8_TC / INT8_TC kernels (cpa_tc.cuh, cpa_tc_kernel.cuh)
 // ---------------------------------------------------------------------------
-// An m16n8 accumulator tile gives lane (g = lane/4, t = lane%4) columns 2t and
-// 2t+1.  Public polynomial r with D digit columns is placed so that all its
-// digit columns belong to the same t, which lets a lane recombine a whole
-// coefficient from its own registers:
-//   D = 2: poly r -> n-tile r/4, columns 2(r%4) + {0,1}
-//   D = 3: slot s = 3(r/4) + d of thread-group t = r%4 lives in n-tile s/2,
-//          column 2t + s%2.
-template <int D>
-__host__ __device__ constexpr int tc_ntiles(int R) {
-  return D == 2 ? (R + 3) / 4 : (3 * ((R - 1) / 4) + 2) / 2 + 1;
-}
-
-// Which (poly, digit) sits in column `col` (0..7) of n-tile q; poly = -1 if
-// the column is padding.
-template <int D>
-__host__ __device__ __forceinline__ void tc_slot(int q, int col, int &poly, int &digit) {
-  int t = col >> 1, e = col & 1;
-  if (D == 2) {
-    poly = 4 * q + t;
-    digit = e;
-  } else {
-    int s = 2 * q + e;
-    poly = 4 * (s / 3) + t;
-    digit = s % 3;
-  }
-}
-
 // Byte strides of the staged tensor-core operands.
 constexpr int kColStride = 272;          // one digit column: 256 bytes + 16 pad
 constexpr int kTzCopyWords = 136;        // one shifted copy of srev: 128 words + 8 pad
 constexpr int kTzBytesPerPoly = 4 * kTzCopyWords * 4;
-
-// e4m3 encodings of two small integers packed as {hi: b, lo: a}.
-__device__ __forceinline__ uint32_t e4m3x2(int a, int b) {
-  uint16_t r;
-  asm("cvt.rn.satfinite.e4m3x2.f32 %0, %1, %2;" : "=h"(r) : "f"((float)b), "f"((float)a));
-  return r;
-}
-
-// Encode four small integers as one word of 8-bit operands.
-template <int FORM>
-__device__ __forceinline__ uint32_t pack4_small(int v0, int v1, int v2, int v3) {
-  if (FORM == kFp8TC) {
-    return e4m3x2(v0, v1) | (e4m3x2(v2, v3) << 16);
-  } else {
-    return (uint32_t)(v0 & 0xff) | ((uint32_t)(v1 & 0xff) << 8) | ((uint32_t)(v2 & 0xff) << 16) |
-           ((uint32_t)(v3 & 0xff) << 24);
-  }
-}
-
-// Digit d of public coefficient x (x < 2^w) for the tensor-core forms.
-//   FP8: centred x in [-2^(w-1), 2^(w-1)), balanced radix-32 digits; the top
-//        digit keeps the remainder (|top| <= 16 for w <= 10 with D = 2 and
-//        for w <= 13 with D = 3).
-//   INT8: unsigned 8-bit limbs.
-template <int FORM, int D>
-__device__ __forceinline__ void public_digits(uint32_t x, int w, int (&dg)[D]) {
-  if (FORM == kFp8TC) {
-    int xc = (int)x - (int)((x >> (w - 1)) << w);
-    int d0 = ((xc + 16) & 31) - 16;
-    int x1 = (xc - d0) >> 5;
-    dg[0] = d0;
-    if (D == 2) {
-      dg[1] = x1;
-    } else {
-      int d1 = ((x1 + 16) & 31) - 16;
-      dg[1] = d1;
-      dg[D - 1] = (x1 - d1) >> 5;
-    }
-  } else {
-    dg[0] = (int)(x & 0xff);
-    dg[1] = (int)(x >> 8);
-    if (D == 3) dg[D - 1] = 0;
-  }
-}
-
-// srev[k] = s_ext[510 - k]: s[255-k] for k <= 255, -s[511-k] for k <= 510.
-template <class T>
-__device__ __forceinline__ int srev_at(const T *s, int k) {
-  return k <= 255 ? (int)s[255 - k] : (k <= 510 ? -(int)s[511 - k] : 0);
-}
-
-// Stage the four shifted copies of srev for one secret polynomial:
-// copy c, word w holds srev[4w + c .. 4w + c + 3].
-template <int FORM, class T>
-__device__ __forceinline__ void stage_toeplitz(uint32_t *tz, const T *s) {
-  for (int idx = threadIdx.x; idx < 4 * 128; idx += blockDim.x) {
-    int c = idx >> 7, w = idx & 127;
-    int k = 4 * w + c;
-    tz[c * kTzCopyWords + w] =
-        pack4_small<FORM>(srev_at(s, k), srev_at(s, k + 1), srev_at(s, k + 2), srev_at(s, k + 3));
-  }
-}
 
 template <int FORM>
 __device__ __forceinline__ void mma_m16n8k32(float (&d)[4], const uint32_t (&a)[4],
@@ -158,104 +70,6 @@ struct AccT<kInt8TC> { typedef int type; };
 
 __device__ __forceinline__ int acc_to_int(float v) { return __float2int_rn(v); }
 __device__ __forceinline__ int acc_to_int(int v) { return v; }
-
-// Tensor-core engine.  tz: l x [4][kTzCopyWords] words; col: l x [Q*8] digit
-// columns of kColStride bytes.  Writes res[r][256] for r < R.
-// The CTA has WARPS warps; warp w owns m-tiles w*MT .. w*MT+MT-1 (16 rows
-// each).  Fragment A(mt, kt) depends only on 16*mt - 32*kt, so the fragment
-// of m-tile i at k-step kt+1 is the one of m-tile i-2 at k-step kt: only two
-// new A fragments are loaded per k-step.
-template <int FORM, int D, int Q, int WARPS>
-__device__ __forceinline__ void tc_engine(const uint32_t *tz, const uint32_t *col, int l, int R,
-                                          uint16_t *res) {
-  constexpr int MT = 16 / WARPS;
-  typedef typename AccT<FORM>::type acc_t;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int g = lane >> 2, t = lane & 3;
-  const int mt0 = warp * MT;
-  const int copy = (3 - g) & 3;
-  // word index of a0 for (mt, kt): 63 - (g >= 4) - 4*mt + 8*kt + t
-  const int wbase = 63 - (g >> 2) + t - 4 * mt0;
-
-  acc_t acc[MT][Q][4];
-#pragma unroll
-  for (int i = 0; i < MT; i++)
-#pragma unroll
-    for (int q = 0; q < Q; q++)
-#pragma unroll
-      for (int e = 0; e < 4; e++) acc[i][q][e] = 0;
-
-  for (int j = 0; j < l; j++) {
-    const uint32_t *T = tz + (j * 4 + copy) * kTzCopyWords;
-    const uint32_t *B = col + (size_t)(j * Q * 8 + g) * (kColStride / 4) + t;
-    uint32_t a[MT][4];
-#pragma unroll
-    for (int kt = 0; kt < 8; kt++) {
-      uint32_t b[Q][2];
-#pragma unroll
-      for (int q = 0; q < Q; q++) {
-        b[q][0] = B[q * 8 * (kColStride / 4) + 8 * kt];
-        b[q][1] = B[q * 8 * (kColStride / 4) + 8 * kt + 4];
-      }
-      if (kt > 0) {
-#pragma unroll
-        for (int i = MT - 1; i >= 2; i--)
-#pragma unroll
-          for (int e = 0; e < 4; e++) a[i][e] = a[i - 2][e];
-      }
-#pragma unroll
-      for (int i = 0; i < MT; i++) {
-        if (kt == 0 || i < 2) {
-          int w0 = wbase - 4 * i + 8 * kt;
-          a[i][0] = T[w0];
-          a[i][1] = T[w0 - 2];
-          a[i][2] = T[w0 + 4];
-          a[i][3] = T[w0 + 2];
-        }
-      }
-#pragma unroll
-      for (int i = 0; i < MT; i++)
-#pragma unroll
-        for (int q = 0; q < Q; q++) {
-          if (FORM == kFp8TC)
-            mma_m16n8k32<FORM>(*reinterpret_cast<float(*)[4]>(&acc[i][q][0]), a[i], b[q]);
-          else
-            mma_m16n8k32_s8u8(*reinterpret_cast<int(*)[4]>(&acc[i][q][0]), a[i], b[q]);
-        }
-    }
-  }
-
-  constexpr int W = (FORM == kFp8TC) ? 5 : 8;  // digit weight 2^W
-#pragma unroll
-  for (int i = 0; i < MT; i++) {
-    const int r0 = 16 * (mt0 + i) + g;
-#pragma unroll
-    for (int h = 0; h < 2; h++) {  // h = 0: row r0 (c0,c1); h = 1: row r0+8 (c2,c3)
-      if (D == 2) {
-#pragma unroll
-        for (int q = 0; q < Q; q++) {
-          int p = 4 * q + t;
-          int v = acc_to_int(acc[i][q][2 * h]) + acc_to_int(acc[i][q][2 * h + 1]) * (1 << W);
-          if (p < R) res[p * 256 + r0 + 8 * h] = (uint16_t)v;
-        }
-      } else {
-        // poly t: slots 0,1,2 = (tile 0, e 0), (tile 0, e 1), (tile 1, e 0)
-        {
-          int v = acc_to_int(acc[i][0][2 * h]) + acc_to_int(acc[i][0][2 * h + 1]) * (1 << W) +
-                  acc_to_int(acc[i][Q > 1 ? 1 : 0][2 * h]) * (1 << (2 * W));
-          if (t < R) res[t * 256 + r0 + 8 * h] = (uint16_t)v;
-        }
-        if (Q >= 3) {
-          // poly t+4: slots 3,4,5 = (tile 1, e 1), (tile 2, e 0), (tile 2, e 1)
-          int v = acc_to_int(acc[i][1][2 * h + 1]) +
-                  acc_to_int(acc[i][Q > 2 ? 2 : 0][2 * h]) * (1 << W) +
-                  acc_to_int(acc[i][Q > 2 ? 2 : 0][2 * h + 1]) * (1 << (2 * W));
-          if (t + 4 < R) res[(t + 4) * 256 + r0 + 8 * h] = (uint16_t)v;
-        }
-      }
-    }
-  }
-}
 
 // ---------------------------------------------------------------------------
 // CUDA-core engine

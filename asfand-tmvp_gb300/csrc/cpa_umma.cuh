@@ -18,10 +18,13 @@
 // (leading byte offset, LBO) and in M/N (stride byte offset, SBO).
 //   * H_j: the core matrix at 8-row group b and 16-byte K chunk a holds
 //     s_ext[8b + 16a + i + e] (row i, byte e), which depends on m = b + 2a
-//     only.  So H_j is stored as 62 distinct core matrices, m = 0..61, at
-//     m * 128 bytes, and described with SBO = 128 and LBO = 256: the MMA's
-//     core matrix (b, a) lands on m = b + 2a.  That is 7.75 KB per secret
-//     polynomial instead of the 64 KB of the dense matrix.
+//     only.  So H_j is stored as distinct core matrices at m * 128 bytes and
+//     described with SBO = 128 and LBO = 256: the MMA's core matrix (b, a)
+//     lands on m = b + 2a.  The per-instance kernel (cpa5i.cuh) reads eight
+//     windows of the sequence and needs 46 of them, m = 0..45 (5.75 KB per
+//     secret polynomial, kHankelCores5); the persistent kernel
+//     (cpa_persist.cuh) keeps the earlier layout of 62 (7.75 KB,
+//     kHankelCores) -- either instead of the 64 KB of the dense matrix.
 //   * B_j: dense, core (8-column group c, K chunk a) at a * (16 N) + c * 128.
 //
 // Every product of an e4m3 digit (0..15) and an e4m3 secret (|s| <= 7) is an

@@ -140,6 +140,21 @@ __global__ void __launch_bounds__(128) k_dec_front(KemParams P, const uint8_t *s
     dec_hash_ct_one(P, ct, hc, t - n);
 }
 
+// The same 2n sponges (GenMatrix, then H(c)) from a capped grid that leaves
+// room on every SM for the decryption beside it: threads stride over the
+// sponges, GenMatrix ones (the longer) first.
+__global__ void __launch_bounds__(128) k_dec_front_strided(KemParams P, const uint8_t *sk,
+                                                            const uint8_t *ct, uint8_t *a_stream,
+                                                            uint8_t *hc, int n) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < 2 * (size_t)n; t += stride) {
+    if (t < (size_t)n)
+      dec_genmatrix_one(P, sk, a_stream, t);
+    else
+      dec_hash_ct_one(P, ct, hc, t - n);
+  }
+}
+
 // Final key derivation.  Encapsulation (cuda_kernel.cu:185-186):
 // K = H(kr[0:32] || H(c)); hc, when given, holds H(c) already.  Decapsulation (cuda_kernel.cu:445-450, with the
 // FO selection done as specified): K = H((fail ? z : kr[0:32]) || H(c)), the

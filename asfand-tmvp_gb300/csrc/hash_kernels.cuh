@@ -32,6 +32,8 @@ __global__ void k_final_key(KemParams P, const uint8_t *ct, const uint8_t *hc, c
                             const uint8_t *fail, const uint8_t *sk, size_t sk_stride, uint8_t *ss, int n);
 __global__ void k_dec_front(KemParams P, const uint8_t *sk, const uint8_t *ct, uint8_t *a_stream,
                             uint8_t *hc, int n, int part);
+__global__ void k_dec_front_strided(KemParams P, const uint8_t *sk, const uint8_t *ct, uint8_t *a_stream,
+                                    uint8_t *hc, int n);
 __global__ void k_kp_final(KemParams P, const uint8_t *pk, uint8_t *sk, const uint8_t *coins,
                            int n);
 __global__ void k_sha3_256_batch(const uint8_t *in, int inbytes, uint8_t *out, int n);

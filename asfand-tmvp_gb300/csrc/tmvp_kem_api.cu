@@ -38,6 +38,7 @@
 namespace tmvp {
 // tensor-core issue-cost diagnostic (diag_umma.cu)
 int diag_umma_rate(int kind, int n, int ctas_per_sm, int iters, int *err, double *out, cudaStream_t s);
+int diag_keccak_rate(int perms, uint64_t *scratch, size_t scratch_words, double *out, cudaStream_t s);
 }  // namespace tmvp
 
 using namespace tmvp;
@@ -60,6 +61,7 @@ struct tmvp_ctx {
   size_t budget = 0;
   uint8_t *ws = nullptr;  // device workspace
   size_t ws_cap = 0;
+  bool ws_external = false;  // ws belongs to the caller (ctx_attach_workspace): never freed or grown
   int *d_err = nullptr;   // device-side input-range flag
   uint64_t launches = 0;
   cudaStream_t side = nullptr;          // GenMatrix and H(c) beside the decryption (highest priority)
@@ -68,6 +70,9 @@ struct tmvp_ctx {
   size_t host_chunk = 16384;                       // chunk of host-input decapsulation (0: none)
   int host_ramp = 1;                               // first chunks host_chunk >> ramp, >> ramp-1, ...
   size_t dev_chunk = 32768;                        // chunk of device-input decapsulation (0: none)
+  bool serial = false;                             // every stage on the caller's stream, one at a time
+  int front_cap = 0;                               // Keccak-front blocks per SM (0: one thread per sponge)
+  int nsm = 0;                                     // SMs of the device
   static constexpr int kLanes = 4;                 // streams for chunk chains
   cudaStream_t lane[kLanes] = {};
   cudaStream_t lane_side[kLanes] = {};             // the Keccak front of each lane (highest priority)
@@ -119,6 +124,7 @@ int cuda_err(cudaError_t e) {
 
 int ensure_ws(tmvp_ctx *c, size_t bytes) {
   if (bytes <= c->ws_cap) return TMVP_OK;
+  if (c->ws_external) return TMVP_ENOMEM;
   if (c->budget && bytes > c->budget) return TMVP_ENOMEM;
   size_t cap = std::max(bytes, c->ws_cap + c->ws_cap / 2);
   if (c->budget) cap = std::min(cap, c->budget);
@@ -367,6 +373,10 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
                  cudaEvent_t a_ready = nullptr, bool key_shared = false) {
   int r;
   if (!side) side = c->side;
+  if (c->serial) {  // each stage alone on s (measurement: isolated stage durations)
+    side = s;
+    fork = false;
+  }
   if (fork) {
     TRY_CUDA(cudaEventRecord(c->fork_ev, s));
     TRY_CUDA(cudaStreamWaitEvent(side, c->fork_ev, 0));
@@ -376,7 +386,12 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
     k_dec_front<<<blocks_for(n, kHashBlock), kHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
   } else {
     StageTimer tm_(c, "dec_front", side);
-    k_dec_front<<<blocks_for(2 * n, kHashBlock), kHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 0);
+    const unsigned grid = blocks_for(2 * n, kHashBlock);
+    if (c->front_cap > 0 && grid > (unsigned)(c->nsm * c->front_cap))
+      k_dec_front_strided<<<(unsigned)(c->nsm * c->front_cap), kHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc,
+                                                                                   (int)n);
+    else
+      k_dec_front<<<grid, kHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 0);
   }
   TRY_CUDA(cudaEventRecord(c->join_ev, side));
   c->launches++;
@@ -519,6 +534,7 @@ int tmvp_ctx_create(int device, size_t mem_budget, tmvp_ctx **out) {
   tmvp_ctx *c = new tmvp_ctx();
   c->device = device;
   c->budget = mem_budget;
+  c->nsm = prop.multiProcessorCount;
   Guard g(c);
   // GenMatrix and H(c), which the re-encryption and the final key wait for,
   // run at the highest stream priority, so their blocks are scheduled ahead
@@ -564,7 +580,7 @@ void tmvp_ctx_destroy(tmvp_ctx *c) {
     cudaDeviceSynchronize();
     collect_stage_times(c);
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
-    if (c->ws) cudaFree(c->ws);
+    if (c->ws && !c->ws_external) cudaFree(c->ws);
     if (c->d_err) cudaFree(c->d_err);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
@@ -599,6 +615,20 @@ int tmvp_ctx_set_host_ramp(tmvp_ctx *c, int steps) {
   if (!c || steps < 0 || steps > 4) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(c->mu);
   c->host_ramp = steps;
+  return set_err(TMVP_OK);
+}
+
+int tmvp_ctx_set_front_cap(tmvp_ctx *c, int blocks_per_sm) {
+  if (!c || blocks_per_sm < 0 || blocks_per_sm > 64) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->front_cap = blocks_per_sm;
+  return set_err(TMVP_OK);
+}
+
+int tmvp_ctx_set_serial(tmvp_ctx *c, int on) {
+  if (!c) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->serial = on != 0;
   return set_err(TMVP_OK);
 }
 
@@ -1039,7 +1069,7 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
   stage_assign(bct, A);
   stage_assign(bsk, A);
   if ((r = upload(bct, s)) || (r = upload(bsk, s))) return set_err(r);
-  if (c->dev_chunk && n > c->dev_chunk)
+  if (c->dev_chunk && n > c->dev_chunk && !c->serial)
     r = dec_lanes(c, P, n, c->dev_chunk, bss.dev, bct.dev, bsk.dev, form, s, w);
   else
     r = dec_pipeline(c, P, n, bss.dev, bct.dev, bsk.dev, form, s, w);
@@ -1576,6 +1606,30 @@ int tmvp_diag_umma_rate(tmvp_ctx *c, int kind, int n, int ctas_per_sm, int iters
   return set_err(r);
 }
 
+int tmvp_diag_keccak_rate(tmvp_ctx *c, int perms, double *out) {
+  if (!c || !out) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  NvtxRange nv_("tmvp_diag_keccak_rate");
+  double o[3] = {0, 0, 0};
+  int e = tmvp::diag_keccak_rate(perms, nullptr, 0, o, c->side);  // sizes the scratch
+  if (e != (int)cudaErrorInvalidValue || o[2] <= 0) return set_err(TMVP_EINVAL);
+  uint64_t *d = nullptr;
+  cudaError_t ce = cudaMalloc(&d, (size_t)o[2] * sizeof(uint64_t));
+  if (ce != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(TMVP_ENOMEM);
+  }
+  e = tmvp::diag_keccak_rate(perms, d, (size_t)o[2], o, c->side);
+  c->launches += 2;
+  cudaFree(d);
+  if (e == (int)cudaErrorInvalidValue) return set_err(TMVP_EINVAL);
+  if (e) return set_err(cuda_err((cudaError_t)e));
+  out[0] = o[0];
+  out[1] = o[1];
+  return set_err(TMVP_OK);
+}
+
 int tmvp_selftest_bounded_wait(tmvp_ctx *c, void *stream) {
   NvtxRange nv_("tmvp_selftest_bounded_wait");
   if (!c) return set_err(TMVP_EINVAL);
@@ -1813,3 +1867,37 @@ extern "C" int tmvp_autotune(tmvp_ctx *c, tmvp_param_set set, size_t n, int *sha
   }
   return set_err(TMVP_OK);
 }
+
+namespace tmvp {
+
+// Library-internal (the serving loop): device workspace bytes that one
+// batched call over n device-resident instances needs.  op 0: encapsulation
+// with each key's A given (tmvp_kem_enc_batch_a); op 1: decapsulation with A
+// given (tmvp_kem_dec_batch_a); op 2: one-key decapsulation on the tcgen05
+// form (tmvp_kem_dec_batch_onekey).
+size_t kem_ws_bytes(int op, const KemParams &P, size_t n) {
+  if (op == 0) return up(n * P.gs_bytes) + 2 * up(n * 64);
+  if (op == 1) return dec_ws_bytes(P, n);
+  return dec_ws_bytes(P, n) + up(P.gm_bytes);
+}
+
+// Library-internal: the context works in the caller's device buffer
+// [ws, ws + bytes) from now on, and never frees or grows it (a call that
+// needs more returns TMVP_ENOMEM).  Any workspace the context allocated
+// itself is freed first.  The caller keeps the buffer alive and unused by
+// others until the context's queued work on it has finished.
+int ctx_attach_workspace(tmvp_ctx *c, uint8_t *ws, size_t bytes) {
+  if (!c || !ws) return TMVP_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (c->ws && !c->ws_external) {
+    Guard g(c);
+    cudaDeviceSynchronize();
+    cudaFree(c->ws);
+  }
+  c->ws = ws;
+  c->ws_cap = bytes;
+  c->ws_external = true;
+  return TMVP_OK;
+}
+
+}  // namespace tmvp

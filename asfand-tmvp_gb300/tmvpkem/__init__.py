@@ -120,7 +120,10 @@ def lib(build_if_missing: bool = False):
     L.tmvp_ctx_set_host_ramp.argtypes = [P, ctypes.c_int]
     L.tmvp_selftest_bounded_wait.argtypes = [P, P]
     L.tmvp_diag_umma_rate.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
+    L.tmvp_diag_keccak_rate.argtypes = [P, ctypes.c_int, P]
     L.tmvp_ctx_set_dev_chunk.argtypes = [P, S]
+    L.tmvp_ctx_set_serial.argtypes = [P, ctypes.c_int]
+    L.tmvp_ctx_set_front_cap.argtypes = [P, ctypes.c_int]
     L.tmvp_kem_dec_batch_noalloc.argtypes = [I, S, P, P, P, I, P, P]
     L.tmvp_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]
     L.tmvp_server_destroy.argtypes = [P]
@@ -211,7 +214,10 @@ class ServerStats(ctypes.Structure):
                 ("batches", ctypes.c_uint64), ("mean_batch", ctypes.c_double),
                 ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double), ("max_us", ctypes.c_double),
                 ("elapsed_s", ctypes.c_double), ("throughput", ctypes.c_double), ("slots", ctypes.c_int),
-                ("failed", ctypes.c_uint64), ("one_key_batches", ctypes.c_uint64)]
+                ("failed", ctypes.c_uint64), ("one_key_batches", ctypes.c_uint64),
+                ("arena_bytes", ctypes.c_uint64), ("peak_arena_bytes", ctypes.c_uint64),
+                ("admission_waits", ctypes.c_uint64), ("admission_splits", ctypes.c_uint64),
+                ("checked", ctypes.c_uint64), ("mismatched", ctypes.c_uint64)]
 
 
 OP_ENCAPS, OP_DECAPS = 0, 1
@@ -353,6 +359,20 @@ class Context:
         """(cycles per MMA of one CTA, of the SM) for tcgen05 kind 0 = f8f6f4, 1 = f16."""
         out = (ctypes.c_double * 2)()
         _check(lib().tmvp_diag_umma_rate(self.h, kind, n, ctas_per_sm, iters, out), "tmvp_diag_umma_rate")
+        return out[0], out[1]
+
+    def set_serial(self, on: bool):
+        """Run every decapsulation stage alone on the caller's stream (measurement)."""
+        _check(lib().tmvp_ctx_set_serial(self.h, int(bool(on))), "tmvp_ctx_set_serial")
+
+    def set_front_cap(self, blocks_per_sm: int):
+        """Keccak-front blocks per SM in decapsulation (0 = one thread per sponge)."""
+        _check(lib().tmvp_ctx_set_front_cap(self.h, blocks_per_sm), "tmvp_ctx_set_front_cap")
+
+    def keccak_rate(self, perms: int = 64):
+        """(Keccak-f[1600] permutations per second at full occupancy, blocks per SM)."""
+        out = (ctypes.c_double * 2)()
+        _check(lib().tmvp_diag_keccak_rate(self.h, perms, out), "tmvp_diag_keccak_rate")
         return out[0], out[1]
 
     def set_host_ramp(self, steps: int):

@@ -1,5 +1,5 @@
 #!/usr/bin/env python3
-"""Saber decapsulations per second at batch 65536, bit-exact.
+"""Saber decapsulations per second at batch 65536, bit-exact; p50/p99 latency.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -13,15 +13,23 @@ resident inputs (inputs are 222 MB, larger than the 129 MB L2, so no flush is
 needed between steps).  `value` is decaps/s of the FP8 tensor-core form;
 `forms` adds the other forms timed the same way: the mma.sync FP8 and INT8
 tensor-core forms, and the CUDA-core forms (TMVP with IMAD, TMVP with dp2a,
-Toom-Cook 4-way).  `e2e` is the same metric through the public C ABI with pinned HOST
-buffers (host-to-device copies of ct and sk and the copy of the keys back are
-inside the timed region).  `roofline` is the dominant kernel of the step,
-timed live with CUDA events on its own stream.  `cpu_baseline` is the CPU
-oracle timed on a sample over all host threads.
+Toom-Cook 4-way).  `e2e` is the same metric through the public C ABI with
+pinned HOST buffers (host-to-device copies of ct and sk and the copy of the
+keys back are inside the timed region), at the library's default host chunk
+and ramp; `e2e_sweep` times the other settings.  `roofline` is the dominant
+kernel of the step (the largest share of the step's per-stage device time),
+timed live with CUDA events on its own stream, with the other large kernels
+in `roofline.others`.  `latency` holds per-call p50/p99: the CPU oracle at
+batch 1 (keypair, encapsulation, decapsulation) and this library through the
+C ABI with host buffers at batch 1 ... 65536.  `cpu_baseline` is the CPU
+oracle with the reference's multiplication (Toom-Cook 4-way over Karatsuba)
+timed on a sample over all host threads.  Clocks are sampled through NVML
+every millisecond inside the timed region.
 
 --impl reference times the reference's CPU path for this workload (the CPU
-oracle port of the reference's serial code; the reference itself has no CPU
-implementation) on the same metric.
+oracle port of the reference's serial code with its Toom-Cook / Karatsuba
+multiplication; the reference itself has no CPU implementation) on all 65536
+decapsulations per step, on all host threads.
 """
 from __future__ import annotations
 
@@ -51,9 +59,13 @@ POLY_OPS = 2 * 256 * 256
 # SM cycles per tcgen05.mma kind::f8f6f4 with M = 128, N = 32, K = 32 when 4 CTAs per SM issue
 # back to back (measured on GB300 by the mma_rates workload); N = 256 takes 128
 MMA_CYCLES = 39.8
+MMA_CYCLES_N16 = 38.8
 # tcgen05.mma per Saber re-encryption: 3 secret polynomials x 8 Hankel windows,
 # each N = 32 over two K steps (the negacyclic wrap serves both M halves)
 REENC_MMAS = 24
+DEC_MMAS = 24
+# the library's default host-buffer chunk and ramp (tmvp_ctx_set_host_chunk / _ramp)
+DEFAULT_HOST_CHUNK, DEFAULT_HOST_RAMP = 16384, 1
 
 
 def _peaks():
@@ -125,19 +137,102 @@ class ClockSampler:
                 "samples_total": len(self.rows)}
 
 
+class NvmlSampler:
+    """SM clock, power and clock-event reasons read through NVML (libnvidia-ml,
+    read-only queries) every `period` seconds on a thread, each sample stamped
+    with the host clock.  Falls back to nothing when NVML is missing."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, uuid: str | None, period: float = 0.001):
+        import ctypes
+        self.rows, self.ok, self.max_mhz = [], False, None
+        self._stop = threading.Event()
+        try:
+            L = ctypes.CDLL("libnvidia-ml.so.1")
+            if L.nvmlInit_v2() != 0:
+                return
+            h = ctypes.c_void_p()
+            if not uuid or L.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(h)) != 0:
+                return
+            self.L, self.h, self.ct = L, h, ctypes
+            mx = ctypes.c_uint()
+            if L.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:
+                self.max_mhz = float(mx.value)
+            self._reasons = getattr(L, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                getattr(L, "nvmlDeviceGetCurrentClocksThrottleReasons")
+            self.ok = True
+        except (OSError, AttributeError):
+            return
+        self.period = period
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+
+    def _run(self):
+        ct, L, h = self.ct, self.L, self.h
+        clk, rs, pw = ct.c_uint(), ct.c_ulonglong(), ct.c_uint()
+        while not self._stop.is_set():
+            if L.nvmlDeviceGetClockInfo(h, 1, ct.byref(clk)) == 0:
+                r = rs.value if self._reasons(h, ct.byref(rs)) == 0 else 0
+                p = pw.value / 1e3 if L.nvmlDeviceGetPowerUsage(h, ct.byref(pw)) == 0 else None
+                self.rows.append((time.perf_counter(), float(clk.value), int(r), p))
+            time.sleep(self.period)
+
+    def stop(self, t0: float, t1: float):
+        if not self.ok:
+            return None
+        self._stop.set()
+        self.t.join(timeout=2)
+        inside = [r for r in self.rows if t0 <= r[0] <= t1]
+        if not inside:
+            return None
+        reasons = sorted({n for _, _, r, _ in inside for bit, n in self.REASONS.items() if r & bit})
+        pw = [p for *_, p in inside if p is not None]
+        return {"sm_mhz": statistics.median(r[1] for r in inside), "sm_max_mhz": self.max_mhz,
+                "reasons": reasons, "samples_in_timed_region": len(inside),
+                "power_w_max": max(pw) if pw else None, "source": "NVML, 1 ms period"}
+
+
 def cpu_decaps_rate(n: int, nthreads: int, seed: int = 99):
-    """Oracle decapsulations per second over all host threads on n instances."""
+    """Oracle decapsulations per second over all host threads on n instances,
+    with the reference's multiplication (Toom-Cook 4-way over Karatsuba)."""
     from oracle import pyoracle as O
     import tmvpkem as T
     O.build()
     coins = T.splitmix_bytes(seed, n * 96).reshape(n, 96)
     pk, sk = O.kem_keypair_batch(SABER, coins, nthreads)
     ct, ss = O.kem_enc_batch(SABER, pk, T.splitmix_bytes(seed + 1, n * 32).reshape(n, 32), nthreads)
-    t0 = time.perf_counter()
-    ss2, fail = O.kem_dec_batch(SABER, ct, sk, nthreads)
-    dt = time.perf_counter() - t0
+    O.set_polmul(O.POLMUL_TOOM4K)
+    try:
+        t0 = time.perf_counter()
+        ss2, fail = O.kem_dec_batch(SABER, ct, sk, nthreads)
+        dt = time.perf_counter() - t0
+    finally:
+        O.set_polmul(O.POLMUL_SCHOOLBOOK)
     assert np.array_equal(ss, ss2) and not fail.any()
     return n / dt, (ct, sk, ss)
+
+
+def cpu_latency_batch1(iters: int = 1000):
+    """Config 1: Saber keypair / encapsulation / decapsulation at batch 1 on
+    one host thread (the oracle with the reference's multiplication), per-call
+    p50 / p99 over `iters` calls each, timed in C."""
+    from oracle import pyoracle as O
+    O.build()
+    out = {}
+    O.set_polmul(O.POLMUL_TOOM4K)
+    try:
+        for op, name in (("keypair", "keypair"), ("enc", "encaps"), ("dec", "decaps")):
+            ns = O.kem_latency_ns(SABER, op, iters)
+            out[name] = {"p50_us": float(np.percentile(ns, 50)) / 1e3,
+                         "p99_us": float(np.percentile(ns, 99)) / 1e3,
+                         "mean_us": float(ns.mean()) / 1e3, "calls": iters}
+    finally:
+        O.set_polmul(O.POLMUL_SCHOOLBOOK)
+    out["note"] = ("CPU oracle (C restatement of the reference's serial code, Toom-Cook 4-way over "
+                   "Karatsuba as the reference's pol_mul), one host thread, gcc -O3")
+    return out
 
 
 def run_reference(args):
@@ -147,29 +242,36 @@ def run_reference(args):
     from oracle import pyoracle as O
     import tmvpkem as T
     nthreads = os.cpu_count() or 1
-    sample = args.ref_sample
+    n = args.batch
     O.build()
-    coins = T.splitmix_bytes(7, sample * 96).reshape(sample, 96)
+    coins = T.splitmix_bytes(7, n * 96).reshape(n, 96)
     pk, sk = O.kem_keypair_batch(SABER, coins, nthreads)
-    ct, ss = O.kem_enc_batch(SABER, pk, T.splitmix_bytes(8, sample * 32).reshape(sample, 32), nthreads)
-    for _ in range(args.warmup):
-        O.kem_dec_batch(SABER, ct, sk, nthreads)
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        ss2, fail = O.kem_dec_batch(SABER, ct, sk, nthreads)
-        times.append(time.perf_counter() - t0)
-        assert np.array_equal(ss, ss2) and not fail.any()
+    ct, ss = O.kem_enc_batch(SABER, pk, T.splitmix_bytes(8, n * 32).reshape(n, 32), nthreads)
+    O.set_polmul(O.POLMUL_TOOM4K)
+    try:
+        for _ in range(args.warmup):
+            O.kem_dec_batch(SABER, ct, sk, nthreads)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            ss2, fail = O.kem_dec_batch(SABER, ct, sk, nthreads)
+            times.append(time.perf_counter() - t0)
+            assert np.array_equal(ss, ss2) and not fail.any()
+    finally:
+        O.set_polmul(O.POLMUL_SCHOOLBOOK)
     step = statistics.mean(times)
-    value = sample / step
-    desc = (f"CPU oracle (C port of the reference's serial Keccak/CBD/pack code, schoolbook "
-            f"multiplication), {sample} of the {BATCH} decapsulations per step")
+    value = n / step
+    desc = (f"CPU oracle (C restatement of the reference's serial Keccak/CBD/pack code, Toom-Cook 4-way "
+            f"over Karatsuba multiplication as the reference's pol_mul, gcc -O3), all {n} decapsulations "
+            f"per step on {nthreads} threads")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step * 1e3 * BATCH / sample,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
             "data": "synthetic: SplitMix64-seeded keys and ciphertexts",
             "config": {"workload": "Saber l=3 decapsulation, batch 65536, per-instance keys",
-                       "batch": BATCH, "sample_per_step": sample},
+                       "batch": n},
+            "latency_ms": {"p50": float(np.percentile(times, 50)) * 1e3,
+                           "p99": float(np.percentile(times, 99)) * 1e3, "batch": n},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                              "sample": desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -249,8 +351,13 @@ def run_ours(args):
         pass
     sampler = ClockSampler(gpu_id)
     sampler.wait_started()
+    nvml = NvmlSampler(gpu_id)
     total_ms, per_ms, launches, stages, exact_main = timed(T.FORM_AUTO, args.steps, stage_timing=True)
-    clocks = sampler.stop(window[0], window[1])
+    clocks_nvml = nvml.stop(window[0], window[1])
+    clocks_smi = sampler.stop(window[0], window[1])
+    clocks = clocks_nvml or clocks_smi
+    if clocks_nvml and clocks_smi:
+        clocks = dict(clocks_nvml, nvidia_smi=clocks_smi)
     if ws > 1:
         import torch.distributed as dist
         t = torch.tensor([total_ms], device=dev)
@@ -320,39 +427,35 @@ def run_ours(args):
                                     os.cpu_count() or 1)
         oracle_ok = bool(np.array_equal(oss, ss.cpu().numpy()[idx]) and not fail.any())
 
-    # ---- roofline of the dominant kernel: the tcgen05 re-encryption, the largest share of the
-    # decapsulation launch list, timed live with CUDA events on the stream it runs on
+    # ---- roofline: the dominant kernel of the step and the other large kernels beside it.
+    # In the pass the stages overlap (the Keccak front on a side stream beside the decryption,
+    # two chunk chains on two lanes), so a stage's events there also count the time it shares
+    # the GPU.  A second run with every stage alone on one stream (tmvp_ctx_set_serial) gives
+    # each kernel's own duration, CUDA events on the stream it runs on; the dominant kernel is
+    # the one with the largest share of that serialised step.
     hbm, bf16, peak_src = _peaks()
-    reenc = next((k for k in stages if k.startswith("cpa_reenc")), None)
-    if reenc is None:
-        reenc = max(stages.items(), key=lambda kv: kv[1][1])[0]
-    cnt, ms = stages[reenc]
-    avg_s = ms / cnt / 1e3
-    per_launch = n * args.steps / cnt  # instances per launch (device batches run in chunks)
-    traffic = _ncu_traffic(reenc)
-    if traffic is not None:
-        traffic = traffic * per_launch / n  # the ncu figure is per full-batch launch
-    ops = per_launch * 12 * POLY_OPS  # 12 negacyclic 256x256 products per re-encryption
-    ach = ops / avg_s / 1e12
     props = torch.cuda.get_device_properties(dev)
     sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
-    mma_floor_s = per_launch * REENC_MMAS * MMA_CYCLES / (props.multi_processor_count * sm_mhz * 1e6)
-    roof = {"kernel": reenc, "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
-            "frac": ach / bf16,
-            "peak_source": f"{peak_src} bf16 dense; achieved = schoolbook-equivalent integer ops",
-            "traffic": traffic, "avg_launch_ms": avg_s * 1e3,
-            "algorithmic": "per instance: 12 products x 2*256^2 ops; 6593 bytes",
-            "mma_instruction_floor_ms": mma_floor_s * 1e3,
-            "frac_of_mma_floor": mma_floor_s / avg_s,
-            "mma_floor_note": f"{REENC_MMAS} tcgen05.mma (M=128, N=32, K=32) per instance at "
-                              f"{MMA_CYCLES} SM cycles each"}
-    front = stages.get("dec_front")
-    if front:
-        fs = front[1] / front[0] / 1e3
-        roof["keccak_front"] = {"kernel": "dec_front (GenMatrix 23 + H(c) 9 Keccak-f per instance)",
-                                "gperm_per_s": (n * args.steps / front[0]) * 32 / fs / 1e9,
-                                "avg_launch_ms": fs * 1e3,
-                                "bound": "integer ALU pipe"}
+    diag = _diag_peaks(ctx, props.multi_processor_count, sm_mhz) if not args.no_diag else {}
+    ks = max(10, args.steps // 10)
+    ctx.set_serial(True)
+    try:
+        _, _, _, stages_iso, exact_iso = timed(T.FORM_AUTO, ks, stage_timing=True)
+    finally:
+        ctx.set_serial(False)
+    exact_main = exact_main and exact_iso
+    roof_all = _roofline_entries(stages_iso, n * ks, hbm, bf16, peak_src, diag,
+                                 props.multi_processor_count, sm_mhz)
+    for k, v in roof_all.items():  # the same kernel inside the pipelined pass
+        if k in stages and stages[k][0]:
+            v["avg_launch_ms_in_pass"] = stages[k][1] / stages[k][0]
+            v["instances_per_launch_in_pass"] = n * args.steps / stages[k][0]
+    lead = max(roof_all, key=lambda k: roof_all[k]["share_of_stage_time"]) if roof_all else None
+    roof = dict(roof_all[lead]) if lead else {}
+    if lead:
+        roof["dominant_by"] = ("largest share of the serialised step (every stage alone on one stream, "
+                               f"{ks} steps, CUDA events on that stream)")
+        roof["others"] = {k: v for k, v in roof_all.items() if k != lead}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -371,10 +474,13 @@ def run_ours(args):
         "bit_exact": {"all_keys_match": exact_main and all(form_exact.values()) and e2e_exact,
                       "checked": n, "oracle_sample": 256, "oracle_match": oracle_ok},
         "roofline": roof,
-        "stages_ms_per_step": {k: v[1] / max(v[0], 1) for k, v in stages.items()},
+        "stages_ms_per_launch_in_pass": {k: v[1] / max(v[0], 1) for k, v in stages.items()},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * (CT_BYTES + SK_BYTES),
                 "d2h_bytes_per_step": n * 32, "ms_per_step": statistics.mean(e2e_ms),
-                "host_chunk_ramp": e2e_chunk[0], "ms_by_host_chunk_ramp": e2e_chunk[1]},
+                "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99)),
+                "host_chunk_ramp": e2e_chunk[0], "setting": "library default host chunk and ramp"},
+        "e2e_sweep": {"ms_by_host_chunk_ramp": e2e_chunk[1],
+                      "note": "the other host chunk / ramp settings, timed after the reported default"},
         "cached_genmatrix": cached,
         "one_key": one_key,
         "oracle_sample_note": "256 random instances decapsulated by the CPU oracle and compared",
@@ -383,11 +489,16 @@ def run_ours(args):
     }
     if not args.no_extra:
         line["workloads"] = _workloads(ctx, T, dev, sp, stream, args)
+    if not args.no_latency:
+        line["latency"] = {"gpu_by_batch": _gpu_latency(ctx, T, dev, sp, args)}
+        if rank == 0 and not args.no_cpu:
+            line["latency"]["cpu_batch1"] = cpu_latency_batch1()
     if rank == 0 and not args.no_cpu:
         rate, _ = cpu_decaps_rate(args.cpu_sample, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-                                "sample": f"{args.cpu_sample} Saber decapsulations (oracle C port, "
-                                          f"schoolbook), all host threads"}
+                                "sample": f"{args.cpu_sample} Saber decapsulations (oracle C restatement of "
+                                          f"the reference's serial code with its Toom-Cook 4-way / Karatsuba "
+                                          f"multiplication, gcc -O3), all host threads"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -398,37 +509,179 @@ def run_ours(args):
 
 
 def _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws):
+    """Host-buffer decapsulation through the C ABI at the library's default
+    host chunk / ramp (the reported figure), then the other settings (a
+    separate sweep, not used for the reported figure)."""
     import torch
     ct_h = ct.cpu().pin_memory()
     sk_h = sk.cpu().pin_memory()
     ss_h = torch.empty((n, 32), dtype=torch.uint8).pin_memory()
     ke = max(3, args.steps // 2)
-    best = None
-    sweep = {}
-    # the copy/compute chunk of the host-buffer path and the ramp of its first
-    # chunks: the library's knobs, set per run
-    for chunk, ramp in ((8192, 0), (8192, 1), (16384, 0), (16384, 1), (16384, 2), (16384, 3),
-                        (32768, 2), (32768, 3), (32768, 4), (0, 0)):
-        ctx.set_host_chunk(chunk)
-        ctx.set_host_ramp(ramp)
+
+    def run(steps):
         for _ in range(min(2, args.warmup)):
             ctx.kem_dec_ptr(SABER, n, ss_h, ct_h, sk_h, T.FORM_AUTO, sp)
-        e2e_ms = []
-        for _ in range(ke):
+        ms = []
+        for _ in range(steps):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
             ctx.kem_dec_ptr(SABER, n, ss_h, ct_h, sk_h, T.FORM_AUTO, sp)
             b.record(stream)
             b.synchronize()
-            e2e_ms.append(a.elapsed_time(b))
-        e2e_exact = bool(torch.equal(ss_h, ss_ref.cpu()))
-        sweep[f"{chunk}/{ramp}"] = statistics.mean(e2e_ms)
-        if best is None or statistics.mean(e2e_ms) < statistics.mean(best[0]):
-            best = (e2e_ms, e2e_exact, f"{chunk}/{ramp}")
-    ctx.set_host_chunk(16384)
-    ctx.set_host_ramp(1)
-    e2e_ms, e2e_exact, chunk = best
-    return e2e_ms, e2e_exact, ws * n / (statistics.mean(e2e_ms) / 1e3), (chunk, sweep)
+            ms.append(a.elapsed_time(b))
+        return ms, bool(torch.equal(ss_h, ss_ref.cpu()))
+
+    default = (DEFAULT_HOST_CHUNK, DEFAULT_HOST_RAMP)
+    e2e_ms, e2e_exact = run(ke)
+    sweep = {f"{default[0]}/{default[1]}": statistics.mean(e2e_ms)}
+    if not args.no_sweep:
+        for chunk, ramp in ((8192, 0), (8192, 1), (16384, 0), (16384, 2), (16384, 3),
+                            (32768, 2), (32768, 3), (32768, 4), (0, 0)):
+            ctx.set_host_chunk(chunk)
+            ctx.set_host_ramp(ramp)
+            ms, ok = run(max(3, ke // 2))
+            e2e_exact = e2e_exact and ok
+            sweep[f"{chunk}/{ramp}"] = statistics.mean(ms)
+        ctx.set_host_chunk(default[0])
+        ctx.set_host_ramp(default[1])
+    return e2e_ms, e2e_exact, ws * n / (statistics.mean(e2e_ms) / 1e3), (f"{default[0]}/{default[1]}", sweep)
+
+
+def _gpu_latency(ctx, T, dev, sp, args):
+    """Per-call latency through the C ABI with pinned host buffers (copies in
+    and out inside the call): host wall time of tmvp_kem_dec_batch at batch
+    1 ... 65536, and of key generation and encapsulation at batch 1."""
+    import torch
+    out = {}
+    nmax = max(args.latency_batches)
+    coins = torch.from_numpy(T.splitmix_bytes(4711, nmax * 96).reshape(nmax, 96))
+    ec = torch.from_numpy(T.splitmix_bytes(4712, nmax * 32).reshape(nmax, 32))
+    pk_d = torch.empty((nmax, PK_BYTES), dtype=torch.uint8, device=dev)
+    sk_d = torch.empty((nmax, SK_BYTES), dtype=torch.uint8, device=dev)
+    ct_d = torch.empty((nmax, CT_BYTES), dtype=torch.uint8, device=dev)
+    ss_d = torch.empty((nmax, 32), dtype=torch.uint8, device=dev)
+    ctx.kem_keypair_ptr(SABER, nmax, pk_d, sk_d, coins.to(dev), T.FORM_AUTO, sp)
+    ctx.kem_enc_ptr(SABER, nmax, ct_d, ss_d, pk_d, ec.to(dev), T.FORM_AUTO, sp)
+    torch.cuda.synchronize()
+    ct_h, sk_h, ss_ref = ct_d.cpu().pin_memory(), sk_d.cpu().pin_memory(), ss_d.cpu()
+    pk_h = pk_d.cpu().pin_memory()
+    coins_h, ec_h = coins.pin_memory(), ec.pin_memory()
+    out_h = torch.empty((nmax, 32), dtype=torch.uint8).pin_memory()
+
+    def percentiles(fn, calls):
+        for _ in range(3):
+            fn()
+        t = []
+        for _ in range(calls):
+            t0 = time.perf_counter()
+            fn()
+            t.append(time.perf_counter() - t0)
+        t = np.array(t) * 1e3
+        return {"p50_ms": float(np.percentile(t, 50)), "p99_ms": float(np.percentile(t, 99)),
+                "mean_ms": float(t.mean()), "calls": calls}
+
+    for b in args.latency_batches:
+        calls = 1000 if b <= 256 else (200 if b <= 4096 else 50)
+        r = percentiles(lambda b=b: ctx.kem_dec_ptr(SABER, b, out_h, ct_h, sk_h, T.FORM_AUTO, sp), calls)
+        r["bit_exact"] = bool(torch.equal(out_h[:b], ss_ref[:b]))
+        r["decaps_per_s"] = b / (r["mean_ms"] / 1e3)
+        out[f"decaps_{b}"] = r
+    pk1 = torch.empty((1, PK_BYTES), dtype=torch.uint8).pin_memory()
+    sk1 = torch.empty((1, SK_BYTES), dtype=torch.uint8).pin_memory()
+    ct1 = torch.empty((1, CT_BYTES), dtype=torch.uint8).pin_memory()
+    ss1 = torch.empty((1, 32), dtype=torch.uint8).pin_memory()
+    out["keypair_1"] = percentiles(lambda: ctx.kem_keypair_ptr(SABER, 1, pk1, sk1, coins_h[:1], T.FORM_AUTO, sp), 1000)
+    out["encaps_1"] = percentiles(lambda: ctx.kem_enc_ptr(SABER, 1, ct1, ss1, pk_h[:1], ec_h[:1], T.FORM_AUTO, sp), 1000)
+    out["encaps_1"]["bit_exact"] = bool(torch.equal(ct1[0], ct_h[0]) and torch.equal(ss1[0], ss_ref[0]))
+    out["note"] = ("host wall time per synchronous C-ABI call with pinned host buffers (host-to-device "
+                   "copies of the inputs and the device-to-host copy of the outputs inside the call)")
+    return out
+
+
+def _diag_peaks(ctx, nsm, sm_mhz):
+    """Live ceilings measured with the library's own diagnostic kernels: the
+    Keccak-f[1600] rate at full occupancy (integer pipe) and the dense e4m3
+    tcgen05 rate (kind::f8f6f4, M = 128, N = 256, K = 32)."""
+    out = {}
+    try:
+        rate, blocks = ctx.keccak_rate(64)
+        out["keccak_perm_per_s"] = rate
+        out["keccak_blocks_per_sm"] = blocks
+    except Exception:
+        pass
+    try:
+        _, cyc = ctx.umma_rate(0, 256, ctas_per_sm=2, iters=4096)
+        out["e4m3_tflops"] = 2 * 128 * 256 * 32 / cyc * nsm * sm_mhz * 1e6 / 1e12
+        out["e4m3_cycles_per_mma_n256"] = cyc
+    except Exception:
+        pass
+    return out
+
+
+# Per Saber instance: (stage prefix, products, algorithmic bytes, Keccak-f, note)
+_STAGE_WORK = {
+    "dec_front": (0, 1088 + 32 + 3744 + 32, 32,
+                  "GenMatrix (23 Keccak-f) + H(c) (9): reads ct 1088 + seed 32, writes the GenMatrix "
+                  "stream 3744 + H(c) 32 bytes"),
+    "dec_g": (0, 64 + 64 + 768, 6, "G (1 Keccak-f) + GenSecret (5): reads m'||H(pk) 64, writes kr 64 + "
+                                   "GenSecret stream 768 bytes"),
+    "cpa_reenc": (12, 6593, 0, "12 products x 2*256^2 ops; 6593 bytes"),
+    "cpa_decrypt": (3, 1088 + 1248 + 64, 0, "3 products x 2*256^2 ops; reads ct 1088 + secret 1248, "
+                                            "writes m' || H(pk) 64 bytes"),
+    "final_key": (0, 64 + 32 + 1 + 32 + 32, 1, "1 Keccak-f; reads kr, H(c), fail, z, writes K"),
+}
+
+
+def _roofline_entries(stages, instances, hbm, bf16, peak_src, diag, nsm, sm_mhz):
+    """One roofline record per large stage: the Keccak stages against HBM
+    (bound 'hbm': their algorithmic bytes) with their permutation rate against
+    the measured Keccak ceiling, the tensor-core stages against the measured
+    e4m3 rate (or the bf16 figure as a stand-in) and their MMA-issue floor."""
+    total = sum(v[1] for v in stages.values()) or 1.0
+    out = {}
+    for name, (cnt, ms) in stages.items():
+        key = next((k for k in _STAGE_WORK if name.startswith(k)), None)
+        if key is None or cnt == 0:
+            continue
+        prods, nbytes, perms, note = _STAGE_WORK[key]
+        avg_s = ms / cnt / 1e3
+        per_launch = instances / cnt
+        rec = {"kernel": name, "avg_launch_ms": avg_s * 1e3, "launches": cnt,
+               "share_of_stage_time": ms / total, "instances_per_launch": per_launch,
+               "algorithmic": note}
+        traffic = _ncu_traffic(name)
+        rec["traffic"] = traffic * per_launch / BATCH if traffic is not None else None
+        if prods:
+            ops = per_launch * prods * POLY_OPS
+            ach = ops / avg_s / 1e12
+            peak = diag.get("e4m3_tflops")
+            rec.update({"bound": "tensor", "achieved": ach, "unit": "TFLOP/s"})
+            if peak:
+                rec.update({"peak": peak, "frac": ach / peak,
+                            "peak_source": "measured live: dense e4m3 tcgen05 rate from the library's "
+                                           "issue-rate diagnostic (kind::f8f6f4 M=128 N=256 K=32) at the "
+                                           "sampled SM clock; achieved = schoolbook-equivalent integer ops"})
+            else:
+                rec.update({"peak": bf16, "frac": ach / bf16,
+                            "peak_source": f"{peak_src} bf16 dense as a stand-in for e4m3"})
+            mmas, cyc, ncol = (REENC_MMAS, MMA_CYCLES, 32) if key == "cpa_reenc" else (DEC_MMAS, MMA_CYCLES_N16, 16)
+            floor_s = per_launch * mmas * cyc / (nsm * sm_mhz * 1e6)
+            rec["mma_instruction_floor_ms"] = floor_s * 1e3
+            rec["frac_of_mma_floor"] = floor_s / avg_s
+            rec["mma_floor_note"] = f"{mmas} tcgen05.mma (M=128, N={ncol}, K=32) per instance at {cyc} SM cycles each"
+        else:
+            gbs = per_launch * nbytes / avg_s / 1e9
+            rec.update({"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                        "peak_source": f"{peak_src} HBM copy bandwidth"})
+            if perms:
+                rate = per_launch * perms / avg_s
+                rec["keccak"] = {"perm_per_s": rate, "peak_perm_per_s": diag.get("keccak_perm_per_s"),
+                                 "frac": rate / diag["keccak_perm_per_s"] if diag.get("keccak_perm_per_s") else None,
+                                 "bound": "integer ALU pipe (LOP3 / funnel shifts)",
+                                 "peak_source": "measured live: the library's Keccak-rate diagnostic at full "
+                                                "occupancy"}
+        out[name] = rec
+    return out
 
 
 def _event_ms(stream, fn, steps, warmup=2):
@@ -574,7 +827,8 @@ def _workloads(ctx, T, dev, sp, stream, args):
                 rates[name][str(ncol)] = {"sm_cycles_per_mma": per_sm, "ctas_per_sm": ctas,
                                           "k_elements": 32 if kind == 0 else 16}
         out["tcgen05_mma_cycles"] = rates
-    # serving loop: Poisson arrivals over LightSaber, Saber, FireSaber and Sable
+    # serving loop: Poisson arrivals over LightSaber, Saber, FireSaber and Sable (the configured
+    # 200 K req/s), then a sweep of offered loads up to saturation
     if "serving" in W:
         rate, secs = 200_000.0, 2.0
         srv = T.Server(device=dev.index or 0, max_batch=4096, slots=4, form=T.FORM_AUTO)
@@ -583,20 +837,59 @@ def _workloads(ctx, T, dev, sp, stream, args):
             for k, sid in enumerate((0, 1, 2, 4)):
                 kpk, ksk = ctx.kem_keypair(sid, T.splitmix_bytes(500 + k, 256 * 96).reshape(256, 96))
                 ids.append(srv.add_keys(sid, kpk, ksk))
-            # warm-up at the same load (module loading, workspace growth), then the measured run
-            srv.loadgen(rate=rate, seconds=0.25, seed=20, key_ids=np.concatenate(ids), decaps_fraction=0.5)
+            ids = np.concatenate(ids)
+            # warm-up at the same load (module loading, first-touch of the arena), then the measured run
+            srv.loadgen(rate=rate, seconds=0.25, seed=20, key_ids=ids, decaps_fraction=0.5)
             srv.reset_stats()
-            nreq = srv.loadgen(rate=rate, seconds=secs, seed=21, key_ids=np.concatenate(ids),
-                               decaps_fraction=0.5)
+            nreq = srv.loadgen(rate=rate, seconds=secs, seed=21, key_ids=ids, decaps_fraction=0.5)
             st = srv.stats()
+            out["serving"] = {"offered_req_per_s": rate, "seconds": secs, "requests": nreq,
+                              "throughput_req_per_s": st["throughput"], "p50_us": st["p50_us"],
+                              "p99_us": st["p99_us"], "max_us": st["max_us"], "mean_batch": st["mean_batch"],
+                              "batches": st["batches"], "slots": st["slots"], "failed": st["failed"],
+                              "decaps_checked": st["checked"], "decaps_mismatched": st["mismatched"],
+                              "arena_bytes": st["arena_bytes"], "peak_arena_bytes": st["peak_arena_bytes"],
+                              "mix": "encaps/decaps 50/50 over LightSaber, Saber, FireSaber, Sable; 256 keys each",
+                              "warmup_s": 0.25}
+            sweep = []
+            for r in args.serving_rates:
+                srv.reset_stats()
+                nq = srv.loadgen(rate=r, seconds=args.serving_seconds, seed=int(r) % 1000 + 31, key_ids=ids,
+                                 decaps_fraction=0.5)
+                st = srv.stats()
+                sweep.append({"offered_req_per_s": r, "requests": nq, "throughput_req_per_s": st["throughput"],
+                              "p50_us": st["p50_us"], "p99_us": st["p99_us"], "mean_batch": st["mean_batch"],
+                              "failed": st["failed"], "decaps_mismatched": st["mismatched"]})
+            out["serving_sweep"] = {"points": sweep, "seconds_per_point": args.serving_seconds,
+                                    "note": "same server, keys and mix; throughput = completed requests / "
+                                            "elapsed since the point's start (the generator's own pace "
+                                            "caps the highest offered loads)"}
         finally:
             srv.close()
-        out["serving"] = {"offered_req_per_s": rate, "seconds": secs, "requests": nreq,
-                          "throughput_req_per_s": st["throughput"], "p50_us": st["p50_us"],
-                          "p99_us": st["p99_us"], "max_us": st["max_us"], "mean_batch": st["mean_batch"],
-                          "batches": st["batches"], "slots": st["slots"], "failed": st["failed"],
-                          "mix": "encaps/decaps 50/50 over LightSaber, Saber, FireSaber, Sable; 256 keys each",
-                          "warmup_s": 0.25}
+        # memory admission under pressure: an arena of 1/32 of one batch of the largest set (room
+        # for ~128 requests) at 1.6 M requests/s
+        probe = T.Server(device=dev.index or 0, max_batch=4096, slots=1, form=T.FORM_AUTO)
+        one_batch = probe.stats()["arena_bytes"]
+        probe.close()
+        srv = T.Server(device=dev.index or 0, max_batch=4096, slots=4, form=T.FORM_AUTO,
+                       mem_budget=one_batch // 32)
+        try:
+            ids = []
+            for k, sid in enumerate((0, 1, 2, 4)):
+                kpk, ksk = ctx.kem_keypair(sid, T.splitmix_bytes(700 + k, 64 * 96).reshape(64, 96))
+                ids.append(srv.add_keys(sid, kpk, ksk))
+            srv.reset_stats()
+            nq = srv.loadgen(rate=1_600_000.0, seconds=0.5, seed=77, key_ids=np.concatenate(ids),
+                             decaps_fraction=0.5)
+            st = srv.stats()
+            out["serving_small_arena"] = {
+                "offered_req_per_s": 1_600_000.0, "requests": nq, "throughput_req_per_s": st["throughput"],
+                "p50_us": st["p50_us"], "p99_us": st["p99_us"], "mean_batch": st["mean_batch"],
+                "arena_bytes": st["arena_bytes"], "peak_arena_bytes": st["peak_arena_bytes"],
+                "admission_waits": st["admission_waits"], "admission_splits": st["admission_splits"],
+                "failed": st["failed"], "decaps_mismatched": st["mismatched"]}
+        finally:
+            srv.close()
     return out
 
 
@@ -620,12 +913,19 @@ def _ncu_traffic(kernel: str):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--cpu-sample", type=int, default=16384)
-    ap.add_argument("--ref-sample", type=int, default=16384)
+    ap.add_argument("--no-latency", action="store_true", help="skip the per-call latency measurements")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the host chunk / ramp sweep")
+    ap.add_argument("--no-diag", action="store_true", help="skip the Keccak / tensor-core ceiling diagnostics")
+    ap.add_argument("--serving-rates", default="100000,200000,400000,800000,1600000,3200000,6400000",
+                    help="offered loads of the serving sweep, requests/s (comma list)")
+    ap.add_argument("--serving-seconds", type=float, default=0.5)
+    ap.add_argument("--latency-batches", default="1,16,256,4096,65536",
+                    help="batches of the per-call latency curve (comma list)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (e2e) leg")
     ap.add_argument("--no-oracle", action="store_true", help="skip the oracle sample check")
@@ -637,6 +937,8 @@ def main():
     ap.add_argument("--forms", default="fp8_tc,int8_tc,cuda_core,dp2a,toom_cook",
                     help="forms to time besides the headline (AUTO) form (comma list, or 'none')")
     args = ap.parse_args()
+    args.latency_batches = [int(x) for x in args.latency_batches.split(",") if x]
+    args.serving_rates = [float(x) for x in args.serving_rates.split(",") if x]
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

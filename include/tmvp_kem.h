@@ -208,6 +208,17 @@ int tmvp_ctx_set_host_ramp(tmvp_ctx *ctx, int steps);
  * decryption; 0 = one chain over the whole batch.  Default 32768; n must
  * be 0 or >= 1024.  Results do not depend on it. */
 int tmvp_ctx_set_dev_chunk(tmvp_ctx *ctx, size_t n);
+/* on != 0: decapsulation runs every stage on the caller's stream, one after
+ * the other and unchunked (no side stream, no lanes), so that the per-stage
+ * timing (tmvp_ctx_set_timing) measures each kernel alone on the GPU.  Slower;
+ * for measurement.  Results do not depend on it.  Default 0. */
+int tmvp_ctx_set_serial(tmvp_ctx *ctx, int on);
+/* Caps the Keccak front of decapsulation (GenMatrix + H(c), one launch beside
+ * the decryption) at blocks_per_sm 64-thread blocks per SM, its threads then
+ * striding over the sponges, so that decryption CTAs fit beside it on every
+ * SM; 0 (the default) launches one thread per sponge.  0..64.  Results do
+ * not depend on it. */
+int tmvp_ctx_set_front_cap(tmvp_ctx *ctx, int blocks_per_sm);
 
 /* ---------------------------------------------------------------------------
  * Request-serving loop with device-resident keys and continuous batching.
@@ -215,12 +226,16 @@ int tmvp_ctx_set_dev_chunk(tmvp_ctx *ctx, size_t n);
  *
  * Requests (one KEM operation each) are queued per (parameter set, op).  A
  * scheduler thread turns the queue with the oldest waiting request into a
- * batch of up to max_batch requests whenever one of `slots` batch slots is
- * free; each slot owns its workspace and CUDA stream, so up to `slots`
- * batches run on the GPU at once while new requests keep arriving.  The slot
- * count is the configured one reduced until all slots' device memory fits
- * mem_budget (memory-based admission).  Keys live in device tables and are
- * gathered per batch by index.
+ * batch whenever one of `slots` batch slots is free (each slot owns a context
+ * and CUDA stream, so up to `slots` batches run on the GPU at once while new
+ * requests keep arriving).  Memory admission: every batch in flight holds a
+ * block of one device arena (mem_budget bytes, or by default what `slots`
+ * batches of max_batch requests of the largest set need) for its inputs,
+ * outputs, gathered keys and matrices and KEM workspace; a batch takes as many
+ * requests (up to max_batch) as the largest free block holds for its own set
+ * and operation, and waits for a batch to finish when not even one fits.
+ * Keys live in device tables (outside the arena) and are gathered per batch
+ * by index.
  *   encaps: in = 32 random bytes,   out = ct || ss   (ct_bytes + 32 bytes)
  *   decaps: in = ct (ct_bytes),     out = ss         (32 bytes)
  * `in` and `out` must stay valid until the request completes.
@@ -228,7 +243,8 @@ int tmvp_ctx_set_dev_chunk(tmvp_ctx *ctx, size_t n);
 typedef struct tmvp_server tmvp_server;
 typedef struct {
   int device;
-  size_t mem_budget; /* device bytes for slots (0 = no cap)            */
+  size_t mem_budget; /* device bytes of the batch arena (0 = default);
+                        must hold one request of every set             */
   int max_batch;     /* largest batch per launch, 1..65536 (0 = 4096)  */
   int slots;         /* batches in flight (0 = 4)                      */
   int form;          /* tmvp_form used for every batch                 */
@@ -238,11 +254,17 @@ typedef struct {
   double mean_batch;          /* requests per batch             */
   double p50_us, p99_us, max_us; /* submit-to-completion latency */
   double elapsed_s, throughput;  /* since the last reset         */
-  int slots;                     /* slots admitted by the budget */
+  int slots;                     /* batch slots                  */
   uint64_t failed;               /* requests of batches whose launch failed
                                     (their outputs are not written) */
   uint64_t one_key_batches;      /* decapsulation batches whose requests all
                                     used one key (tmvp_kem_dec_batch_onekey) */
+  uint64_t arena_bytes;          /* device bytes of the batch arena */
+  uint64_t peak_arena_bytes;     /* most arena bytes held at once   */
+  uint64_t admission_waits;      /* times a batch waited for arena memory */
+  uint64_t admission_splits;     /* batches cut short by arena memory     */
+  uint64_t checked, mismatched;  /* load generator: decapsulations checked
+                                    against the encapsulated key, and wrong */
 } tmvp_server_stats;
 enum { TMVP_OP_ENCAPS = 0, TMVP_OP_DECAPS = 1 };
 int tmvp_server_create(const tmvp_server_config *cfg, tmvp_server **out);
@@ -260,7 +282,11 @@ int tmvp_server_get_stats(tmvp_server *srv, tmvp_server_stats *out);
 void tmvp_server_reset_stats(tmvp_server *srv);
 /* Load generator for benchmarking: Poisson arrivals at `rate` requests/s for
  * `seconds`, keys drawn uniformly from key_ids, decapsulations with
- * probability decaps_fraction (of a ciphertext made once per key), seeded. */
+ * probability decaps_fraction (of a ciphertext made once per key), seeded.
+ * Every decapsulation's key is checked against the encapsulated one
+ * (stats.checked / stats.mismatched).  Waits are bounded: TMVP_ETIMEOUT if the
+ * server does not finish the requests in time (their buffers then stay with
+ * the server until it is destroyed). */
 int tmvp_server_loadgen(tmvp_server *srv, double rate, double seconds, uint64_t seed,
                         const uint32_t *key_ids, size_t nkeys, double decaps_fraction,
                         uint64_t *submitted);
@@ -308,6 +334,13 @@ int tmvp_selftest_bounded_wait(tmvp_ctx *ctx, void *stream);
  * MMA of one CTA (issue to completion), out[1] = out[0] / ctas_per_sm, the
  * SM's cycles per MMA.  A diagnostic with no counterpart in the reference. */
 int tmvp_diag_umma_rate(tmvp_ctx *ctx, int kind, int n, int ctas_per_sm, int iters, double *out);
+/* Keccak-f[1600] permutation rate at full occupancy (one register-resident
+ * state per thread, the hash stages' permutation, `perms` per thread, as
+ * many 64-thread blocks as fit on every SM): out[0] = permutations per
+ * second over the GPU, out[1] = resident blocks per SM.  The integer-pipe
+ * ceiling of the hash stages.  A diagnostic with no counterpart in the
+ * reference. */
+int tmvp_diag_keccak_rate(tmvp_ctx *ctx, int perms, double *out);
 
 /* ---------------------------------------------------------------------------
  * Mixed-parameter decapsulation.  No counterpart in the reference (one

@@ -51,6 +51,9 @@ def lib():
         L.orc_polmul_schoolbook.argtypes = [P, P, P]
         L.orc_polmul_tmvp2.argtypes = [P, P, P]
         L.orc_polmul_toom4.argtypes = [P, P, P]
+        L.orc_polmul_toom4k.argtypes = [P, P, P]
+        L.orc_set_polmul.argtypes = [ctypes.c_int]
+        L.orc_kem_latency.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
         L.orc_matvec_batch.argtypes = [ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        P, P, P, ctypes.c_int]
         L.orc_indcpa_keypair.argtypes = [ctypes.c_int, P, P, P, P]
@@ -138,9 +141,30 @@ def polmul(a: np.ndarray, b: np.ndarray, method: str = "schoolbook") -> np.ndarr
     b = np.ascontiguousarray(b, dtype=np.uint16)
     r = np.zeros(256, np.uint16)
     fn = {"schoolbook": lib().orc_polmul_schoolbook, "tmvp2": lib().orc_polmul_tmvp2,
-          "toom4": lib().orc_polmul_toom4}[method]
+          "toom4": lib().orc_polmul_toom4, "toom4k": lib().orc_polmul_toom4k}[method]
     fn(_p(r), _p(a), _p(b))
     return r
+
+
+POLMUL_SCHOOLBOOK, POLMUL_TOOM4K = 0, 1
+
+
+def set_polmul(which: int) -> None:
+    """Multiplication of the IND-CPA / KEM functions: POLMUL_SCHOOLBOOK (the
+    default, used for parity) or POLMUL_TOOM4K (Toom-Cook 4-way with two
+    Karatsuba levels, the reference's serial pol_mul; the CPU baseline)."""
+    if lib().orc_set_polmul(which) != 0:
+        raise ValueError(f"unknown multiplication {which}")
+
+
+def kem_latency_ns(set_id: int, op: str, iters: int) -> np.ndarray:
+    """Per-call wall time in ns of `iters` single-instance keypair / enc / dec
+    calls on the calling thread (timed in C with CLOCK_MONOTONIC)."""
+    ns = np.zeros(iters, np.float64)
+    rc = lib().orc_kem_latency(set_id, {"keypair": 0, "enc": 1, "dec": 2}[op], iters, _p(ns))
+    if rc != 0:
+        raise RuntimeError(f"orc_kem_latency failed ({rc})")
+    return ns
 
 
 def matvec(A: np.ndarray, s: np.ndarray, eq: int = 13, transpose: bool = False,

@@ -21,9 +21,22 @@ _libs: dict = {}
 SCHEMES = {"saber": "libref_saber.so", "sable": "libref_sable.so"}
 
 
-def build(ref_root: str) -> bool:
-    """Compile the reference kernels from ``ref_root``; False if absent."""
-    if not os.path.isdir(ref_root):
+def reference_root() -> str:
+    """Where the reference sources are read from: $TMVP_REFERENCE_ROOT, else
+    the recipe's own default (``make -C oracle/ref_build print-ref``)."""
+    env = os.environ.get("TMVP_REFERENCE_ROOT")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "-C", os.path.join(_HERE, "ref_build"), "print-ref"],
+                       capture_output=True, text=True)
+    return r.stdout.strip() if r.returncode == 0 else ""
+
+
+def build(ref_root: str | None = None) -> bool:
+    """Compile the reference kernels from ``ref_root`` (default:
+    reference_root()); False if the sources are absent."""
+    ref_root = ref_root or reference_root()
+    if not ref_root or not os.path.isdir(ref_root):
         return False
     subprocess.run(["make", "-s", "-C", os.path.join(_HERE, "ref_build"), f"REF={ref_root}"],
                    check=True)

@@ -10,9 +10,11 @@
  *   Saber family  TMVP-Saber/SABER-GPU/include/params.h:1-50
  *   Sable family  TMVP_SABLE/include/SABLE_params.h:1-73 (Saber_type 1/2/3)
  */
+#define _POSIX_C_SOURCE 200809L /* clock_gettime */
 #include "tmvp_oracle.h"
 
 #include <pthread.h>
+#include <time.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -101,23 +103,35 @@ static inline uint64_t rol64(uint64_t v, int n) {
 
 void orc_keccakf1600(uint64_t A[25]) {
   pthread_once(&g_keccak_once, keccak_init_tables);
+  /* the loops over x and y are unrolled so that every index is a constant
+   * and the state stays in registers (the CPU baseline runs this code) */
+  int rho[25];
+  for (int i = 0; i < 25; i++) rho[i] = g_rho[i];
+  uint64_t S[25];
+  for (int i = 0; i < 25; i++) S[i] = A[i];
   for (int ir = 0; ir < 24; ir++) {
     uint64_t C[5], D[5], B[25];
+#pragma GCC unroll 5
     for (int x = 0; x < 5; x++)
-      C[x] = A[x] ^ A[x + 5] ^ A[x + 10] ^ A[x + 15] ^ A[x + 20];
+      C[x] = S[x] ^ S[x + 5] ^ S[x + 10] ^ S[x + 15] ^ S[x + 20];
+#pragma GCC unroll 5
     for (int x = 0; x < 5; x++) D[x] = C[(x + 4) % 5] ^ rol64(C[(x + 1) % 5], 1);
-    for (int i = 0; i < 25; i++) A[i] ^= D[i % 5];
-    /* rho + pi: B[y, 2x+3y] = rot(A[x,y], r[x,y]) */
+    /* theta, then rho + pi: B[y, 2x+3y] = rot(A[x,y], r[x,y]) */
+#pragma GCC unroll 5
     for (int x = 0; x < 5; x++)
+#pragma GCC unroll 5
       for (int y = 0; y < 5; y++)
-        B[y + 5 * ((2 * x + 3 * y) % 5)] = rol64(A[x + 5 * y], g_rho[x + 5 * y]);
+        B[y + 5 * ((2 * x + 3 * y) % 5)] = rol64(S[x + 5 * y] ^ D[x], rho[x + 5 * y]);
     /* chi */
+#pragma GCC unroll 5
     for (int y = 0; y < 5; y++)
+#pragma GCC unroll 5
       for (int x = 0; x < 5; x++)
-        A[x + 5 * y] = B[x + 5 * y] ^ (~B[(x + 1) % 5 + 5 * y] & B[(x + 2) % 5 + 5 * y]);
+        S[x + 5 * y] = B[x + 5 * y] ^ (~B[(x + 1) % 5 + 5 * y] & B[(x + 2) % 5 + 5 * y]);
     /* iota */
-    A[0] ^= g_rc[ir];
+    S[0] ^= g_rc[ir];
   }
+  for (int i = 0; i < 25; i++) A[i] = S[i];
 }
 
 static uint64_t load64le(const uint8_t *x) {
@@ -184,9 +198,13 @@ void orc_shake128(uint8_t *out, size_t outlen, const uint8_t *in, size_t inlen) 
 /* stream of w-bit fields: 13-bit BS2POLq (SABER poly.cu:799-816), 11-bit   */
 /* BS2POLq_gpu2 (SABLE pack.cu:22-37), 10-bit BS2POLp/POLp2BS (SABER        */
 /* pack.cu:7-32), 9-bit (SABLE pack.cu:182-246), 4-bit POLT2BS/BS2POLT      */
-/* (SABER pack.cu:101-197, incl. the ET=3/6 variants), 5-bit (SABLE         */
-/* pack.cu:339-421), 2-bit secret (SABLE pack.cu:366-377) and 1-bit message */
-/* (SABER pack.cu:86-97, :201-212).                                          */
+/* (SABER pack.cu:114-120, :179-184), 5-bit (SABLE pack.cu:339-421), 2-bit  */
+/* secret (SABLE pack.cu:366-377) and 1-bit message (SABER pack.cu:86-97,  */
+/* :201-212).  The 3-bit (LightSaber) and 6-bit (FireSaber) c_m packings    */
+/* follow the reference's commented-out branches: ET = 3 packs eight 3-bit  */
+/* fields into three bytes (POLT2BS pack.cu:105-113, BS2POLT :165-178), ET  */
+/* = 6 four 6-bit fields into three bytes (POLT2BS :121-129, BS2POLT        */
+/* :185-194); both are the same little-endian field stream.                 */
 /* ------------------------------------------------------------------------ */
 
 void orc_pack_bits(uint8_t *out, const uint16_t *in, int n, int w) {
@@ -201,13 +219,14 @@ void orc_pack_bits(uint8_t *out, const uint16_t *in, int n, int w) {
 }
 
 void orc_unpack_bits(uint16_t *out, const uint8_t *in, int n, int w) {
+  const size_t nbytes = ((size_t)n * w + 7) / 8;
   for (int i = 0; i < n; i++) {
-    uint32_t v = 0;
-    for (int b = 0; b < w; b++) {
-      int bit = i * w + b;
-      v |= (uint32_t)((in[bit >> 3] >> (bit & 7)) & 1) << b;
-    }
-    out[i] = (uint16_t)v;
+    /* the field lies in the three bytes from bit i*w (w <= 16) */
+    const size_t bit = (size_t)i * w, byte = bit >> 3;
+    uint32_t win = in[byte];
+    if (byte + 1 < nbytes) win |= (uint32_t)in[byte + 1] << 8;
+    if (byte + 2 < nbytes) win |= (uint32_t)in[byte + 2] << 16;
+    out[i] = (uint16_t)((win >> (bit & 7)) & ((1u << w) - 1));
   }
 }
 
@@ -363,6 +382,94 @@ void orc_polmul_toom4(uint16_t r[256], const uint16_t a[256], const uint16_t b[2
   for (int i = 0; i < 256; i++) r[i] = (uint16_t)(full[i] - full[i + 256]);
 }
 
+/* Toom-Cook 4-way with two levels of Karatsuba for the seven 64 x 64
+ * products, the multiplication of the reference's serial pol_mul
+ * (TMVP_SABLE pack.cu:719-736) over toom_cook_4way (:590-714) and
+ * karatsuba_simple (:520-588, which splits a 64-coefficient product into
+ * halves and quarters: nine 16 x 16 schoolbook products).  As in the
+ * reference the products run in 16-bit arithmetic, so the evaluations are
+ * right mod 2^16 and the interpolation (toom4_interp's, which divides by at
+ * most 8 along any path) leaves every coefficient right mod 2^13: enough for
+ * every parameter set (q <= 2^13), not for 16-bit results.  This is the CPU
+ * baseline's multiplication; the parity checks use the schoolbook form. */
+static inline void sb16_u16(uint16_t *restrict r, const uint16_t *restrict a,
+                            const uint16_t *restrict b) {
+  uint16_t acc[32] = {0};
+  for (int j = 0; j < 16; j++)
+    for (int i = 0; i < 16; i++) acc[i + j] = (uint16_t)(acc[i + j] + a[i] * b[j]);
+  for (int i = 0; i < 32; i++) r[i] = acc[i];
+}
+
+/* r[0..62] = a * b for 32 coefficients: one Karatsuba level over halves. */
+static inline void kara32_u16(uint16_t r[64], const uint16_t *a, const uint16_t *b) {
+  uint16_t lo[32], hi[32], mid[32], as[16], bs[16];
+  for (int i = 0; i < 16; i++) {
+    as[i] = (uint16_t)(a[i] + a[16 + i]);
+    bs[i] = (uint16_t)(b[i] + b[16 + i]);
+  }
+  sb16_u16(lo, a, b);
+  sb16_u16(hi, a + 16, b + 16);
+  sb16_u16(mid, as, bs);
+  for (int i = 0; i < 64; i++) r[i] = 0;
+  for (int i = 0; i < 31; i++) {
+    r[i] += lo[i];
+    r[32 + i] += hi[i];
+    r[16 + i] += (uint16_t)(mid[i] - lo[i] - hi[i]);
+  }
+}
+
+/* r[0..126] = a * b for 64 coefficients: Karatsuba over halves again. */
+static void kara64_u16(uint16_t r[128], const uint16_t *a, const uint16_t *b) {
+  uint16_t lo[64], hi[64], mid[64], as[32], bs[32];
+  for (int i = 0; i < 32; i++) {
+    as[i] = (uint16_t)(a[i] + a[32 + i]);
+    bs[i] = (uint16_t)(b[i] + b[32 + i]);
+  }
+  kara32_u16(lo, a, b);
+  kara32_u16(hi, a + 32, b + 32);
+  kara32_u16(mid, as, bs);
+  for (int i = 0; i < 128; i++) r[i] = 0;
+  for (int i = 0; i < 63; i++) {
+    r[i] += lo[i];
+    r[64 + i] += hi[i];
+    r[32 + i] += (uint16_t)(mid[i] - lo[i] - hi[i]);
+  }
+}
+
+void orc_polmul_toom4k(uint16_t r[256], const uint16_t a[256], const uint16_t b[256]) {
+  uint32_t ea[7][64], eb[7][64], full[512];
+  uint16_t ha[7][64], hb[7][64], w[7][128];
+  toom4_eval(ea, a);
+  toom4_eval(eb, b);
+  for (int k = 0; k < 7; k++)
+    for (int i = 0; i < 64; i++) {
+      ha[k][i] = (uint16_t)ea[k][i];
+      hb[k][i] = (uint16_t)eb[k][i];
+    }
+  for (int k = 0; k < 7; k++) kara64_u16(w[k], ha[k], hb[k]);
+  for (int i = 0; i < 512; i++) full[i] = 0;
+  for (int i = 0; i < 128; i++) {
+    uint32_t wi[7], ci[7];
+    for (int k = 0; k < 7; k++) wi[k] = w[k][i];
+    toom4_interp(ci, wi);
+    for (int k = 0; k < 7; k++) full[64 * k + i] += ci[k];
+  }
+  for (int i = 0; i < 256; i++) r[i] = (uint16_t)(full[i] - full[i + 256]);
+}
+
+/* The multiplication the IND-CPA functions use: schoolbook (the default, for
+ * parity) or Toom-Cook 4-way with Karatsuba (the CPU baseline).  Set before
+ * any batch starts; the batch threads only read it. */
+typedef void (*polmul_fn)(uint16_t *, const uint16_t *, const uint16_t *);
+static polmul_fn g_polmul = orc_polmul_schoolbook;
+
+int orc_set_polmul(int which) {
+  if (which == ORC_POLMUL_SCHOOLBOOK) g_polmul = orc_polmul_schoolbook;
+  else if (which == ORC_POLMUL_TOOM4K) g_polmul = orc_polmul_toom4k;
+  else return -1;
+  return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Raw matrix-vector product (the TMVP benchmark shape).                     */
 /* ------------------------------------------------------------------------ */
@@ -464,7 +571,7 @@ static void matvec_u16(const orc_params *P, uint16_t *acc, const uint16_t *M,
   for (int i = 0; i < l; i++)
     for (int j = 0; j < l; j++) {
       const uint16_t *a = transpose ? M + 256 * (j * l + i) : M + 256 * (i * l + j);
-      orc_polmul_schoolbook(prod, a, v + 256 * j);
+      g_polmul(prod, a, v + 256 * j);
       for (int k = 0; k < 256; k++) acc[256 * i + k] += prod[k];
     }
 }
@@ -474,7 +581,7 @@ static void innerprod_u16(const orc_params *P, uint16_t acc[256], const uint16_t
   uint16_t prod[256];
   memset(acc, 0, sizeof(uint16_t) * 256);
   for (int j = 0; j < P->l; j++) {
-    orc_polmul_schoolbook(prod, b + 256 * j, s + 256 * j);
+    g_polmul(prod, b + 256 * j, s + 256 * j);
     for (int k = 0; k < 256; k++) acc[k] += prod[k];
   }
 }
@@ -664,4 +771,40 @@ void orc_kem_enc_batch(int set, size_t n, uint8_t *ct, uint8_t *ss, const uint8_
 void orc_kem_dec_batch(int set, size_t n, uint8_t *ss, const uint8_t *ct, const uint8_t *sk,
                        uint8_t *fail, int nthreads) {
   kem_batch(2, set, n, ss, NULL, fail, ct, sk, nthreads);
+}
+
+/* Single-instance latency of keypair (op 0), encapsulation (1) or
+ * decapsulation (2) on the calling thread: `iters` calls on a fixed
+ * instance, each timed with CLOCK_MONOTONIC; ns[i] receives call i's time.
+ * Returns 0, or -1 for a bad argument. */
+int orc_kem_latency(int set, int op, int iters, double *ns) {
+  orc_params P;
+  if (orc_get_params(set, &P) != 0 || op < 0 || op > 2 || iters < 1) return -1;
+  uint8_t coins[96], ec[32], ss[32], ss2[32];
+  for (int i = 0; i < 96; i++) coins[i] = (uint8_t)(17 * i + 3);
+  for (int i = 0; i < 32; i++) ec[i] = (uint8_t)(29 * i + 5);
+  uint8_t *pk = (uint8_t *)malloc(P.pk_bytes), *sk = (uint8_t *)malloc(P.sk_bytes),
+          *ct = (uint8_t *)malloc(P.ct_bytes);
+  orc_kem_keypair(set, pk, sk, coins);
+  orc_kem_enc(set, ct, ss, pk, ec);
+  int bad = 0;
+  for (int it = 0; it < iters; it++) {
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    if (op == 0) {
+      coins[0] = (uint8_t)it;
+      orc_kem_keypair(set, pk, sk, coins);
+    } else if (op == 1) {
+      ec[0] = (uint8_t)it;
+      orc_kem_enc(set, ct, ss, pk, ec);
+    } else {
+      bad |= orc_kem_dec(set, ss2, ct, sk) || memcmp(ss, ss2, 32) != 0;
+    }
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    ns[it] = (double)(t1.tv_sec - t0.tv_sec) * 1e9 + (double)(t1.tv_nsec - t0.tv_nsec);
+  }
+  free(pk);
+  free(sk);
+  free(ct);
+  return bad ? -2 : 0;
 }

@@ -70,6 +70,13 @@ void orc_unpack_bits(uint16_t *out, const uint8_t *in, int n, int w);
 void orc_polmul_schoolbook(uint16_t r[256], const uint16_t a[256], const uint16_t b[256]);
 void orc_polmul_tmvp2(uint16_t r[256], const uint16_t a[256], const uint16_t b[256]);
 void orc_polmul_toom4(uint16_t r[256], const uint16_t a[256], const uint16_t b[256]);
+/* toom4k: Toom-Cook 4-way over 16-bit Karatsuba products; right mod 2^13 only. */
+void orc_polmul_toom4k(uint16_t r[256], const uint16_t a[256], const uint16_t b[256]);
+
+/* Multiplication used by the IND-CPA / KEM functions (default schoolbook).
+ * Returns 0, or -1 for an unknown id.  Not thread-safe: set it before a batch. */
+enum { ORC_POLMUL_SCHOOLBOOK = 0, ORC_POLMUL_TOOM4K = 1 };
+int orc_set_polmul(int which);
 
 /* Raw matrix-vector product: out[i] = sum_j A[i][j]*s[j] (transpose=0) or
  * sum_j A[j][i]*s[j] (transpose=1), reduced mod 2^eq.  s is int8 per
@@ -101,6 +108,11 @@ void orc_kem_enc_batch(int set, size_t n, uint8_t *ct, uint8_t *ss,
                        const uint8_t *pk, const uint8_t *coins, int nthreads);
 void orc_kem_dec_batch(int set, size_t n, uint8_t *ss, const uint8_t *ct,
                        const uint8_t *sk, uint8_t *fail, int nthreads);
+
+/* Single-instance latency: `iters` calls of keypair (op 0), encapsulation
+ * (1) or decapsulation (2) on one thread, ns[i] = call i's wall time.
+ * Returns 0; -1 for a bad argument; -2 if a decapsulation did not match. */
+int orc_kem_latency(int set, int op, int iters, double *ns);
 
 #ifdef __cplusplus
 }

@@ -21,3 +21,14 @@ def test_umma_rate_refuses_bad_shapes(kem):
         with pytest.raises(T.TmvpError) as e:
             ctx.umma_rate(kind, n, ctas_per_sm=ctas, iters=16)
         assert e.value.code == T.EINVAL
+
+
+def test_keccak_rate(kem):
+    """The permutation-rate diagnostic runs at full occupancy and refuses a
+    bad permutation count."""
+    T, ctx = kem
+    rate, blocks = ctx.keccak_rate(16)
+    assert blocks >= 1 and 1e8 < rate < 1e11
+    with pytest.raises(T.TmvpError) as e:
+        ctx.keccak_rate(0)
+    assert e.value.code == T.EINVAL

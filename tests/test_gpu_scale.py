@@ -139,6 +139,69 @@ def test_chunked_device_decapsulation(kem, chunk):
     assert not torch.equal(out[n - 5], ss[n - 5])
 
 
+@pytest.mark.parametrize("cap", [1, 3, 8])
+def test_capped_keccak_front_gives_same_keys(kem, cap):
+    """A Keccak front capped at `cap` blocks per SM (threads striding over the
+    GenMatrix and H(c) sponges) gives the same keys, rejection included."""
+    import torch
+    T, ctx = kem
+    dev = torch.device("cuda", 0)
+    n = 20000
+    z = T.sizes(T.SABER)
+    coins = torch.from_numpy(T.splitmix_bytes(61, n * 96).reshape(n, 96)).to(dev)
+    ec = torch.from_numpy(T.splitmix_bytes(62, n * 32).reshape(n, 32)).to(dev)
+    pk = torch.empty((n, z.pk_bytes), dtype=torch.uint8, device=dev)
+    sk = torch.empty((n, z.sk_bytes), dtype=torch.uint8, device=dev)
+    ct = torch.empty((n, z.ct_bytes), dtype=torch.uint8, device=dev)
+    ss = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+    ctx.kem_keypair_ptr(T.SABER, n, pk, sk, coins)
+    ctx.kem_enc_ptr(T.SABER, n, ct, ss, pk, ec)
+    ct[n - 1, 3] ^= 16
+    out = torch.zeros_like(ss)
+    try:
+        ctx.set_front_cap(cap)
+        ctx.kem_dec_ptr(T.SABER, n, out, ct, sk)
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_front_cap(0)
+    assert torch.equal(out[:n - 1], ss[:n - 1]) and not torch.equal(out[n - 1], ss[n - 1])
+
+
+def test_serial_stages_give_same_keys(kem):
+    """The measurement mode that runs every decapsulation stage alone on the
+    caller's stream gives the pipelined pass's keys, rejection included."""
+    import torch
+    T, ctx = kem
+    dev = torch.device("cuda", 0)
+    n = 40000
+    z = T.sizes(T.SABER)
+    coins = torch.from_numpy(T.splitmix_bytes(51, n * 96).reshape(n, 96)).to(dev)
+    ec = torch.from_numpy(T.splitmix_bytes(52, n * 32).reshape(n, 32)).to(dev)
+    pk = torch.empty((n, z.pk_bytes), dtype=torch.uint8, device=dev)
+    sk = torch.empty((n, z.sk_bytes), dtype=torch.uint8, device=dev)
+    ct = torch.empty((n, z.ct_bytes), dtype=torch.uint8, device=dev)
+    ss = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+    ctx.kem_keypair_ptr(T.SABER, n, pk, sk, coins)
+    ctx.kem_enc_ptr(T.SABER, n, ct, ss, pk, ec)
+    ct[7, 9] ^= 2
+    want = torch.empty_like(ss)
+    ctx.kem_dec_ptr(T.SABER, n, want, ct, sk)
+    out = torch.zeros_like(ss)
+    try:
+        ctx.set_serial(True)
+        ctx.set_timing(True)
+        ctx.kem_dec_ptr(T.SABER, n, out, ct, sk)
+        torch.cuda.synchronize()
+        stages = ctx.stage_stats()
+    finally:
+        ctx.set_timing(False)
+        ctx.set_serial(False)
+    assert torch.equal(out, want)
+    assert not torch.equal(out[7], ss[7]) and torch.equal(out[8:], ss[8:])
+    # one unchunked chain: each stage launched once
+    assert all(v[0] == 1 for v in stages.values()) and "dec_front" in stages
+
+
 @pytest.mark.parametrize("chunk,ramp,pinned", [(1024, 4, True), (4096, 2, True), (16384, 0, True),
                                                (16384, 3, True), (0, 0, True), (4096, 2, False)])
 def test_chunked_host_decapsulation(kem, chunk, ramp, pinned):

@@ -1,6 +1,7 @@
 """The request-serving loop: results are the same alone and in a concurrent
 mix of parameter sets and operations, and match the oracle; batches form and
-overlap under load; memory-based admission bounds the slots."""
+overlap under load; memory admission cuts and holds batches to fit the batch
+arena."""
 import threading
 
 import numpy as np
@@ -84,13 +85,21 @@ def test_alone_and_in_the_mix(kem, oracle):
 
 
 def test_memory_admission_and_loadgen(kem):
+    """A batch arena far smaller than the slots could fill: batches are cut to
+    what the largest free block holds and wait for blocks to come back, the
+    arena is never exceeded, and every decapsulation of the load generator
+    gives the encapsulated key."""
     T, ctx = kem
-    # a budget that holds two slots of 256 requests, while four were asked for
-    # (per request: input, output, key, index, the key's expanded A, KEM workspace)
-    one_slot = 256 * (1472 + 1504 + 3040 + 4 + 16 * 416 + 16 * 416 + 768 + 64 + 64 + 1 + 32) + 64 * 256
-    srv = T.Server(max_batch=256, slots=4, mem_budget=2 * one_slot + 1000)
+    probe = T.Server(max_batch=256, slots=4)
     try:
-        assert srv.stats()["slots"] == 2
+        full = probe.stats()["arena_bytes"]  # 4 batches of 256 requests of the largest set
+    finally:
+        probe.close()
+    budget = full // 6  # two thirds of one such batch
+    srv = T.Server(max_batch=256, slots=4, mem_budget=budget)
+    try:
+        st0 = srv.stats()
+        assert st0["slots"] == 4 and budget <= st0["arena_bytes"] < budget + 256
         ids = []
         for s in SETS:
             pk, sk = _keys(T, ctx, s, 16, 300 + s)
@@ -99,9 +108,43 @@ def test_memory_admission_and_loadgen(kem):
                         decaps_fraction=0.5)
         st = srv.stats()
         assert n > 5000 and st["completed"] == n and st["failed"] == 0
+        assert st["checked"] > 1000 and st["mismatched"] == 0
         assert st["p99_us"] >= st["p50_us"] > 0
+        assert 0 < st["peak_arena_bytes"] <= st["arena_bytes"]
     finally:
         srv.close()
+
+
+def test_admission_refuses_then_admits(kem):
+    """With room for a third of one FireSaber batch, a dense burst of requests
+    is admitted piecewise: batches are cut to what fits, further batches wait
+    until memory returns, the arena is never exceeded, and every
+    decapsulation gives the encapsulated key."""
+    T, ctx = kem
+    probe = T.Server(max_batch=512, slots=1)
+    try:
+        one_batch = probe.stats()["arena_bytes"]  # one batch of 512 requests of the largest set
+    finally:
+        probe.close()
+    srv = T.Server(max_batch=512, slots=3, mem_budget=one_batch // 3)
+    try:
+        pk, sk = _keys(T, ctx, 2, 8, 777)  # FireSaber
+        ids = srv.add_keys(2, pk, sk)
+        n = srv.loadgen(rate=1_000_000.0, seconds=0.1, seed=5, key_ids=ids, decaps_fraction=1.0)
+        st = srv.stats()
+        assert st["completed"] == n and st["failed"] == 0
+        assert st["checked"] == n and st["mismatched"] == 0
+        assert st["admission_splits"] >= 1 and st["admission_waits"] >= 1
+        assert 0 < st["peak_arena_bytes"] <= st["arena_bytes"]
+    finally:
+        srv.close()
+
+
+def test_budget_below_one_request_is_refused(kem):
+    T, ctx = kem
+    with pytest.raises(T.TmvpError) as e:
+        T.Server(max_batch=64, slots=2, mem_budget=4096)
+    assert e.value.code == T.ENOMEM
 
 
 def test_one_key_batches(kem, oracle):

@@ -115,6 +115,41 @@ def test_toom4_equals_schoolbook(oracle):
     cases.append((np.full(256, 8191, np.uint16), (-rng.integers(0, 6, 256)).astype(np.uint16)))
     for a, b in cases:
         assert np.array_equal(oracle.polmul(a, b), oracle.polmul(a, b, "toom4"))
+        # 16-bit products (as in the reference's pol_mul): right mod 2^13
+        assert np.array_equal(oracle.polmul(a, b) & 8191, oracle.polmul(a, b, "toom4k") & 8191)
+
+
+@pytest.mark.parametrize("set_id", SETS)
+def test_toom4k_kem_equals_schoolbook_kem(oracle, set_id):
+    """The CPU baseline's multiplication (Toom-Cook 4-way with Karatsuba, the
+    reference's serial pol_mul) gives the schoolbook KEM's bytes: keys,
+    ciphertexts, shared secrets and implicit rejection."""
+    rng = np.random.default_rng(300 + set_id)
+    coins = rng.integers(0, 256, (6, 96), dtype=np.uint8)
+    ec = rng.integers(0, 256, (6, 32), dtype=np.uint8)
+    pk, sk = oracle.kem_keypair_batch(set_id, coins)
+    ct, ss = oracle.kem_enc_batch(set_id, pk, ec)
+    ct[2, 5] ^= 1
+    ss_d, fail = oracle.kem_dec_batch(set_id, ct, sk)
+    try:
+        oracle.set_polmul(oracle.POLMUL_TOOM4K)
+        pk2, sk2 = oracle.kem_keypair_batch(set_id, coins, 2)
+        ct2, ss2 = oracle.kem_enc_batch(set_id, pk2, ec, 2)
+        ct2[2, 5] ^= 1
+        ss_d2, fail2 = oracle.kem_dec_batch(set_id, ct2, sk2, 2)
+    finally:
+        oracle.set_polmul(oracle.POLMUL_SCHOOLBOOK)
+    assert np.array_equal(pk, pk2) and np.array_equal(sk, sk2)
+    assert np.array_equal(ct, ct2) and np.array_equal(ss, ss2)
+    assert np.array_equal(ss_d, ss_d2) and np.array_equal(fail, fail2) and fail.tolist() == [0, 0, 1, 0, 0, 0]
+
+
+def test_single_instance_latency_timer(oracle):
+    """orc_kem_latency times single calls (the batch-1 CPU configuration) and
+    checks each decapsulation against its encapsulation."""
+    for op in ("keypair", "enc", "dec"):
+        ns = oracle.kem_latency_ns(oracle.SABER, op, 5)
+        assert ns.shape == (5,) and (ns > 0).all()
 
 
 @pytest.mark.parametrize("w", [1, 2, 3, 4, 5, 6, 9, 10, 11, 13])

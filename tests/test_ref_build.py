@@ -7,10 +7,10 @@ import pytest
 
 from oracle import pyref
 
-REF = os.environ.get("TMVP_REFERENCE_ROOT", "/root/reference")
+REF = pyref.reference_root()
 
 pytestmark = pytest.mark.skipif(
-    not (pyref.available("saber") or os.path.isdir(REF)),
+    not (pyref.available("saber") or (REF and os.path.isdir(REF))),
     reason="reference sources not present; golden fixtures cover this case")
 
 
