@@ -626,6 +626,31 @@ __global__ void __launch_bounds__(kI5Threads, 2) k_cpa5m(const __grid_constant__
   }
 }
 
+// Mixed launch whose groups all have parameter set SET (the per-set launches
+// of a mixed pass): the group table travels as a kernel parameter (constant
+// bank), so a CTA finds its group and reads its arguments without a global
+// round trip; then the same body as k_cpa5i, with the same registers and
+// occupancy.  CTA gi runs instance gi of the table.
+struct MixParam {
+  int ngroups, total;
+  int first[kMaxGroups + 1];
+  CpaArgs g[kMaxGroups];
+};
+static_assert(sizeof(MixParam) < 32000, "the group table fits the kernel-parameter space");
+
+template <int OP, int SET>
+__global__ void __launch_bounds__(kI5Threads, 2) k_cpa5ms(const __grid_constant__ MixParam T) {
+  extern __shared__ __align__(16) uint8_t sm[];
+  const int gi = blockIdx.x;
+  int lo = 0, hi = T.ngroups - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (gi >= T.first[mid]) lo = mid;
+    else hi = mid - 1;
+  }
+  cpa5i_body<OP, SET>(T.g[lo], (unsigned)(gi - T.first[lo]), sm);
+}
+
 template <int OP>
 inline void layout5_of(int set, int &total, int &cols) {
   switch (set) {
@@ -657,6 +682,31 @@ inline int cap_tmem_residency(F fn, int &smem, int cols) {
   return 0;
 }
 
+template <int OP, int SET>
+inline int launch_cpa5ms(const CpaArgs *groups, int ng, cudaStream_t s) {
+  using LO = LayoutC<OP, SET>;
+  using S = ShapeC<OP, SET>;
+  if (ng < 1 || ng > kMaxGroups) return (int)cudaErrorInvalidValue;
+  MixParam T;
+  T.ngroups = ng;
+  T.first[0] = 0;
+  for (int g = 0; g < ng; g++) {
+    T.g[g] = groups[g];
+    T.first[g + 1] = T.first[g] + groups[g].n;
+  }
+  T.total = T.first[ng];
+  for (int g = ng; g < kMaxGroups; g++) T.first[g + 1] = T.total;
+  if (T.total <= 0) return 0;
+  auto fn = k_cpa5ms<OP, SET>;
+  int smem = LO::TOTAL;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return (int)e;
+  int rc = cap_tmem_residency(fn, smem, S::TMEM_COLS);
+  if (rc) return rc;
+  fn<<<T.total, kI5Threads, smem, s>>>(T);
+  return (int)cudaGetLastError();
+}
+
 template <int OP>
 inline int launch_cpa5m(const CpaArgs *groups, int ng, const MixTable *dev_tab, cudaStream_t s) {
   MixRef R{};
@@ -676,6 +726,18 @@ inline int launch_cpa5m(const CpaArgs *groups, int ng, const MixTable *dev_tab, 
   } else {
     if (!dev_tab) return (int)cudaErrorInvalidValue;
     R.tab = dev_tab;
+  }
+  bool one_set = true;
+  for (int g = 1; g < ng; g++) one_set = one_set && groups[g].P.set == groups[0].P.set;
+  if (one_set) {
+    switch (groups[0].P.set) {
+      case 0: return launch_cpa5ms<OP, 0>(groups, ng, s);
+      case 1: return launch_cpa5ms<OP, 1>(groups, ng, s);
+      case 2: return launch_cpa5ms<OP, 2>(groups, ng, s);
+      case 3: return launch_cpa5ms<OP, 3>(groups, ng, s);
+      case 4: return launch_cpa5ms<OP, 4>(groups, ng, s);
+      case 5: return launch_cpa5ms<OP, 5>(groups, ng, s);
+    }
   }
   auto fn = k_cpa5m<OP>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);

@@ -23,6 +23,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <map>
 #include <mutex>
 #include <string>
 #include <utility>
@@ -72,6 +73,8 @@ struct tmvp_ctx {
   size_t dev_chunk = 32768;                        // chunk of device-input decapsulation (0: none)
   bool serial = false;                             // every stage on the caller's stream, one at a time
   int front_cap = 0;                               // Keccak-front blocks per SM (0: one thread per sponge)
+  // set by the caller (tmvp_ctx_set_*): then the autotuner's per-batch choice does not apply
+  bool host_chunk_set = false, host_ramp_set = false, dev_chunk_set = false, front_cap_set = false;
   int nsm = 0;                                     // SMs of the device
   static constexpr int kLanes = 4;                 // streams for chunk chains
   cudaStream_t lane[kLanes] = {};
@@ -343,6 +346,51 @@ constexpr size_t kHostChunk = 16384;
 // ahead of its chunks (1M Saber instances take 3.6 GiB).
 constexpr size_t kGmFirstBytes = size_t(4) << 30;
 
+// ---- per-batch pass settings picked by the autotuner (process-wide), keyed
+// by (parameter set, batch bucket = ceil(log2 n) clamped to 8..20)
+struct PassChoice {
+  int dev_chunk, front_cap, host_chunk, host_ramp;
+};
+std::mutex g_pass_mu;
+std::map<std::pair<int, int>, PassChoice> g_pass;
+
+int batch_bucket(size_t n) {
+  int b = 0;
+  while (b < 20 && ((size_t)1 << b) < n) b++;
+  return std::max(b, 8);
+}
+
+bool pass_lookup(int set, size_t n, PassChoice *out) {
+  std::lock_guard<std::mutex> lk(g_pass_mu);
+  auto it = g_pass.find({set, batch_bucket(n)});
+  if (it == g_pass.end()) return false;
+  *out = it->second;
+  return true;
+}
+
+// For the duration of one call (the context's lock held): the autotuner's
+// choice for (set, n) replaces every pass setting the caller did not set.
+struct PassScope {
+  tmvp_ctx *c;
+  int dev_chunk, front_cap, host_chunk, host_ramp;
+  PassScope(tmvp_ctx *cc, int set, size_t n)
+      : c(cc), dev_chunk((int)cc->dev_chunk), front_cap(cc->front_cap), host_chunk((int)cc->host_chunk),
+        host_ramp(cc->host_ramp) {
+    PassChoice t;
+    if (!pass_lookup(set, n, &t)) return;
+    if (!c->dev_chunk_set) c->dev_chunk = (size_t)t.dev_chunk;
+    if (!c->front_cap_set) c->front_cap = t.front_cap;
+    if (!c->host_chunk_set) c->host_chunk = (size_t)t.host_chunk;
+    if (!c->host_ramp_set) c->host_ramp = t.host_ramp;
+  }
+  ~PassScope() {
+    c->dev_chunk = (size_t)dev_chunk;
+    c->front_cap = front_cap;
+    c->host_chunk = (size_t)host_chunk;
+    c->host_ramp = host_ramp;
+  }
+};
+
 // Intermediate buffers of one decapsulation pass over n instances.
 struct DecScratch {
   uint8_t *a_stream, *s_stream, *mbuf, *kr, *fail, *hc;
@@ -387,7 +435,7 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   } else {
     StageTimer tm_(c, "dec_front", side);
     const unsigned grid = blocks_for(2 * n, kHashBlock);
-    if (c->front_cap > 0 && grid > (unsigned)(c->nsm * c->front_cap))
+    if (c->front_cap > 0 && !c->serial && grid > (unsigned)(c->nsm * c->front_cap))
       k_dec_front_strided<<<(unsigned)(c->nsm * c->front_cap), kHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc,
                                                                                    (int)n);
     else
@@ -531,6 +579,10 @@ int tmvp_ctx_create(int device, size_t mem_budget, tmvp_ctx **out) {
   cudaDeviceProp prop;
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return set_err(TMVP_EDEVICE);
   if (prop.major < 10) return set_err(TMVP_ENOTSUP);  // built for sm_103a only
+  static std::once_flag tune_cache_once;
+  std::call_once(tune_cache_once, [] {
+    if (const char *path = getenv("TMVP_TUNE_CACHE")) tmvp_tune_load(path);  // absent file: nothing loaded
+  });
   tmvp_ctx *c = new tmvp_ctx();
   c->device = device;
   c->budget = mem_budget;
@@ -608,6 +660,7 @@ int tmvp_ctx_set_host_chunk(tmvp_ctx *c, size_t n) {
   if (!c || (n != 0 && n < 1024)) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(c->mu);
   c->host_chunk = n;
+  c->host_chunk_set = true;
   return set_err(TMVP_OK);
 }
 
@@ -615,6 +668,7 @@ int tmvp_ctx_set_host_ramp(tmvp_ctx *c, int steps) {
   if (!c || steps < 0 || steps > 4) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(c->mu);
   c->host_ramp = steps;
+  c->host_ramp_set = true;
   return set_err(TMVP_OK);
 }
 
@@ -622,6 +676,7 @@ int tmvp_ctx_set_front_cap(tmvp_ctx *c, int blocks_per_sm) {
   if (!c || blocks_per_sm < 0 || blocks_per_sm > 64) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(c->mu);
   c->front_cap = blocks_per_sm;
+  c->front_cap_set = true;
   return set_err(TMVP_OK);
 }
 
@@ -636,6 +691,7 @@ int tmvp_ctx_set_dev_chunk(tmvp_ctx *c, size_t n) {
   if (!c || (n != 0 && n < 1024)) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(c->mu);
   c->dev_chunk = n;
+  c->dev_chunk_set = true;
   return set_err(TMVP_OK);
 }
 
@@ -862,6 +918,7 @@ int tmvp_kem_dec_batch_onekey(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t
   if (!ss || !ct || !sk) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(c->mu);
   Guard g(c);
+  PassScope pass_(c, set, n);
   cudaStream_t s = (cudaStream_t)stream;
   Buf bss = classify(ss, n * 32, c->device), bct = classify(ct, n * P.ct_bytes, c->device),
       bsk = classify(sk, P.sk_bytes, c->device);
@@ -972,6 +1029,7 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
   if (!ss || !ct || !sk) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(c->mu);
   Guard g(c);
+  PassScope pass_(c, set, n);
   cudaStream_t s = (cudaStream_t)stream;
   Buf bss = classify(ss, n * 32, c->device), bct = classify(ct, n * P.ct_bytes, c->device),
       bsk = classify(sk, n * P.sk_bytes, c->device);
@@ -1433,8 +1491,18 @@ size_t mixed_tab_bytes(size_t ng) {
 // memory; tabs: mixed_tab_bytes of device memory for the group tables, which
 // are built into host_tabs and, if upload_tabs, copied on s.  Makes no
 // allocation and no host synchronisation, so it can be captured into a graph.
+// Streams of one mixed chain: its own stream, the side stream of its Keccak
+// front, and the lanes [lane0, lane0 + nlanes) its per-set launches spread over.
+struct MixStreams {
+  cudaStream_t side;
+  int lane0, nlanes;
+};
+
 int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws, uint8_t *tabs,
-                  std::vector<uint8_t> &host_tabs, bool upload_tabs, cudaStream_t s) {
+                  std::vector<uint8_t> &host_tabs, bool upload_tabs, cudaStream_t s,
+                  MixStreams ms = MixStreams{nullptr, 0, tmvp_ctx::kLanes}) {
+  if (!ms.side) ms.side = c->side;
+  if (c->serial) ms.side = s;  // measurement: every stage alone on s
   std::vector<CpaArgs> ga(ng), gb(ng);
   std::vector<HashGroup> hg(ng);
   Arena A{ws};
@@ -1526,10 +1594,13 @@ int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws,
   const HashGroup *th = reinterpret_cast<const HashGroup *>(tabs + 2 * kNumSets * tb);
   const unsigned nb = blocks_for((size_t)total, kHashBlock);
   TRY_CUDA(cudaEventRecord(c->fork_ev, s));
-  TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+  TRY_CUDA(cudaStreamWaitEvent(ms.side, c->fork_ev, 0));
   // GenMatrix and H(c) of every group in one launch (2 total sponges)
-  k_mix_front<<<blocks_for(2 * (size_t)total, kHashBlock), kHashBlock, 0, c->side>>>(th, (int)ng, total, 0);
-  TRY_CUDA(cudaEventRecord(c->join_ev, c->side));
+  {
+    StageTimer tm_(c, "mix_front", ms.side);
+    k_mix_front<<<blocks_for(2 * (size_t)total, kHashBlock), kHashBlock, 0, ms.side>>>(th, (int)ng, total, 0);
+  }
+  TRY_CUDA(cudaEventRecord(c->join_ev, ms.side));
   // the per-set IND-CPA launches of a step run side by side on the context's
   // lanes (forked from s and joined back), so one set's last wave overlaps
   // the next set's launch
@@ -1539,27 +1610,113 @@ int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws,
     int li = 0;
     for (int st = 0; st < kNumSets; st++) {
       if (groups[st].empty()) continue;
-      cudaStream_t ls = c->lane[li % tmvp_ctx::kLanes];
+      const int lane = ms.lane0 + li % ms.nlanes;
+      cudaStream_t ls = c->serial ? s : c->lane[lane];
       TRY_CUDA(cudaStreamWaitEvent(ls, c->fork_ev, 0));
+      static const char *tags[2][kNumSets] = {
+          {"mix_decrypt_0", "mix_decrypt_1", "mix_decrypt_2", "mix_decrypt_3", "mix_decrypt_4", "mix_decrypt_5"},
+          {"mix_reenc_0", "mix_reenc_1", "mix_reenc_2", "mix_reenc_3", "mix_reenc_4", "mix_reenc_5"}};
+      StageTimer tm_(c, tags[op == kReenc ? 1 : 0][st], ls);
       if (cpa_launch_mixed(op, groups[st].data(), (int)groups[st].size(), table(st), ls,
                            persist_ctas_per_sm(op, st)) != 0)
         return TMVP_EDEVICE;
-      TRY_CUDA(cudaEventRecord(c->lane_ev[li % tmvp_ctx::kLanes], ls));
+      TRY_CUDA(cudaEventRecord(c->lane_ev[lane], ls));
       li++;
     }
-    for (int i = 0; i < std::min(li, tmvp_ctx::kLanes); i++) TRY_CUDA(cudaStreamWaitEvent(s, c->lane_ev[i], 0));
+    for (int i = 0; i < std::min(li, ms.nlanes); i++) TRY_CUDA(cudaStreamWaitEvent(s, c->lane_ev[ms.lane0 + i], 0));
     return li;
   };
   int r1 = per_set(kDecrypt, sa, tdec);
   if (r1 < 0) return r1;
   nsets = r1;
-  k_mix_g<<<nb, kHashBlock, 0, s>>>(th, (int)ng, total);
+  {
+    StageTimer tm_(c, "mix_g", s);
+    k_mix_g<<<nb, kHashBlock, 0, s>>>(th, (int)ng, total);
+  }
   TRY_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));  // GenMatrix
   int r2 = per_set(kReenc, sb, tre);
   if (r2 < 0) return r2;
-  k_mix_final<<<nb, kHashBlock, 0, s>>>(th, (int)ng, total);
+  {
+    StageTimer tm_(c, "mix_final", s);
+    k_mix_final<<<nb, kHashBlock, 0, s>>>(th, (int)ng, total);
+  }
   c->launches += 3 + 2 * nsets;
   TRY_CUDA(cudaGetLastError());
+  return TMVP_OK;
+}
+
+// The groups of a mixed pass split into `chains` parts (each group's
+// instances cut in order; groups too small to split stay in part 0).
+std::vector<std::vector<tmvp_dec_group>> mixed_split(size_t ng, const tmvp_dec_group *gr, int chains) {
+  std::vector<std::vector<tmvp_dec_group>> parts(chains);
+  for (size_t g = 0; g < ng; g++) {
+    KemParams P;
+    make_params(gr[g].set, &P);
+    const size_t n = gr[g].n;
+    if (chains == 1 || n < 1024) {
+      parts[0].push_back(gr[g]);
+      continue;
+    }
+    size_t off = 0;
+    for (int k = 0; k < chains; k++) {
+      const size_t m = n * (k + 1) / chains - off;
+      tmvp_dec_group h = gr[g];
+      h.n = m;
+      h.ss = gr[g].ss + off * 32;
+      h.ct = gr[g].ct + off * P.ct_bytes;
+      h.sk = gr[g].sk + off * P.sk_bytes;
+      parts[k].push_back(h);
+      off += m;
+    }
+  }
+  return parts;
+}
+
+// Chains of a mixed pass over `total` instances: two (each on its own stream,
+// side stream and pair of lanes, so one chain's Keccak front overlaps the
+// other's tensor-core steps) once the batch exceeds the device chunk, else one.
+int mixed_chains(const tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr) {
+  size_t total = 0;
+  for (size_t g = 0; g < ng; g++) total += gr[g].n;
+  return (c->dev_chunk && total > c->dev_chunk && !c->serial) ? 2 : 1;
+}
+
+size_t mixed_ws_total(size_t ng, const tmvp_dec_group *gr, int chains) {
+  size_t b = 0;
+  for (auto &part : mixed_split(ng, gr, chains)) b += up(mixed_ws_bytes(part.size(), part.data())) + mixed_tab_bytes(part.size());
+  return b;
+}
+
+// The whole pass on s, as `chains` chains forked from s and joined back.
+int mixed_enqueue_chains(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, int chains, uint8_t *ws,
+                         std::vector<std::vector<uint8_t>> &host_tabs, std::vector<uint8_t *> &tab_ptrs,
+                         bool upload_tabs, cudaStream_t s) {
+  auto parts = mixed_split(ng, gr, chains);
+  host_tabs.assign(parts.size(), {});
+  tab_ptrs.assign(parts.size(), nullptr);
+  if (chains == 1) {
+    tab_ptrs[0] = ws + up(mixed_ws_bytes(ng, gr));
+    return mixed_enqueue(c, ng, gr, ws, tab_ptrs[0], host_tabs[0], upload_tabs, s);
+  }
+  TRY_CUDA(cudaEventRecord(c->gm_ev, s));
+  uint8_t *p = ws;
+  const int nl = tmvp_ctx::kLanes / chains;
+  for (int k = 0; k < chains; k++) {
+    const auto &part = parts[k];
+    uint8_t *wk = p;
+    p += up(mixed_ws_bytes(part.size(), part.data()));
+    tab_ptrs[k] = p;
+    p += mixed_tab_bytes(part.size());
+    cudaStream_t cs = c->lane[k * nl];
+    TRY_CUDA(cudaStreamWaitEvent(cs, c->gm_ev, 0));
+    int r = mixed_enqueue(c, part.size(), part.data(), wk, tab_ptrs[k], host_tabs[k], upload_tabs, cs,
+                          MixStreams{c->lane_side[k], k * nl, nl});
+    if (r) return r;
+  }
+  for (int k = 0; k < chains; k++) {
+    TRY_CUDA(cudaEventRecord(c->lane_ev[k * nl], c->lane[k * nl]));
+    TRY_CUDA(cudaStreamWaitEvent(s, c->lane_ev[k * nl], 0));
+  }
   return TMVP_OK;
 }
 
@@ -1567,8 +1724,9 @@ int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws,
 
 struct tmvp_mixed_plan {
   tmvp_ctx *c = nullptr;
-  uint8_t *ws = nullptr, *tabs = nullptr;
-  std::vector<uint8_t> host_tabs;  // pageable: copied into the graph's memcpy node at capture
+  uint8_t *ws = nullptr;  // workspace and group tables of every chain
+  std::vector<std::vector<uint8_t>> host_tabs;  // per chain, written to tab_ptrs once after capture
+  std::vector<uint8_t *> tab_ptrs;
   cudaStream_t cs = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -1666,10 +1824,12 @@ int tmvp_kem_dec_mixed(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, void *s
   if (r) return set_err(r);
   std::lock_guard<std::mutex> lk(c->mu);
   Guard g(c);
-  if ((r = ensure_ws(c, mixed_ws_bytes(ng, gr) + mixed_tab_bytes(ng)))) return set_err(r);
-  std::vector<uint8_t> host_tabs;
-  uint8_t *tabs = c->ws + mixed_ws_bytes(ng, gr);
-  if ((r = mixed_enqueue(c, ng, gr, c->ws, tabs, host_tabs, true, (cudaStream_t)stream))) return set_err(r);
+  const int chains = mixed_chains(c, ng, gr);
+  if ((r = ensure_ws(c, mixed_ws_total(ng, gr, chains)))) return set_err(r);
+  std::vector<std::vector<uint8_t>> host_tabs;
+  std::vector<uint8_t *> tabs;
+  if ((r = mixed_enqueue_chains(c, ng, gr, chains, c->ws, host_tabs, tabs, true, (cudaStream_t)stream)))
+    return set_err(r);
   return set_err(TMVP_OK);
 }
 
@@ -1687,27 +1847,31 @@ int tmvp_mixed_plan_create(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, tmv
     if (p->graph) cudaGraphDestroy(p->graph);
     if (p->cs) cudaStreamDestroy(p->cs);
     if (p->ws) cudaFree(p->ws);
-    if (p->tabs) cudaFree(p->tabs);
     delete p;
     cudaGetLastError();
     return set_err(code);
   };
   // the plan owns its workspace: the graph keeps these addresses
-  if (cudaMalloc(&p->ws, std::max<size_t>(mixed_ws_bytes(ng, gr), 256)) != cudaSuccess ||
-      cudaMalloc(&p->tabs, mixed_tab_bytes(ng)) != cudaSuccess)
+  const int chains = mixed_chains(c, ng, gr);
+  if (cudaMalloc(&p->ws, std::max<size_t>(mixed_ws_total(ng, gr, chains), 256)) != cudaSuccess)
     return fail(TMVP_ENOMEM);
   if (cudaStreamCreateWithFlags(&p->cs, cudaStreamNonBlocking) != cudaSuccess) return fail(TMVP_EDEVICE);
   // the group tables are fixed for the plan: the capture records no copy of
   // them; they are written once, below, after the capture built them
   if (cudaStreamBeginCapture(p->cs, cudaStreamCaptureModeRelaxed) != cudaSuccess) return fail(TMVP_EDEVICE);
-  r = mixed_enqueue(c, ng, gr, p->ws, p->tabs, p->host_tabs, false, p->cs);
+  const bool timing = c->timing;  // no stage events inside the graph
+  c->timing = false;
+  r = mixed_enqueue_chains(c, ng, gr, chains, p->ws, p->host_tabs, p->tab_ptrs, false, p->cs);
+  c->timing = timing;
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamEndCapture(p->cs, &graph);
   p->graph = graph;
   if (r) return fail(r);
   if (e != cudaSuccess || !graph) return fail(TMVP_EDEVICE);
-  if (cudaMemcpy(p->tabs, p->host_tabs.data(), p->host_tabs.size(), cudaMemcpyHostToDevice) != cudaSuccess)
-    return fail(TMVP_EDEVICE);
+  for (size_t k = 0; k < p->tab_ptrs.size(); k++)
+    if (cudaMemcpy(p->tab_ptrs[k], p->host_tabs[k].data(), p->host_tabs[k].size(), cudaMemcpyHostToDevice) !=
+        cudaSuccess)
+      return fail(TMVP_EDEVICE);
   if (cudaGraphInstantiate(&p->exec, p->graph, 0) != cudaSuccess) return fail(TMVP_EDEVICE);
   *out = p;
   return set_err(TMVP_OK);
@@ -1732,7 +1896,6 @@ void tmvp_mixed_plan_destroy(tmvp_mixed_plan *p) {
     if (p->graph) cudaGraphDestroy(p->graph);
     if (p->cs) cudaStreamDestroy(p->cs);
     if (p->ws) cudaFree(p->ws);
-    if (p->tabs) cudaFree(p->tabs);
   }
   delete p;
 }
@@ -1865,8 +2028,218 @@ extern "C" int tmvp_autotune(tmvp_ctx *c, tmvp_param_set set, size_t n, int *sha
     persist_set_ctas_per_sm(step, set, best);
     if (shapes) shapes[step] = best;
   }
+
+  // the decapsulation pass settings for this batch bucket: device chunk and
+  // Keccak-front cap on device buffers, host chunk and ramp on pinned host
+  // buffers; every candidate must give the same keys
+  PassChoice best{};
+  {
+    PassChoice t0;
+    if (!pass_lookup(set, n, &t0)) t0 = PassChoice{(int)c->dev_chunk, c->front_cap, (int)c->host_chunk, c->host_ramp};
+    best = t0;
+  }
+  const bool keep[4] = {c->dev_chunk_set, c->front_cap_set, c->host_chunk_set, c->host_ramp_set};
+  c->dev_chunk_set = c->front_cap_set = c->host_chunk_set = c->host_ramp_set = false;
+  auto restore_flags = [&] {
+    c->dev_chunk_set = keep[0];
+    c->front_cap_set = keep[1];
+    c->host_chunk_set = keep[2];
+    c->host_ramp_set = keep[3];
+  };
+  auto try_choice = [&](const PassChoice &pc, bool host, uint8_t *hct, uint8_t *hsk, uint8_t *hss, float &ms) -> int {
+    {
+      std::lock_guard<std::mutex> lk(g_pass_mu);
+      g_pass[{set, batch_bucket(n)}] = pc;
+    }
+    std::function<int()> fn;
+    if (host)
+      fn = [&] { return tmvp_kem_dec_batch(c, set, n, hss, hct, hsk, TMVP_FORM_FP8_TCGEN05, st); };
+    else
+      fn = [&] { return tmvp_kem_dec_batch(c, set, n, ss2, ct, sk, TMVP_FORM_FP8_TCGEN05, st); };
+    int rr = timed(fn, ms);
+    if (rr) return rr;
+    if (host) {
+      if (cudaStreamSynchronize(st) != cudaSuccess) return TMVP_EDEVICE;
+      if (memcmp(hss, want.data(), n * 32) != 0) return TMVP_EDEVICE;
+    } else {
+      if (cudaMemcpy(got.data(), ss2, n * 32, cudaMemcpyDeviceToHost) != cudaSuccess) return TMVP_EDEVICE;
+      if (got != want) return TMVP_EDEVICE;
+    }
+    return TMVP_OK;
+  };
+  auto fail = [&](int rr) {
+    std::lock_guard<std::mutex> lk(g_pass_mu);
+    g_pass.erase({set, batch_bucket(n)});
+    return rr;
+  };
+  {
+    float best_ms = 1e30f;
+    const int chunks[] = {0, 16384, 32768};
+    const int caps[] = {0, 8};
+    for (int ch : chunks) {
+      if (ch && (size_t)ch >= n) continue;
+      for (int cap : caps) {
+        PassChoice pc = best;
+        pc.dev_chunk = ch;
+        pc.front_cap = cap;
+        float ms = 0;
+        if ((r = try_choice(pc, false, nullptr, nullptr, nullptr, ms))) {
+          restore_flags();
+          return set_err(fail(r));
+        }
+        if (ms < best_ms) {
+          best_ms = ms;
+          best.dev_chunk = ch;
+          best.front_cap = cap;
+        }
+      }
+    }
+  }
+  {
+    uint8_t *hct = nullptr, *hsk = nullptr, *hss = nullptr;
+    if (cudaMallocHost(&hct, n * P.ct_bytes) != cudaSuccess || cudaMallocHost(&hsk, n * P.sk_bytes) != cudaSuccess ||
+        cudaMallocHost(&hss, n * 32) != cudaSuccess) {
+      cudaGetLastError();
+      if (hct) cudaFreeHost(hct);
+      if (hsk) cudaFreeHost(hsk);
+      restore_flags();
+      return set_err(fail(TMVP_ENOMEM));
+    }
+    struct HostGuard {
+      uint8_t *a, *b, *c;
+      ~HostGuard() {
+        cudaFreeHost(a);
+        cudaFreeHost(b);
+        cudaFreeHost(c);
+      }
+    } hg{hct, hsk, hss};
+    if (cudaMemcpy(hct, ct, n * P.ct_bytes, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(hsk, sk, n * P.sk_bytes, cudaMemcpyDeviceToHost) != cudaSuccess) {
+      restore_flags();
+      return set_err(fail(TMVP_EDEVICE));
+    }
+    float best_ms = 1e30f;
+    const int hc[][2] = {{0, 0}, {8192, 1}, {16384, 0}, {16384, 1}, {16384, 2}, {32768, 2}};
+    PassChoice base = best;
+    for (auto &h : hc) {
+      if (h[0] && (size_t)h[0] >= n) continue;
+      PassChoice pc = base;
+      pc.host_chunk = h[0];
+      pc.host_ramp = h[1];
+      float ms = 0;
+      if ((r = try_choice(pc, true, hct, hsk, hss, ms))) {
+        restore_flags();
+        return set_err(fail(r));
+      }
+      if (ms < best_ms) {
+        best_ms = ms;
+        best.host_chunk = h[0];
+        best.host_ramp = h[1];
+      }
+    }
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_pass_mu);
+    g_pass[{set, batch_bucket(n)}] = best;
+  }
+  restore_flags();
+  if (const char *path = getenv("TMVP_TUNE_CACHE")) tmvp_tune_save(path);
   return set_err(TMVP_OK);
 }
+
+extern "C" {
+
+int tmvp_tune_pass_set(tmvp_param_set set, size_t n, const int *choice) {
+  KemParams P;
+  if (!make_params(set, &P) || !choice || n == 0) return set_err(TMVP_EINVAL);
+  if (choice[0] < 0 || (choice[0] && choice[0] < 1024) || choice[1] < 0 || choice[1] > 64 || choice[2] < 0 ||
+      (choice[2] && choice[2] < 1024) || choice[3] < 0 || choice[3] > 4)
+    return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(g_pass_mu);
+  g_pass[{(int)set, batch_bucket(n)}] = PassChoice{choice[0], choice[1], choice[2], choice[3]};
+  return set_err(TMVP_OK);
+}
+
+int tmvp_tune_pass_get(tmvp_param_set set, size_t n, int *choice) {
+  KemParams P;
+  if (!make_params(set, &P) || !choice || n == 0) return set_err(TMVP_EINVAL);
+  PassChoice t;
+  if (!pass_lookup(set, n, &t)) return 0;
+  choice[0] = t.dev_chunk;
+  choice[1] = t.front_cap;
+  choice[2] = t.host_chunk;
+  choice[3] = t.host_ramp;
+  return 1;
+}
+
+void tmvp_tune_clear(void) {
+  {
+    std::lock_guard<std::mutex> lk(g_pass_mu);
+    g_pass.clear();
+  }
+  for (int step = 0; step < 5; step++)
+    for (int set = 0; set < 6; set++) persist_set_ctas_per_sm(step, set, -1);
+}
+
+// Cache file: one choice per line, "shape <step> <set> <shape>" and
+// "pass <set> <bucket> <dev_chunk> <front_cap> <host_chunk> <host_ramp>".
+int tmvp_tune_save(const char *path) {
+  if (!path) return set_err(TMVP_EINVAL);
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE *f = fopen(tmp.c_str(), "w");
+  if (!f) return set_err(TMVP_EINVAL);
+  fprintf(f, "# tmvp autotuner choices\n");
+  for (int step = 0; step < 5; step++)
+    for (int set = 0; set < 6; set++) {
+      const int sh = persist_ctas_per_sm(step, set);
+      if (sh >= 0) fprintf(f, "shape %d %d %d\n", step, set, sh);
+    }
+  {
+    std::lock_guard<std::mutex> lk(g_pass_mu);
+    for (auto &kv : g_pass)
+      fprintf(f, "pass %d %d %d %d %d %d\n", kv.first.first, kv.first.second, kv.second.dev_chunk,
+              kv.second.front_cap, kv.second.host_chunk, kv.second.host_ramp);
+  }
+  const bool ok = fclose(f) == 0;
+  if (!ok || rename(tmp.c_str(), path) != 0) {
+    remove(tmp.c_str());
+    return set_err(TMVP_EINVAL);
+  }
+  return set_err(TMVP_OK);
+}
+
+int tmvp_tune_load(const char *path) {
+  if (!path) return set_err(TMVP_EINVAL);
+  FILE *f = fopen(path, "r");
+  if (!f) return set_err(TMVP_EINVAL);
+  char line[256];
+  int bad = 0;
+  while (fgets(line, sizeof line, f)) {
+    if (line[0] == '#' || line[0] == '\n') continue;
+    int a[6];
+    if (sscanf(line, "shape %d %d %d", &a[0], &a[1], &a[2]) == 3) {
+      if (a[0] < 0 || a[0] > 4 || a[1] < 0 || a[1] > 5 || a[2] < -1 || a[2] > 2) {
+        bad = 1;
+        continue;
+      }
+      persist_set_ctas_per_sm(a[0], a[1], a[2]);
+    } else if (sscanf(line, "pass %d %d %d %d %d %d", &a[0], &a[1], &a[2], &a[3], &a[4], &a[5]) == 6) {
+      if (a[0] < 0 || a[0] > 5 || a[1] < 8 || a[1] > 20 || a[2] < 0 || (a[2] && a[2] < 1024) || a[3] < 0 ||
+          a[3] > 64 || a[4] < 0 || (a[4] && a[4] < 1024) || a[5] < 0 || a[5] > 4) {
+        bad = 1;
+        continue;
+      }
+      std::lock_guard<std::mutex> lk(g_pass_mu);
+      g_pass[{a[0], a[1]}] = PassChoice{a[2], a[3], a[4], a[5]};
+    } else {
+      bad = 1;
+    }
+  }
+  fclose(f);
+  return set_err(bad ? TMVP_EINVAL : TMVP_OK);
+}
+
+}  // extern "C"
 
 namespace tmvp {
 

@@ -140,6 +140,12 @@ def lib(build_if_missing: bool = False):
     L.tmvp_tune_set.argtypes = [I, I, I]
     L.tmvp_tune_get.argtypes = [I, I]
     L.tmvp_autotune.argtypes = [P, I, S, ctypes.POINTER(ctypes.c_int)]
+    L.tmvp_tune_pass_set.argtypes = [I, S, ctypes.POINTER(ctypes.c_int)]
+    L.tmvp_tune_pass_get.argtypes = [I, S, ctypes.POINTER(ctypes.c_int)]
+    L.tmvp_tune_clear.argtypes = []
+    L.tmvp_tune_clear.restype = None
+    L.tmvp_tune_save.argtypes = [ctypes.c_char_p]
+    L.tmvp_tune_load.argtypes = [ctypes.c_char_p]
     L.tmvp_ctx_sync_status.argtypes = [P, P]
     L.tmvp_kem_dec_mixed.argtypes = [P, S, ctypes.POINTER(DecGroup), P]
     L.tmvp_mixed_plan_create.argtypes = [P, S, ctypes.POINTER(DecGroup), ctypes.POINTER(P)]
@@ -169,6 +175,35 @@ def tune_set(step: int, set_id: int, shape: int):
 
 def tune_get(step: int, set_id: int) -> int:
     return lib().tmvp_tune_get(step, set_id)
+
+
+PASS_FIELDS = ("dev_chunk", "front_cap", "host_chunk", "host_ramp")
+
+
+def tune_pass_set(set_id: int, n: int, dev_chunk: int, front_cap: int, host_chunk: int, host_ramp: int):
+    arr = (ctypes.c_int * 4)(dev_chunk, front_cap, host_chunk, host_ramp)
+    _check(lib().tmvp_tune_pass_set(set_id, n, arr), "tmvp_tune_pass_set")
+
+
+def tune_pass_get(set_id: int, n: int):
+    """The autotuner's pass settings for (set, n's batch bucket), or None."""
+    arr = (ctypes.c_int * 4)()
+    rc = lib().tmvp_tune_pass_get(set_id, n, arr)
+    if rc < 0:
+        raise TmvpError(rc, "tmvp_tune_pass_get")
+    return dict(zip(PASS_FIELDS, list(arr))) if rc == 1 else None
+
+
+def tune_clear():
+    lib().tmvp_tune_clear()
+
+
+def tune_save(path: str):
+    _check(lib().tmvp_tune_save(path.encode()), "tmvp_tune_save")
+
+
+def tune_load(path: str):
+    _check(lib().tmvp_tune_load(path.encode()), "tmvp_tune_load")
 
 
 def _groups(groups):

@@ -209,7 +209,8 @@ int tmvp_ctx_set_host_ramp(tmvp_ctx *ctx, int steps);
  * be 0 or >= 1024.  Results do not depend on it. */
 int tmvp_ctx_set_dev_chunk(tmvp_ctx *ctx, size_t n);
 /* on != 0: decapsulation runs every stage on the caller's stream, one after
- * the other and unchunked (no side stream, no lanes), so that the per-stage
+ * the other, unchunked and with the Keccak front uncapped (no side stream, no
+ * lanes), so that the per-stage
  * timing (tmvp_ctx_set_timing) measures each kernel alone on the GPU.  Slower;
  * for measurement.  Results do not depend on it.  Default 0. */
 int tmvp_ctx_set_serial(tmvp_ctx *ctx, int on);
@@ -301,7 +302,17 @@ int tmvp_server_loadgen(tmvp_server *srv, double rate, double seconds, uint64_t 
  * tmvp_autotune times every shape of every step for `set` on n synthetic
  * instances (key pairs and ciphertexts made with this library; every shape
  * must decapsulate to the same keys), keeps the fastest and, if `shapes` is
- * not NULL, writes them to shapes[5] (indexed by step).
+ * not NULL, writes them to shapes[5] (indexed by step).  It then picks the
+ * decapsulation pass settings for n's batch bucket (ceil(log2 n), 256 ..
+ * 2^20): the device chunk (tmvp_ctx_set_dev_chunk) and Keccak-front cap
+ * (tmvp_ctx_set_front_cap) on device buffers, the host chunk and ramp
+ * (tmvp_ctx_set_host_chunk / _ramp) on pinned host buffers, each the fastest
+ * of its candidates that gives the same keys.  Decapsulations of that set and
+ * bucket then use them, in every context, for each setting the context's
+ * caller did not set explicitly.  n is clamped to 1024 .. 65536.  Run it with
+ * no other call in flight on `ctx`.  If $TMVP_TUNE_CACHE names a file, the
+ * choices are saved there after tuning and loaded from it when the first
+ * context of the process is created.
  * ------------------------------------------------------------------------- */
 enum {
   TMVP_STEP_DECRYPT = 0,
@@ -313,6 +324,18 @@ enum {
 int tmvp_tune_set(int step, tmvp_param_set set, int shape);
 int tmvp_tune_get(int step, tmvp_param_set set);
 int tmvp_autotune(tmvp_ctx *ctx, tmvp_param_set set, size_t n, int *shapes);
+/* The pass settings of (set, n's batch bucket): choice[4] = device chunk,
+ * Keccak-front cap, host chunk, host ramp (the ranges of the tmvp_ctx_set_*
+ * calls).  _get returns 1 and fills choice if the bucket has a choice, 0 if
+ * not, TMVP_EINVAL on a bad argument. */
+int tmvp_tune_pass_set(tmvp_param_set set, size_t n, const int *choice);
+int tmvp_tune_pass_get(tmvp_param_set set, size_t n, int *choice);
+/* Forget every choice (launch shapes back to one CTA per instance). */
+void tmvp_tune_clear(void);
+/* Write / read the choices as a text file (TMVP_EINVAL if it cannot be
+ * written or read, or holds a malformed line; good lines are still loaded). */
+int tmvp_tune_save(const char *path);
+int tmvp_tune_load(const char *path);
 
 /* Waits for `stream`, then reads and clears the context's device status:
  * TMVP_EINVAL if a secret was outside the tensor-core range, TMVP_ETIMEOUT if

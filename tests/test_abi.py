@@ -67,3 +67,39 @@ def test_genmatrix_bytes(T, oracle):
         assert T.genmatrix_bytes(s) == p.l * p.l * p.eq * 32
     assert T.genmatrix_bytes(T.SABER) == 3744
     assert T.lib().tmvp_genmatrix_bytes(17) == 0
+
+
+def test_tune_table_and_cache_file(T, tmp_path):
+    """The autotuner's per-batch-bucket pass settings and launch shapes round
+    trip through the cache file; buckets are ceil(log2 n); malformed lines and
+    out-of-range values are refused (no GPU needed)."""
+    T.tune_clear()
+    try:
+        assert T.tune_pass_get(T.SABER, 65536) is None
+        T.tune_pass_set(T.SABER, 65536, 16384, 8, 8192, 2)
+        T.tune_pass_set(T.SABLE, 3000, 0, 0, 0, 0)
+        assert T.tune_pass_get(T.SABER, 40000) == {"dev_chunk": 16384, "front_cap": 8, "host_chunk": 8192,
+                                                    "host_ramp": 2}          # same bucket (2^16)
+        assert T.tune_pass_get(T.SABER, 32768) is None                       # bucket 2^15
+        assert T.tune_pass_get(T.SABLE, 4096)["dev_chunk"] == 0              # 3000 and 4096: bucket 2^12
+        assert T.lib().tmvp_tune_set(T.TMVP_STEP_REENC if hasattr(T, "TMVP_STEP_REENC") else 2, T.SABER, 1) == T.OK
+        for bad in ((100, 0, 0, 0), (0, 65, 0, 0), (0, 0, 512, 0), (0, 0, 0, 5), (-1, 0, 0, 0)):
+            with pytest.raises(T.TmvpError):
+                T.tune_pass_set(T.SABER, 1024, *bad)
+        path = str(tmp_path / "tune.txt")
+        T.tune_save(path)
+        T.tune_clear()
+        assert T.tune_pass_get(T.SABER, 65536) is None and T.tune_get(2, T.SABER) == -1
+        T.tune_load(path)
+        assert T.tune_pass_get(T.SABER, 65536)["front_cap"] == 8
+        assert T.tune_pass_get(T.SABLE, 4000)["host_chunk"] == 0
+        assert T.tune_get(2, T.SABER) == 1
+        with open(path, "a") as f:
+            f.write("pass 1 16 100 0 0 0\nnonsense\n")
+        with pytest.raises(T.TmvpError):
+            T.tune_load(path)  # the good lines still load
+        assert T.tune_pass_get(T.SABER, 65536)["dev_chunk"] == 16384
+        with pytest.raises(T.TmvpError):
+            T.tune_load(str(tmp_path / "missing.txt"))
+    finally:
+        T.tune_clear()

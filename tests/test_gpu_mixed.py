@@ -106,15 +106,27 @@ def test_every_launch_shape_is_exact(kem, oracle, set_id):
 
 
 def test_autotune_choice_is_exact(kem):
+    """The autotuner's launch shapes and its pass settings for the batch
+    bucket (device chunk, Keccak-front cap, host chunk and ramp) are among
+    the candidates, and decapsulation under them stays exact, from device and
+    from host buffers."""
     T, ctx = kem
     try:
         shapes = ctx.autotune(1, 4096)
         assert len(shapes) == 5 and all(s in (-1, 0, 1, 2) for s in shapes)
         assert [T.tune_get(step, 1) for step in range(5)] == shapes
-        coins = T.splitmix_bytes(99, 300 * 96).reshape(300, 96)
+        pc = T.tune_pass_get(1, 4096)
+        assert pc is not None and pc["dev_chunk"] == 0 and pc["front_cap"] in (0, 8)
+        assert (pc["host_chunk"], pc["host_ramp"]) in ((0, 0), (0, 1), (0, 2))  # chunks >= n are skipped
+        assert T.tune_pass_get(1, 2500) == pc and T.tune_pass_get(1, 8192) is None
+        n = 3000
+        coins = T.splitmix_bytes(99, n * 96).reshape(n, 96)
         pk, sk = ctx.kem_keypair(1, coins)
-        ct, ss = ctx.kem_enc(1, pk, T.splitmix_bytes(98, 300 * 32).reshape(300, 32))
+        ct, ss = ctx.kem_enc(1, pk, T.splitmix_bytes(98, n * 32).reshape(n, 32))
         assert np.array_equal(ctx.kem_dec(1, ct, sk), ss)
+        # a bucket with chunking: every candidate was checked against the keys
+        shapes = ctx.autotune(1, 40000)
+        pc = T.tune_pass_get(1, 40000)
+        assert pc["dev_chunk"] in (0, 16384, 32768) and pc["host_chunk"] in (0, 8192, 16384, 32768)
     finally:
-        for step in range(5):
-            T.tune_set(step, 1, -1)
+        T.tune_clear()
