@@ -192,6 +192,49 @@ __device__ __forceinline__ uint2 raw_digits8(const uint32_t (&X)[4], int d) {
   return make_uint2(a, b);
 }
 
+// Digit columns of 32 coefficients of one W-bit packed polynomial: lane m
+// (0..7) of an 8-lane group takes coefficients 32m .. 32m + 31, exactly W
+// aligned words of the stream at src, so that four groups (a warp) reading
+// four polynomials load conflict-free, one 32-bit word per lane per load.
+// Coefficient groups 4m .. 4m + 3 of 8 (K rows 8 kq .. 8 kq + 7, kq = 31 - g,
+// K reversed) fill the two 16-byte K chunks a = 15 - 2m and 14 - 2m of each
+// digit column, one 128-bit store each.  colbase: the digit columns of this
+// j (LO::BM + j * LO::BJ as a shared-window address); cb: first column.
+template <int W, class LO>
+__device__ __forceinline__ void stage_digits32(const uint8_t *sm, int src, uint32_t colbase, int cb, int m) {
+  const uint32_t wp = smem_u32(sm) + (uint32_t)(src + 4 * W * m);
+  uint32_t w[W];
+#pragma unroll
+  for (int i = 0; i < W; i++) w[i] = lds32(wp + 4 * i);
+  constexpr uint32_t mask = (1u << W) - 1u;
+  uint32_t X[16];  // coefficients 2k, 2k + 1 as the low / high 16-bit lanes of X[k]
+#pragma unroll
+  for (int k = 0; k < 16; k++) {
+    uint32_t v[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int bit = W * (2 * k + h), i = bit >> 5, sh = bit & 31;
+      v[h] = ((sh + W <= 32) ? (w[i] >> sh) : __funnelshift_r(w[i], w[i + 1], sh)) & mask;
+    }
+    X[k] = __byte_perm(v[0], v[1], 0x5410);
+  }
+  const int a1 = 14 - 2 * m;  // and a0 = a1 + 1, LB bytes after it
+  const uint32_t c1 = colbase + (uint32_t)LO::chunk_off(a1);
+#pragma unroll
+  for (int d = 0; d < r16_digits(W); d++) {
+    uint2 v[4];
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      const uint32_t Xt[4] = {X[4 * t], X[4 * t + 1], X[4 * t + 2], X[4 * t + 3]};
+      v[t] = raw_digits8<W>(Xt, d);
+    }
+    const int n = cb + d;
+    const uint32_t col = c1 + (uint32_t)((n >> 3) * 128 + (n & 7) * 16);
+    sts128(col + LO::LB, v[1].x, v[1].y, v[0].x, v[0].y);  // chunk a0: kq 30 - 4m, then 31 - 4m
+    sts128(col, v[3].x, v[3].y, v[2].x, v[2].y);           // chunk a1: kq 28 - 4m, then 29 - 4m
+  }
+}
+
 // One instance (CTA of kI5Threads threads; sm: its dynamic shared memory).
 template <int OP, int SET>
 __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst, uint8_t *sm) {
@@ -376,17 +419,28 @@ __device__ __forceinline__ void cpa5i_body(const CpaArgs &a, const unsigned inst
       }
     } else if constexpr (S::R == 1) {
       if (warp < L) item(std::integral_constant<int, S::WB>{}, LO::CTO + 32 * warp * S::WB, 0, warp);
-    } else if (warp < S::RA) {
-      const int p = warp;
-#pragma unroll
-      for (int j = 0; j < L; j++) {
-        const int ij = (OP == kKeygen) ? (j * L + p) : (p * L + j);
-        item(std::integral_constant<int, S::WA>{}, LO::A + 32 * ij * S::WA, p * S::DA, j);
+    } else {
+      // public matrix A (RA x L polynomials), then b (encryption, re-encryption):
+      // four polynomials per warp, eight lanes each
+      constexpr int NA = S::RA * L, NB = (S::R - S::RA) * L;
+      constexpr int WA_WARPS = (NA + 3) / 4, WB_WARPS = (NB + 3) / 4;
+      static_assert(WA_WARPS + WB_WARPS <= 8, "digit polynomials fit the CTA's warps");
+      const uint32_t bm32 = smem_u32(Bm);
+      if (warp < WA_WARPS) {
+        const int t = 4 * warp + (lane >> 3);
+        if (t < NA) {
+          const int p = t / L, j = t % L;
+          const int ij = (OP == kKeygen) ? (j * L + p) : (p * L + j);
+          stage_digits32<S::WA, LO>(sm, LO::A + 32 * ij * S::WA, bm32 + (uint32_t)(j * LO::BJ), p * S::DA, lane & 7);
+        }
+      } else if (warp < WA_WARPS + WB_WARPS) {
+        const int t = 4 * (warp - WA_WARPS) + (lane >> 3);
+        if (t < NB) {
+          const int pb = t / L, j = t % L;
+          stage_digits32<S::WB, LO>(sm, LO::B + 32 * j * S::WB, bm32 + (uint32_t)(j * LO::BJ),
+                                    S::RA * S::DA + pb * S::DB, lane & 7);
+        }
       }
-    } else if (warp < S::R) {
-#pragma unroll
-      for (int j = 0; j < L; j++)
-        item(std::integral_constant<int, S::WB>{}, LO::B + 32 * j * S::WB, S::RA * S::DA + (warp - S::RA) * S::DB, j);
     }
   }
   __syncthreads();  // s_ext complete, and the streams inside H read, before H is written

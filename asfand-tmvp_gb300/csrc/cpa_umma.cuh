@@ -232,6 +232,9 @@ __device__ __forceinline__ uint32_t lds32(uint32_t a) {
   asm volatile("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(a));
   return v;
 }
+__device__ __forceinline__ void lds128(uint32_t a, uint32_t &x, uint32_t &y, uint32_t &z, uint32_t &w) {
+  asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];" : "=r"(x), "=r"(y), "=r"(z), "=r"(w) : "r"(a));
+}
 __device__ __forceinline__ void sts64(uint32_t a, uint32_t x, uint32_t y) {
   asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(a), "r"(x), "r"(y) : "memory");
 }
@@ -241,20 +244,31 @@ __device__ __forceinline__ void sts128(uint32_t a, uint32_t x, uint32_t y, uint3
 
 // stage_hankel with compile-time sizes and 32-bit shared addresses (H, ext:
 // shared-window byte addresses): the same thread groups, each thread's rows
-// unrolled from one load of the ext words they span.
+// unrolled from one load of the ext words they span.  A thread's window
+// starts at word q = 2 u0 + par with u0 even, so it loads the 16-byte-aligned
+// words from q - par with 128-bit loads (the eight lanes of a row pair share
+// them, so a warp's load is one 64-byte wavefront) and takes word i + par by
+// a funnel shift.
 template <int L, int NT, int CORES>
 __device__ __forceinline__ void stage_hankel_ct(uint32_t H, uint32_t ext, int tid) {
   constexpr int PAIRS = NT >> 3;
   constexpr int RUN = (CORES + PAIRS - 1) / PAIRS;  // rows per thread and polynomial
+  constexpr int NW = (2 * RUN + 4 + 3) & ~3;         // the 2 RUN + 3 window words, plus one for par
+  static_assert(RUN % 2 == 0, "every thread's window starts on a 16-byte boundary");
+  static_assert(2 * (CORES - 1) + NW <= 128, "the loads stay inside one polynomial's 512-byte s_ext");
   const int sh = tid & 3, par = (tid >> 2) & 1, u0 = (tid >> 3) * RUN;
   if (u0 >= CORES) return;
   const uint32_t sel = 0x3210u + 0x1111u * (uint32_t)sh;
-  const int q = 2 * u0 + par;
+  const int b = 2 * u0;  // q - par, a multiple of 4
+  const int q = b + par;
 #pragma unroll
   for (int j = 0; j < L; j++) {
+    uint32_t a[NW];
+#pragma unroll
+    for (int i = 0; i < NW; i += 4) lds128(ext + 512 * j + 4 * (b + i), a[i], a[i + 1], a[i + 2], a[i + 3]);
     uint32_t w[2 * RUN + 3];
 #pragma unroll
-    for (int i = 0; i < 2 * RUN + 3; i++) w[i] = lds32(ext + 512 * j + 4 * (q + i));
+    for (int i = 0; i < 2 * RUN + 3; i++) w[i] = __funnelshift_rc(a[i], a[i + 1], 32u * (uint32_t)par);
     const uint32_t h = H + (uint32_t)(j * CORES * 128) + 16 * (4 * q + sh);
 #pragma unroll
     for (int r = 0; r < RUN; r++)
