@@ -54,19 +54,34 @@ __device__ __forceinline__ uint64_t rotl64(uint64_t v, int n) {
 // the constant is indexed by the round counter).
 __constant__ KeccakTables kKeccak = make_keccak_tables();
 
+// a ^ b ^ c on both 32-bit halves, one three-input LOP3 each.  Theta applies
+// C[x-1] ^ rot(C[x+1], 1) to a lane this way instead of first forming that
+// term per column and then XORing it into five lanes (one XOR per column
+// half fewer per round).
+__device__ __forceinline__ uint64_t xor3_64(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t d;
+  asm("{\n\t.reg .b32 al, ah, bl, bh, cl, ch, dl, dh;\n\t"
+      "mov.b64 {al, ah}, %1;\n\tmov.b64 {bl, bh}, %2;\n\tmov.b64 {cl, ch}, %3;\n\t"
+      "lop3.b32 dl, al, bl, cl, 0x96;\n\tlop3.b32 dh, ah, bh, ch, 0x96;\n\t"
+      "mov.b64 %0, {dl, dh};\n\t}"
+      : "=l"(d)
+      : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
 // One round over a register-resident state (theta, rho+pi, chi, iota).
 __device__ __forceinline__ void keccak_round(uint64_t (&A)[25], uint64_t rc) {
   constexpr KeccakTables T = make_keccak_tables();
-  uint64_t C[5], D[5], B[25];
+  uint64_t C[5], E[5], B[25];
 #pragma unroll
   for (int x = 0; x < 5; x++) C[x] = A[x] ^ A[x + 5] ^ A[x + 10] ^ A[x + 15] ^ A[x + 20];
 #pragma unroll
-  for (int x = 0; x < 5; x++) D[x] = C[(x + 4) % 5] ^ rotl64(C[(x + 1) % 5], 1);
+  for (int x = 0; x < 5; x++) E[x] = rotl64(C[(x + 1) % 5], 1);
 #pragma unroll
   for (int x = 0; x < 5; x++)
 #pragma unroll
     for (int y = 0; y < 5; y++)
-      B[y + 5 * ((2 * x + 3 * y) % 5)] = rotl64(A[x + 5 * y] ^ D[x], T.rho[x + 5 * y]);
+      B[y + 5 * ((2 * x + 3 * y) % 5)] = rotl64(xor3_64(A[x + 5 * y], C[(x + 4) % 5], E[x]), T.rho[x + 5 * y]);
 #pragma unroll
   for (int y = 0; y < 5; y++)
 #pragma unroll

@@ -383,7 +383,7 @@ def run_ours(args):
     if args.no_e2e:
         e2e_ms, e2e_exact, e2e_value, e2e_chunk = [float("nan")], True, None, (None, {}, False)
     else:
-        e2e_ms, e2e_exact, e2e_value, e2e_chunk = _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws)
+        e2e_ms, e2e_exact, e2e_value, e2e_chunk = _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws, local)
     # ---- the same decapsulations with each key's A expanded once beforehand (the
     # serving loop's device-resident keys): GenMatrix leaves the per-call work
     cached = None
@@ -513,7 +513,7 @@ def run_ours(args):
     return 0
 
 
-def _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws):
+def _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws, device):
     """Host-buffer decapsulation through the C ABI with the library's own
     host chunk / ramp (the autotuner's choice for this batch, else the
     built-in default): the reported figure.  Then, on a second context, the
@@ -542,7 +542,7 @@ def _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws):
     e2e_ms, e2e_exact = run(ctx, ke)
     sweep = {}
     if not args.no_sweep:
-        c2 = T.Context(ctx_device(ctx))
+        c2 = T.Context(device)
         try:
             for chunk, ramp in ((8192, 0), (8192, 1), (16384, 0), (16384, 1), (16384, 2), (16384, 3),
                                 (32768, 2), (32768, 3), (32768, 4), (0, 0)):
@@ -555,11 +555,6 @@ def _e2e(ctx, T, n, ct, sk, ss_ref, sp, stream, args, ws):
             c2.close()
     setting = f"{used[0]}/{used[1]}"
     return e2e_ms, e2e_exact, ws * n / (statistics.mean(e2e_ms) / 1e3), (setting, sweep, bool(tuned))
-
-
-def ctx_device(ctx):
-    import torch
-    return torch.cuda.current_device()
 
 
 def _gpu_latency(ctx, T, dev, sp, args):
