@@ -36,22 +36,23 @@ __device__ __forceinline__ void run_shake_job(const ShakeJob &J, size_t i) {
 }
 
 __global__ void __launch_bounds__(128) k_shake_jobs(ShakeJob j0, ShakeJob j1, int n) {
-  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nal = warp_round((size_t)n);
   if (t < (size_t)n) {
     run_shake_job(j0, t);
-  } else if (j1.out && t < 2 * (size_t)n) {
-    run_shake_job(j1, t - n);
+  } else if (j1.out && t >= nal && t < nal + n) {
+    run_shake_job(j1, t - nal);
   }
 }
 
 // Encapsulation front (saber_enc, cuda_kernel.cu:116-127): thread i < n runs
 // m = H(coins), H(pk), kr = G(m || H(pk)) and the GenSecret stream
-// SHAKE-128(kr[32:64]); threads n..2n-1 expand GenMatrix from pk's seed.
+// SHAKE-128(kr[32:64]); threads warp_round(n) + i expand GenMatrix from pk's
+// seed.
 __global__ void __launch_bounds__(128) k_enc_front(KemParams P, const uint8_t *pk,
                                                     const uint8_t *coins, uint8_t *mbuf,
                                                     uint8_t *kr, uint8_t *s_stream,
                                                     uint8_t *a_stream, int n) {
-  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nal = warp_round((size_t)n);
   if (t < (size_t)n) {
     uint64_t c[4], buf[8], g[8];
     load_words(c, coins + t * 32, 4);
@@ -67,8 +68,8 @@ __global__ void __launch_bounds__(128) k_enc_front(KemParams P, const uint8_t *p
     }
     uint64_t seed[4] = {g[4], g[5], g[6], g[7]};
     shake128_32(reinterpret_cast<uint64_t *>(s_stream + t * P.gs_bytes), P.gs_bytes, seed);
-  } else if (t < 2 * (size_t)n) {
-    size_t i = t - n;
+  } else if (t >= nal && t < nal + n) {
+    const size_t i = t - nal;
     uint64_t seed[4];
     load_words(seed, pk + i * P.pk_bytes + (size_t)P.l * P.polycompbytes, 4);
     shake128_32(reinterpret_cast<uint64_t *>(a_stream + i * P.gm_bytes), P.gm_bytes, seed);
@@ -127,31 +128,38 @@ __device__ __forceinline__ void dec_hash_ct_one(const KemParams &P, const uint8_
 // Decapsulation front, independent of the decryption: GenMatrix from the seed
 // of the pk embedded in sk, and the ciphertext hash H(c) (saber_dec,
 // cuda_kernel.cu:383-384 and :447).  part 0: threads i < n expand GenMatrix,
-// threads n..2n-1 hash; part 1: GenMatrix only; part 2: H(c) only (n threads).
+// threads warp_round(n) + i hash; part 1: GenMatrix only; part 2: H(c) only
+// (n threads each).
 __global__ void __launch_bounds__(128) k_dec_front(KemParams P, const uint8_t *sk,
                                                     const uint8_t *ct, uint8_t *a_stream,
                                                     uint8_t *hc, int n, int part) {
-  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (part == 1 && t >= (size_t)n) return;
-  if (part == 2) t += (size_t)n;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nal = warp_round((size_t)n);
+  if (part != 0) {
+    if (t < (size_t)n) {
+      if (part == 1) dec_genmatrix_one(P, sk, a_stream, t);
+      else dec_hash_ct_one(P, ct, hc, t);
+    }
+    return;
+  }
   if (t < (size_t)n)
     dec_genmatrix_one(P, sk, a_stream, t);
-  else if (t < 2 * (size_t)n)
-    dec_hash_ct_one(P, ct, hc, t - n);
+  else if (t >= nal && t < nal + n)
+    dec_hash_ct_one(P, ct, hc, t - nal);
 }
 
 // The same 2n sponges (GenMatrix, then H(c)) from a capped grid that leaves
 // room on every SM for the decryption beside it: threads stride over the
-// sponges, GenMatrix ones (the longer) first.
+// sponges, GenMatrix ones (the longer) first.  The stride is a multiple of
+// the block, so a warp's threads keep one role.
 __global__ void __launch_bounds__(128) k_dec_front_strided(KemParams P, const uint8_t *sk,
                                                             const uint8_t *ct, uint8_t *a_stream,
                                                             uint8_t *hc, int n) {
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < 2 * (size_t)n; t += stride) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x, nal = warp_round((size_t)n);
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nal + n; t += stride) {
     if (t < (size_t)n)
       dec_genmatrix_one(P, sk, a_stream, t);
-    else
-      dec_hash_ct_one(P, ct, hc, t - n);
+    else if (t >= nal)
+      dec_hash_ct_one(P, ct, hc, t - nal);
   }
 }
 
@@ -203,14 +211,15 @@ __device__ __forceinline__ int hash_group(const HashGroup *T, int ng, int gi) {
 }
 
 // part 1: GenMatrix of every instance; part 2: H(c); part 0: both, threads
-// total..2 total - 1 hashing.
+// warp_round(total) + i hashing.
 __global__ void __launch_bounds__(128) k_mix_front(const HashGroup *T, int ng, int total, int part) {
   int gi = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   bool gen = part == 1;
   if (part == 0) {
-    if (gi >= 2 * total) return;
+    const int tal = (int)warp_round((size_t)total);
     gen = gi < total;
-    if (!gen) gi -= total;
+    if (!gen && (gi < tal || gi >= tal + total)) return;
+    if (!gen) gi -= tal;
   } else if (gi >= total) {
     return;
   }

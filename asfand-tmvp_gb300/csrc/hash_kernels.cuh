@@ -22,6 +22,12 @@ struct ShakeJob {
   size_t seed_out_stride, seed_out_off;
 };
 
+// Kernels with two sponge roles over n instances start the second role at
+// thread warp_round(n), so that no warp runs both roles: their loops differ
+// in length, and a warp holding both would run one after the other.  Their
+// grids cover warp_round(n) + n threads.
+__host__ __device__ inline size_t warp_round(size_t n) { return (n + 31) & ~(size_t)31; }
+
 __global__ void k_shake_jobs(ShakeJob j0, ShakeJob j1, int n);
 __global__ void k_enc_front(KemParams P, const uint8_t *pk, const uint8_t *coins, uint8_t *mbuf,
                             uint8_t *kr, uint8_t *s_stream, uint8_t *a_stream, int n);
@@ -37,6 +43,21 @@ __global__ void k_dec_front_strided(KemParams P, const uint8_t *sk, const uint8_
 __global__ void k_kp_final(KemParams P, const uint8_t *pk, uint8_t *sk, const uint8_t *coins,
                            int n);
 __global__ void k_sha3_256_batch(const uint8_t *in, int inbytes, uint8_t *out, int n);
+
+// The same stages with one warp per sponge (hash_warp.cu): sponge w of a
+// launch is block w of kWarpHashBlock threads, warp_blocks(sponges) blocks.
+constexpr unsigned kWarpHashBlock = 32;
+inline unsigned warp_blocks(size_t sponges) { return (unsigned)sponges; }
+__global__ void k_dec_front_w(KemParams P, const uint8_t *sk, const uint8_t *ct, uint8_t *a_stream, uint8_t *hc,
+                              int n, int part);
+__global__ void k_dec_g_w(KemParams P, const uint8_t *mbuf, uint8_t *kr, uint8_t *s_stream, int n);
+__global__ void k_final_key_w(KemParams P, const uint8_t *ct, const uint8_t *hc, const uint8_t *kr,
+                              const uint8_t *fail, const uint8_t *sk, size_t sk_stride, uint8_t *ss, int n);
+__global__ void k_enc_front_w(KemParams P, const uint8_t *pk, const uint8_t *coins, uint8_t *mbuf, uint8_t *kr,
+                              uint8_t *s_stream, uint8_t *a_stream, int n, int with_gm);
+__global__ void k_genmatrix_w(KemParams P, const uint8_t *pk, size_t pk_stride, uint8_t *a_stream, int n);
+__global__ void k_shake_jobs_w(ShakeJob j0, ShakeJob j1, int n);
+__global__ void k_kp_final_w(KemParams P, const uint8_t *pk, uint8_t *sk, const uint8_t *coins, int n);
 
 // Mixed-parameter decapsulation: group g covers global instances
 // [first, first + n) with its own parameters and buffers (device table).

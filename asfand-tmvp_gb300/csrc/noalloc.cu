@@ -178,7 +178,7 @@ extern "C" int tmvp_kem_dec_batch_noalloc(tmvp_param_set set, size_t n, uint8_t 
           *kr = base + kOffKr, *fail = base + kOffFail, *hc = base + kOffHc;
   // the error bits must start at zero; every other buffer is fully rewritten
   if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return TMVP_EDEVICE;
-  k_dec_front<<<nblocks(2 * n), 128, 0, s>>>(P, sk, ct, a_stream, hc, (int)n, 0);
+  k_dec_front<<<nblocks(warp_round(n) + n), 128, 0, s>>>(P, sk, ct, a_stream, hc, (int)n, 0);
   CpaArgs a{};
   a.P = P;
   a.n = (int)n;

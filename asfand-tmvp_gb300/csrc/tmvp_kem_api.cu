@@ -73,6 +73,7 @@ struct tmvp_ctx {
   size_t dev_chunk = 32768;                        // chunk of device-input decapsulation (0: none)
   bool serial = false;                             // every stage on the caller's stream, one at a time
   int front_cap = 0;                               // Keccak-front blocks per SM (0: one thread per sponge)
+  size_t warp_hash = 2048;                         // Keccak launches of <= this many sponges: a warp per sponge
   // set by the caller (tmvp_ctx_set_*): then the autotuner's per-batch choice does not apply
   bool host_chunk_set = false, host_ramp_set = false, dev_chunk_set = false, front_cap_set = false;
   int nsm = 0;                                     // SMs of the device
@@ -299,6 +300,14 @@ inline unsigned blocks_for(size_t threads, unsigned bs) { return (unsigned)((thr
 // Threads per block of the Keccak kernels (one sponge per thread): small
 // blocks spread a batch evenly over the 152 SMs of an ALU-bound stage.
 constexpr unsigned kHashBlock = 64;
+// Keccak launches of few sponges run one warp per sponge (hash_warp.cu): a
+// lone thread-per-sponge permutation takes ~4.7 us however idle the GPU is,
+// the warp form ~2.1 us until its shuffles fill the SMs (~2.5 K sponges of
+// GenMatrix alone).  Launches of short sponges (G, the final key: 1-6
+// permutations) gain less and, beside the other stages of a pass, lose from
+// ~1 K sponges, so they count four times.
+inline bool warp_hash(const tmvp_ctx *c, size_t sponges) { return sponges <= c->warp_hash; }
+inline bool warp_hash_short(const tmvp_ctx *c, size_t sponges) { return 4 * sponges <= c->warp_hash; }
 
 int check_common(tmvp_ctx *c, int set, size_t n, int form, KemParams *P) {
   if (!c) return TMVP_EINVAL;
@@ -431,11 +440,16 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   }
   if (a_cached) {  // GenMatrix given: the front is H(c) alone
     StageTimer tm_(c, "dec_front", side);
-    k_dec_front<<<blocks_for(n, kHashBlock), kHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
+    if (warp_hash(c, n))
+      k_dec_front_w<<<warp_blocks(n), kWarpHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
+    else
+      k_dec_front<<<blocks_for(n, kHashBlock), kHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
   } else {
     StageTimer tm_(c, "dec_front", side);
-    const unsigned grid = blocks_for(2 * n, kHashBlock);
-    if (c->front_cap > 0 && !c->serial && grid > (unsigned)(c->nsm * c->front_cap))
+    const unsigned grid = blocks_for(warp_round(n) + n, kHashBlock);
+    if (warp_hash(c, 2 * n))
+      k_dec_front_w<<<warp_blocks(2 * n), kWarpHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 0);
+    else if (c->front_cap > 0 && !c->serial && grid > (unsigned)(c->nsm * c->front_cap))
       k_dec_front_strided<<<(unsigned)(c->nsm * c->front_cap), kHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc,
                                                                                    (int)n);
     else
@@ -464,7 +478,10 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   }
   {
     StageTimer tm_(c, "dec_g", s);
-    k_dec_g<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, w.mbuf, w.kr, w.s_stream, (int)n);
+    if (warp_hash_short(c, n))
+      k_dec_g_w<<<warp_blocks(n), kWarpHashBlock, 0, s>>>(P, w.mbuf, w.kr, w.s_stream, (int)n);
+    else
+      k_dec_g<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, w.mbuf, w.kr, w.s_stream, (int)n);
   }
   c->launches++;
   TRY_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));  // join: GenMatrix
@@ -485,8 +502,12 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   if ((r = run_cpa(c, form, kReenc, b, s))) return r;
   {
     StageTimer tm_(c, "final_key", s);
-    k_final_key<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, ct, w.hc, w.kr, w.fail, sk,
-                                                                 key_shared ? 0 : (size_t)P.sk_bytes, ss, (int)n);
+    const size_t sk_stride = key_shared ? 0 : (size_t)P.sk_bytes;
+    if (warp_hash_short(c, n))
+      k_final_key_w<<<warp_blocks(n), kWarpHashBlock, 0, s>>>(P, ct, w.hc, w.kr, w.fail, sk, sk_stride, ss, (int)n);
+    else
+      k_final_key<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, ct, w.hc, w.kr, w.fail, sk, sk_stride, ss,
+                                                                   (int)n);
   }
   c->launches++;
   return TMVP_OK;
@@ -680,6 +701,13 @@ int tmvp_ctx_set_front_cap(tmvp_ctx *c, int blocks_per_sm) {
   return set_err(TMVP_OK);
 }
 
+int tmvp_ctx_set_warp_hash(tmvp_ctx *c, size_t max_sponges) {
+  if (!c) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->warp_hash = max_sponges;
+  return set_err(TMVP_OK);
+}
+
 int tmvp_ctx_set_serial(tmvp_ctx *c, int on) {
   if (!c) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(c->mu);
@@ -760,7 +788,10 @@ int tmvp_kem_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *p
   ShakeJob j1{bco.dev, 96, 32, s_stream, (size_t)P.gs_bytes, P.gs_bytes, 0, nullptr, 0, 0};
   {
     StageTimer tm_(c, "shake_jobs", s);
-    k_shake_jobs<<<blocks_for(2 * n, kHashBlock), kHashBlock, 0, s>>>(j0, j1, (int)n);
+    if (warp_hash(c, 2 * n))
+      k_shake_jobs_w<<<warp_blocks(2 * n), kWarpHashBlock, 0, s>>>(j0, j1, (int)n);
+    else
+      k_shake_jobs<<<blocks_for(warp_round(n) + n, kHashBlock), kHashBlock, 0, s>>>(j0, j1, (int)n);
   }
   c->launches++;
   CpaArgs a{};
@@ -774,7 +805,10 @@ int tmvp_kem_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *p
   if ((r = run_cpa(c, form, kKeygen, a, s))) return set_err(r);
   {
     StageTimer tm_(c, "kp_final", s);
-    k_kp_final<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, bpk.dev, bsk.dev, bco.dev, (int)n);
+    if (warp_hash_short(c, n))
+      k_kp_final_w<<<warp_blocks(n), kWarpHashBlock, 0, s>>>(P, bpk.dev, bsk.dev, bco.dev, (int)n);
+    else
+      k_kp_final<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, bpk.dev, bsk.dev, bco.dev, (int)n);
   }
   c->launches++;
   if ((r = download(bpk, s)) || (r = download(bsk, s))) return set_err(r);
@@ -812,9 +846,13 @@ int enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, uint8_t *s
   if ((r = upload(bpk, s)) || (r = upload(bco, s))) return set_err(r);
   {
     StageTimer tm_(c, "enc_front", s);
-    // threads n..2n-1 expand GenMatrix, unless it is given
-    k_enc_front<<<blocks_for((a_cached ? 1 : 2) * n, kHashBlock), kHashBlock, 0, s>>>(P, bpk.dev, bco.dev, mbuf,
-                                                                                      kr, s_stream, a_stream, (int)n);
+    // the second role expands GenMatrix, unless it is given
+    if (warp_hash(c, a_cached ? n : 2 * n))
+      k_enc_front_w<<<warp_blocks(a_cached ? n : 2 * n), kWarpHashBlock, 0, s>>>(
+          P, bpk.dev, bco.dev, mbuf, kr, s_stream, a_stream, (int)n, a_cached ? 0 : 1);
+    else
+      k_enc_front<<<blocks_for(a_cached ? n : warp_round(n) + n, kHashBlock), kHashBlock, 0, s>>>(
+          P, bpk.dev, bco.dev, mbuf, kr, s_stream, a_stream, (int)n);
   }
   c->launches++;
   CpaArgs a{};
@@ -831,8 +869,12 @@ int enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, uint8_t *s
   if ((r = run_cpa(c, form, kEncrypt, a, s))) return set_err(r);
   {
     StageTimer tm_(c, "final_key", s);
-    k_final_key<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, bct.dev, nullptr, kr, nullptr, nullptr, 0,
-                                                                 bss.dev, (int)n);
+    if (warp_hash_short(c, n))
+      k_final_key_w<<<warp_blocks(n), kWarpHashBlock, 0, s>>>(P, bct.dev, nullptr, kr, nullptr, nullptr, 0, bss.dev,
+                                                               (int)n);
+    else
+      k_final_key<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, bct.dev, nullptr, kr, nullptr, nullptr, 0,
+                                                                   bss.dev, (int)n);
   }
   c->launches++;
   if ((r = download(bct, s)) || (r = download(bss, s))) return set_err(r);
@@ -865,7 +907,10 @@ int tmvp_genmatrix_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *a_s
   if (classify(a_stream, n * P.gm_bytes, c->device).host || classify(pk, n * pk_stride, c->device).host)
     return set_err(TMVP_EINVAL);  // device buffers only
   cudaStream_t s = (cudaStream_t)stream;
-  k_genmatrix<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, pk, pk_stride, a_stream, (int)n);
+  if (warp_hash(c, n))
+    k_genmatrix_w<<<warp_blocks(n), kWarpHashBlock, 0, s>>>(P, pk, pk_stride, a_stream, (int)n);
+  else
+    k_genmatrix<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, pk, pk_stride, a_stream, (int)n);
   c->launches++;
   return set_err(finish(c, s, false));
 }
@@ -946,7 +991,10 @@ int tmvp_kem_dec_batch_onekey(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t
     TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
     {
       StageTimer tm_(c, "genmatrix", c->side);
-      k_genmatrix<<<1, kHashBlock, 0, c->side>>>(P, bsk.dev + P.indcpa_sk_bytes, 0, a_one, 1);
+      if (warp_hash(c, 1))
+        k_genmatrix_w<<<1, kWarpHashBlock, 0, c->side>>>(P, bsk.dev + P.indcpa_sk_bytes, 0, a_one, 1);
+      else
+        k_genmatrix<<<1, kHashBlock, 0, c->side>>>(P, bsk.dev + P.indcpa_sk_bytes, 0, a_one, 1);
     }
     c->launches++;
     TRY_CUDA(cudaEventRecord(c->gm_ev, c->side));
@@ -1000,7 +1048,10 @@ int tmvp_kem_dec_batch_onekey(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t
   TRY_CUDA(cudaStreamWaitEvent(gs, c->fork_ev, 0));
   {
     StageTimer tm_(c, "genmatrix", gs);
-    k_genmatrix<<<1, kHashBlock, 0, gs>>>(P, bsk.dev + P.indcpa_sk_bytes, 0, a_one, 1);
+    if (warp_hash(c, 1))
+      k_genmatrix_w<<<1, kWarpHashBlock, 0, gs>>>(P, bsk.dev + P.indcpa_sk_bytes, 0, a_one, 1);
+    else
+      k_genmatrix<<<1, kHashBlock, 0, gs>>>(P, bsk.dev + P.indcpa_sk_bytes, 0, a_one, 1);
     if (!shared)
       k_replicate16<<<grid, 256, 0, gs>>>(reinterpret_cast<uint4 *>(a_rep), reinterpret_cast<const uint4 *>(a_one),
                                           P.gm_bytes / 16, n);
@@ -1165,7 +1216,10 @@ int tmvp_indcpa_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t
   ShakeJob j1{bse.dev, 64, 32, s_stream, (size_t)P.gs_bytes, P.gs_bytes, 0, nullptr, 0, 0};
   {
     StageTimer tm_(c, "shake_jobs", s);
-    k_shake_jobs<<<blocks_for(2 * n, kHashBlock), kHashBlock, 0, s>>>(j0, j1, (int)n);
+    if (warp_hash(c, 2 * n))
+      k_shake_jobs_w<<<warp_blocks(2 * n), kWarpHashBlock, 0, s>>>(j0, j1, (int)n);
+    else
+      k_shake_jobs<<<blocks_for(warp_round(n) + n, kHashBlock), kHashBlock, 0, s>>>(j0, j1, (int)n);
   }
   c->launches++;
   CpaArgs a{};
@@ -1212,7 +1266,10 @@ int tmvp_indcpa_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct
               (size_t)P.gm_bytes, P.gm_bytes, 0, nullptr, 0, 0};
   {
     StageTimer tm_(c, "shake_jobs", s);
-    k_shake_jobs<<<blocks_for(2 * n, kHashBlock), kHashBlock, 0, s>>>(j0, j1, (int)n);
+    if (warp_hash(c, 2 * n))
+      k_shake_jobs_w<<<warp_blocks(2 * n), kWarpHashBlock, 0, s>>>(j0, j1, (int)n);
+    else
+      k_shake_jobs<<<blocks_for(warp_round(n) + n, kHashBlock), kHashBlock, 0, s>>>(j0, j1, (int)n);
   }
   c->launches++;
   CpaArgs a{};
@@ -1598,7 +1655,8 @@ int mixed_enqueue(tmvp_ctx *c, size_t ng, const tmvp_dec_group *gr, uint8_t *ws,
   // GenMatrix and H(c) of every group in one launch (2 total sponges)
   {
     StageTimer tm_(c, "mix_front", ms.side);
-    k_mix_front<<<blocks_for(2 * (size_t)total, kHashBlock), kHashBlock, 0, ms.side>>>(th, (int)ng, total, 0);
+    k_mix_front<<<blocks_for(warp_round((size_t)total) + total, kHashBlock), kHashBlock, 0, ms.side>>>(
+        th, (int)ng, total, 0);
   }
   TRY_CUDA(cudaEventRecord(c->join_ev, ms.side));
   // the per-set IND-CPA launches of a step run side by side on the context's

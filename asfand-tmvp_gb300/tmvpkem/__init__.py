@@ -124,6 +124,7 @@ def lib(build_if_missing: bool = False):
     L.tmvp_ctx_set_dev_chunk.argtypes = [P, S]
     L.tmvp_ctx_set_serial.argtypes = [P, ctypes.c_int]
     L.tmvp_ctx_set_front_cap.argtypes = [P, ctypes.c_int]
+    L.tmvp_ctx_set_warp_hash.argtypes = [P, S]
     L.tmvp_kem_dec_batch_noalloc.argtypes = [I, S, P, P, P, I, P, P]
     L.tmvp_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]
     L.tmvp_server_destroy.argtypes = [P]
@@ -403,6 +404,10 @@ class Context:
     def set_front_cap(self, blocks_per_sm: int):
         """Keccak-front blocks per SM in decapsulation (0 = one thread per sponge)."""
         _check(lib().tmvp_ctx_set_front_cap(self.h, blocks_per_sm), "tmvp_ctx_set_front_cap")
+
+    def set_warp_hash(self, max_sponges: int):
+        """Keccak launches of at most max_sponges sponges run one warp per sponge (0: never)."""
+        _check(lib().tmvp_ctx_set_warp_hash(self.h, max_sponges), "tmvp_ctx_set_warp_hash")
 
     def keccak_rate(self, perms: int = 64):
         """(Keccak-f[1600] permutations per second at full occupancy, blocks per SM)."""
