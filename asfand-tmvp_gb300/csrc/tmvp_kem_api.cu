@@ -55,6 +55,7 @@ struct StageStat {
   std::string name;
   uint64_t launches = 0;
   double total_ms = 0;
+  double busy_ms = 0;  // union of the launches' intervals (launches on several streams overlap)
 };
 
 struct tmvp_ctx {
@@ -259,14 +260,33 @@ struct StageTimer {
 };
 
 void collect_stage_times(tmvp_ctx *c) {
+  if (c->pending.empty()) return;
+  for (auto &p : c->pending) cudaEventSynchronize(p.second.second);
+  // every launch's interval relative to the first pending event; per stage,
+  // the union of its intervals is the time at least one of them ran
+  const cudaEvent_t ref = c->pending.front().second.first;
+  std::vector<std::vector<std::pair<float, float>>> iv(c->stages.size());
   for (auto &p : c->pending) {
-    cudaEventSynchronize(p.second.second);
-    float ms = 0;
+    float ms = 0, t0 = 0, t1 = 0;
     cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+    cudaEventElapsedTime(&t0, ref, p.second.first);
+    cudaEventElapsedTime(&t1, ref, p.second.second);
     c->stages[p.first].launches++;
     c->stages[p.first].total_ms += ms;
+    iv[p.first].push_back({t0, t1});
     c->ev_pool.push_back(p.second.first);
     c->ev_pool.push_back(p.second.second);
+  }
+  for (size_t i = 0; i < iv.size(); i++) {
+    auto &v = iv[i];
+    std::sort(v.begin(), v.end());
+    double busy = 0;
+    for (size_t k = 0; k < v.size();) {
+      float a = v[k].first, b = v[k].second;
+      for (k++; k < v.size() && v[k].first <= b; k++) b = std::max(b, v[k].second);
+      busy += b - a;
+    }
+    c->stages[i].busy_ms += busy;
   }
   c->pending.clear();
 }
@@ -757,6 +777,16 @@ int tmvp_ctx_stage_stats(tmvp_ctx *c, int idx, char *name, size_t name_len, uint
   }
   if (launches) *launches = st.launches;
   if (total_ms) *total_ms = st.total_ms;
+  return set_err(TMVP_OK);
+}
+
+int tmvp_ctx_stage_busy(tmvp_ctx *c, int idx, double *busy_ms) {
+  if (!c || !busy_ms) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  Guard g(c);
+  collect_stage_times(c);
+  if (idx < 0 || (size_t)idx >= c->stages.size()) return set_err(TMVP_EINVAL);
+  *busy_ms = c->stages[idx].busy_ms;
   return set_err(TMVP_OK);
 }
 uint64_t tmvp_ctx_launch_count(const tmvp_ctx *c) { return c ? c->launches : 0; }

@@ -125,6 +125,7 @@ def lib(build_if_missing: bool = False):
     L.tmvp_ctx_set_serial.argtypes = [P, ctypes.c_int]
     L.tmvp_ctx_set_front_cap.argtypes = [P, ctypes.c_int]
     L.tmvp_ctx_set_warp_hash.argtypes = [P, S]
+    L.tmvp_ctx_stage_busy.argtypes = [P, I, ctypes.POINTER(ctypes.c_double)]
     L.tmvp_kem_dec_batch_noalloc.argtypes = [I, S, P, P, P, I, P, P]
     L.tmvp_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]
     L.tmvp_server_destroy.argtypes = [P]
@@ -345,6 +346,20 @@ class Context:
             _check(L.tmvp_ctx_stage_stats(self.h, i, name, 64, ctypes.byref(la), ctypes.byref(ms)),
                    "tmvp_ctx_stage_stats")
             out[name.value.decode()] = (la.value, ms.value)
+        return out
+
+    def stage_busy(self) -> dict:
+        """{kernel name: busy device ms} since timing was enabled: the union of
+        the stage's launch intervals (overlapping launches counted once)."""
+        L = lib()
+        n = L.tmvp_ctx_stage_stats(self.h, -1, None, 0, None, None)
+        out = {}
+        for i in range(n):
+            name = ctypes.create_string_buffer(64)
+            busy = ctypes.c_double()
+            _check(L.tmvp_ctx_stage_stats(self.h, i, name, 64, None, None), "tmvp_ctx_stage_stats")
+            _check(L.tmvp_ctx_stage_busy(self.h, i, ctypes.byref(busy)), "tmvp_ctx_stage_busy")
+            out[name.value.decode()] = busy.value
         return out
 
     # --- pointer-level calls (host or device buffers, caller-owned) --------

@@ -342,10 +342,11 @@ def run_ours(args):
         per = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
         total = ev[0].elapsed_time(ev[steps])
         stages = ctx.stage_stats() if stage_timing else {}
+        busy = ctx.stage_busy() if stage_timing else {}
         if stage_timing:
             ctx.set_timing(False)
         ok = bool(torch.equal(ss, ss_ref))
-        return total, per, launches, stages, ok
+        return total, per, launches, (stages, busy), ok
 
     gpu_id = None
     try:
@@ -355,7 +356,8 @@ def run_ours(args):
     sampler = ClockSampler(gpu_id)
     sampler.wait_started()
     nvml = NvmlSampler(gpu_id)
-    total_ms, per_ms, launches, stages, exact_main = timed(T.FORM_AUTO, args.steps, stage_timing=True)
+    total_ms, per_ms, launches, (stages, stages_busy), exact_main = timed(T.FORM_AUTO, args.steps,
+                                                                         stage_timing=True)
     clocks_nvml = nvml.stop(window[0], window[1])
     clocks_smi = sampler.stop(window[0], window[1])
     clocks = clocks_nvml or clocks_smi
@@ -443,7 +445,7 @@ def run_ours(args):
     ks = max(10, args.steps // 10)
     ctx.set_serial(True)
     try:
-        _, _, _, stages_iso, exact_iso = timed(T.FORM_AUTO, ks, stage_timing=True)
+        _, _, _, (stages_iso, _), exact_iso = timed(T.FORM_AUTO, ks, stage_timing=True)
     finally:
         ctx.set_serial(False)
     exact_main = exact_main and exact_iso
@@ -453,6 +455,20 @@ def run_ours(args):
         if k in stages and stages[k][0]:
             v["avg_launch_ms_in_pass"] = stages[k][1] / stages[k][0]
             v["instances_per_launch_in_pass"] = n * args.steps / stages[k][0]
+            # the chunk chains' launches of a stage overlap in the pass: the union of their
+            # intervals is the time the stage held the GPU in each step
+            busy = stages_busy.get(k)
+            if busy:
+                v["busy_ms_per_step_in_pass"] = busy / args.steps
+                if "keccak" in v:
+                    key = next(x for x in _STAGE_WORK if k.startswith(x))
+                    rate = n * args.steps * _STAGE_WORK[key][2] / (busy / 1e3)
+                    pk = v["keccak"].get("peak_perm_per_s")
+                    v["keccak"]["perm_per_s_in_pass"] = rate
+                    v["keccak"]["frac_in_pass"] = rate / pk if pk else None
+                    v["keccak"]["in_pass_note"] = ("permutations of the step over the stage's busy time in the "
+                                                   "pass (union of its launches' intervals; it shares the SMs "
+                                                   "with the decryption there)")
     lead = max(roof_all, key=lambda k: roof_all[k]["share_of_stage_time"]) if roof_all else None
     roof = dict(roof_all[lead]) if lead else {}
     if lead:
@@ -478,6 +494,7 @@ def run_ours(args):
                       "checked": n, "oracle_sample": 256, "oracle_match": oracle_ok},
         "roofline": roof,
         "stages_ms_per_launch_in_pass": {k: v[1] / max(v[0], 1) for k, v in stages.items()},
+        "stages_busy_ms_per_step_in_pass": {k: b / args.steps for k, b in stages_busy.items()},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * (CT_BYTES + SK_BYTES),
                 "d2h_bytes_per_step": n * 32, "ms_per_step": statistics.mean(e2e_ms),
                 "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99)),

@@ -119,6 +119,11 @@ uint64_t tmvp_ctx_launch_count(const tmvp_ctx *ctx);
 int tmvp_ctx_set_timing(tmvp_ctx *ctx, int enable);
 int tmvp_ctx_stage_stats(tmvp_ctx *ctx, int idx, char *name, size_t name_len,
                          uint64_t *launches, double *total_ms);
+/* The stage's busy milliseconds: the union of its launches' intervals, the
+ * time during which at least one of them ran.  Launches of one stage on
+ * several streams (the chunk chains of a decapsulation) overlap, so their
+ * summed milliseconds overstate the time the stage took. */
+int tmvp_ctx_stage_busy(tmvp_ctx *ctx, int idx, double *busy_ms);
 
 /* Batched, derandomised KEM.  stream: a cudaStream_t (NULL = legacy default).
  * A secret key whose coefficients are outside the tensor-core forms' range
