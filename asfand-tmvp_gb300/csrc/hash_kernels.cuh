@@ -59,6 +59,23 @@ __global__ void k_genmatrix_w(KemParams P, const uint8_t *pk, size_t pk_stride, 
 __global__ void k_shake_jobs_w(ShakeJob j0, ShakeJob j1, int n);
 __global__ void k_kp_final_w(KemParams P, const uint8_t *pk, uint8_t *sk, const uint8_t *coins, int n);
 
+// The same stages with two threads per sponge (hash_pair.cu): thread t holds
+// half t & 1 of sponge t >> 1; kernels with two roles start the second at
+// thread warp_round(2n).  Grids of pair_blocks(threads) blocks of
+// kPairHashBlock.
+constexpr unsigned kPairHashBlock = 128;
+inline unsigned pair_blocks(size_t threads) { return (unsigned)((threads + kPairHashBlock - 1) / kPairHashBlock); }
+__global__ void k_dec_front_p(KemParams P, const uint8_t *sk, const uint8_t *ct, uint8_t *a_stream, uint8_t *hc,
+                              int n, int part);
+__global__ void k_dec_g_p(KemParams P, const uint8_t *mbuf, uint8_t *kr, uint8_t *s_stream, int n);
+__global__ void k_final_key_p(KemParams P, const uint8_t *ct, const uint8_t *hc, const uint8_t *kr,
+                              const uint8_t *fail, const uint8_t *sk, size_t sk_stride, uint8_t *ss, int n);
+__global__ void k_enc_front_p(KemParams P, const uint8_t *pk, const uint8_t *coins, uint8_t *mbuf, uint8_t *kr,
+                              uint8_t *s_stream, uint8_t *a_stream, int n, int with_gm);
+__global__ void k_genmatrix_p(KemParams P, const uint8_t *pk, size_t pk_stride, uint8_t *a_stream, int n);
+__global__ void k_shake_jobs_p(ShakeJob j0, ShakeJob j1, int n);
+__global__ void k_kp_final_p(KemParams P, const uint8_t *pk, uint8_t *sk, const uint8_t *coins, int n);
+
 // Mixed-parameter decapsulation: group g covers global instances
 // [first, first + n) with its own parameters and buffers (device table).
 struct HashGroup {

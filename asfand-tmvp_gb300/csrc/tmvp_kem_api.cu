@@ -74,7 +74,8 @@ struct tmvp_ctx {
   size_t dev_chunk = 32768;                        // chunk of device-input decapsulation (0: none)
   bool serial = false;                             // every stage on the caller's stream, one at a time
   int front_cap = 0;                               // Keccak-front blocks per SM (0: one thread per sponge)
-  size_t warp_hash = 2048;                         // Keccak launches of <= this many sponges: a warp per sponge
+  size_t warp_hash = 1024;                         // Keccak launches of <= this many sponges: a warp per sponge
+  size_t pair_hash = 16384;                        // else of <= this many: two threads per sponge
   // set by the caller (tmvp_ctx_set_*): then the autotuner's per-batch choice does not apply
   bool host_chunk_set = false, host_ramp_set = false, dev_chunk_set = false, front_cap_set = false;
   int nsm = 0;                                     // SMs of the device
@@ -320,14 +321,22 @@ inline unsigned blocks_for(size_t threads, unsigned bs) { return (unsigned)((thr
 // Threads per block of the Keccak kernels (one sponge per thread): small
 // blocks spread a batch evenly over the 152 SMs of an ALU-bound stage.
 constexpr unsigned kHashBlock = 64;
-// Keccak launches of few sponges run one warp per sponge (hash_warp.cu): a
-// lone thread-per-sponge permutation takes ~4.7 us however idle the GPU is,
-// the warp form ~2.1 us until its shuffles fill the SMs (~2.5 K sponges of
-// GenMatrix alone).  Launches of short sponges (G, the final key: 1-6
-// permutations) gain less and, beside the other stages of a pass, lose from
-// ~1 K sponges, so they count four times.
-inline bool warp_hash(const tmvp_ctx *c, size_t sponges) { return sponges <= c->warp_hash; }
-inline bool warp_hash_short(const tmvp_ctx *c, size_t sponges) { return 4 * sponges <= c->warp_hash; }
+// The form of a Keccak launch.  One thread per sponge (hash_kernels.cu)
+// keeps a warp's share of the integer pipe busy: ~4.7 us per permutation
+// however idle the GPU is, and the best rate once the pipe is full.  One warp
+// per sponge (hash_warp.cu): ~2.1 us per permutation until its shuffles fill
+// the SMs (~1 K GenMatrix sponges).  Two threads per sponge (hash_pair.cu):
+// ~3.3 us per permutation up to ~10 K sponges, the thread form's integer work
+// per sponge with twice its warps.  Launches of short sponges (G, the final
+// key, the key-generation tail: 1-8 permutations) count four times against
+// the warp form's limit: beside the other stages of a pass they lose there
+// sooner.
+enum HashForm { kHashThread, kHashWarp, kHashPair };
+inline HashForm hash_form(const tmvp_ctx *c, size_t sponges, bool short_sponges = false) {
+  if ((short_sponges ? 4 * sponges : sponges) <= c->warp_hash) return kHashWarp;
+  if (sponges <= c->pair_hash) return kHashPair;
+  return kHashThread;
+}
 
 int check_common(tmvp_ctx *c, int set, size_t n, int form, KemParams *P) {
   if (!c) return TMVP_EINVAL;
@@ -460,15 +469,22 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   }
   if (a_cached) {  // GenMatrix given: the front is H(c) alone
     StageTimer tm_(c, "dec_front", side);
-    if (warp_hash(c, n))
+    const HashForm f = hash_form(c, n);
+    if (f == kHashWarp)
       k_dec_front_w<<<warp_blocks(n), kWarpHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
+    else if (f == kHashPair)
+      k_dec_front_p<<<pair_blocks(2 * n), kPairHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
     else
       k_dec_front<<<blocks_for(n, kHashBlock), kHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 2);
   } else {
     StageTimer tm_(c, "dec_front", side);
     const unsigned grid = blocks_for(warp_round(n) + n, kHashBlock);
-    if (warp_hash(c, 2 * n))
+    const HashForm f = hash_form(c, 2 * n);
+    if (f == kHashWarp)
       k_dec_front_w<<<warp_blocks(2 * n), kWarpHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc, (int)n, 0);
+    else if (f == kHashPair)
+      k_dec_front_p<<<pair_blocks(warp_round(2 * n) + 2 * n), kPairHashBlock, 0, side>>>(P, sk, ct, w.a_stream,
+                                                                                        w.hc, (int)n, 0);
     else if (c->front_cap > 0 && !c->serial && grid > (unsigned)(c->nsm * c->front_cap))
       k_dec_front_strided<<<(unsigned)(c->nsm * c->front_cap), kHashBlock, 0, side>>>(P, sk, ct, w.a_stream, w.hc,
                                                                                    (int)n);
@@ -498,8 +514,11 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   }
   {
     StageTimer tm_(c, "dec_g", s);
-    if (warp_hash_short(c, n))
+    const HashForm f = hash_form(c, n, true);
+    if (f == kHashWarp)
       k_dec_g_w<<<warp_blocks(n), kWarpHashBlock, 0, s>>>(P, w.mbuf, w.kr, w.s_stream, (int)n);
+    else if (f == kHashPair)
+      k_dec_g_p<<<pair_blocks(2 * n), kPairHashBlock, 0, s>>>(P, w.mbuf, w.kr, w.s_stream, (int)n);
     else
       k_dec_g<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, w.mbuf, w.kr, w.s_stream, (int)n);
   }
@@ -523,8 +542,12 @@ int dec_pipeline(tmvp_ctx *c, const KemParams &P, size_t n, uint8_t *ss, const u
   {
     StageTimer tm_(c, "final_key", s);
     const size_t sk_stride = key_shared ? 0 : (size_t)P.sk_bytes;
-    if (warp_hash_short(c, n))
+    const HashForm f = hash_form(c, n, true);
+    if (f == kHashWarp)
       k_final_key_w<<<warp_blocks(n), kWarpHashBlock, 0, s>>>(P, ct, w.hc, w.kr, w.fail, sk, sk_stride, ss, (int)n);
+    else if (f == kHashPair)
+      k_final_key_p<<<pair_blocks(2 * n), kPairHashBlock, 0, s>>>(P, ct, w.hc, w.kr, w.fail, sk, sk_stride, ss,
+                                                                  (int)n);
     else
       k_final_key<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, ct, w.hc, w.kr, w.fail, sk, sk_stride, ss,
                                                                    (int)n);
@@ -728,6 +751,13 @@ int tmvp_ctx_set_warp_hash(tmvp_ctx *c, size_t max_sponges) {
   return set_err(TMVP_OK);
 }
 
+int tmvp_ctx_set_pair_hash(tmvp_ctx *c, size_t max_sponges) {
+  if (!c) return set_err(TMVP_EINVAL);
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->pair_hash = max_sponges;
+  return set_err(TMVP_OK);
+}
+
 int tmvp_ctx_set_serial(tmvp_ctx *c, int on) {
   if (!c) return set_err(TMVP_EINVAL);
   std::lock_guard<std::mutex> lk(c->mu);
@@ -818,8 +848,11 @@ int tmvp_kem_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *p
   ShakeJob j1{bco.dev, 96, 32, s_stream, (size_t)P.gs_bytes, P.gs_bytes, 0, nullptr, 0, 0};
   {
     StageTimer tm_(c, "shake_jobs", s);
-    if (warp_hash(c, 2 * n))
+    const HashForm f = hash_form(c, 2 * n);
+    if (f == kHashWarp)
       k_shake_jobs_w<<<warp_blocks(2 * n), kWarpHashBlock, 0, s>>>(j0, j1, (int)n);
+    else if (f == kHashPair)
+      k_shake_jobs_p<<<pair_blocks(warp_round(2 * n) + 2 * n), kPairHashBlock, 0, s>>>(j0, j1, (int)n);
     else
       k_shake_jobs<<<blocks_for(warp_round(n) + n, kHashBlock), kHashBlock, 0, s>>>(j0, j1, (int)n);
   }
@@ -835,8 +868,11 @@ int tmvp_kem_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *p
   if ((r = run_cpa(c, form, kKeygen, a, s))) return set_err(r);
   {
     StageTimer tm_(c, "kp_final", s);
-    if (warp_hash_short(c, n))
+    const HashForm f = hash_form(c, n, true);
+    if (f == kHashWarp)
       k_kp_final_w<<<warp_blocks(n), kWarpHashBlock, 0, s>>>(P, bpk.dev, bsk.dev, bco.dev, (int)n);
+    else if (f == kHashPair)
+      k_kp_final_p<<<pair_blocks(2 * n), kPairHashBlock, 0, s>>>(P, bpk.dev, bsk.dev, bco.dev, (int)n);
     else
       k_kp_final<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, bpk.dev, bsk.dev, bco.dev, (int)n);
   }
@@ -877,8 +913,12 @@ int enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, uint8_t *s
   {
     StageTimer tm_(c, "enc_front", s);
     // the second role expands GenMatrix, unless it is given
-    if (warp_hash(c, a_cached ? n : 2 * n))
+    const HashForm f = hash_form(c, a_cached ? n : 2 * n);
+    if (f == kHashWarp)
       k_enc_front_w<<<warp_blocks(a_cached ? n : 2 * n), kWarpHashBlock, 0, s>>>(
+          P, bpk.dev, bco.dev, mbuf, kr, s_stream, a_stream, (int)n, a_cached ? 0 : 1);
+    else if (f == kHashPair)
+      k_enc_front_p<<<pair_blocks(a_cached ? 2 * n : warp_round(2 * n) + 2 * n), kPairHashBlock, 0, s>>>(
           P, bpk.dev, bco.dev, mbuf, kr, s_stream, a_stream, (int)n, a_cached ? 0 : 1);
     else
       k_enc_front<<<blocks_for(a_cached ? n : warp_round(n) + n, kHashBlock), kHashBlock, 0, s>>>(
@@ -899,9 +939,13 @@ int enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct, uint8_t *s
   if ((r = run_cpa(c, form, kEncrypt, a, s))) return set_err(r);
   {
     StageTimer tm_(c, "final_key", s);
-    if (warp_hash_short(c, n))
+    const HashForm f = hash_form(c, n, true);
+    if (f == kHashWarp)
       k_final_key_w<<<warp_blocks(n), kWarpHashBlock, 0, s>>>(P, bct.dev, nullptr, kr, nullptr, nullptr, 0, bss.dev,
                                                                (int)n);
+    else if (f == kHashPair)
+      k_final_key_p<<<pair_blocks(2 * n), kPairHashBlock, 0, s>>>(P, bct.dev, nullptr, kr, nullptr, nullptr, 0,
+                                                                  bss.dev, (int)n);
     else
       k_final_key<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, bct.dev, nullptr, kr, nullptr, nullptr, 0,
                                                                    bss.dev, (int)n);
@@ -937,8 +981,11 @@ int tmvp_genmatrix_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *a_s
   if (classify(a_stream, n * P.gm_bytes, c->device).host || classify(pk, n * pk_stride, c->device).host)
     return set_err(TMVP_EINVAL);  // device buffers only
   cudaStream_t s = (cudaStream_t)stream;
-  if (warp_hash(c, n))
+  const HashForm f = hash_form(c, n);
+  if (f == kHashWarp)
     k_genmatrix_w<<<warp_blocks(n), kWarpHashBlock, 0, s>>>(P, pk, pk_stride, a_stream, (int)n);
+  else if (f == kHashPair)
+    k_genmatrix_p<<<pair_blocks(2 * n), kPairHashBlock, 0, s>>>(P, pk, pk_stride, a_stream, (int)n);
   else
     k_genmatrix<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, pk, pk_stride, a_stream, (int)n);
   c->launches++;
@@ -1021,7 +1068,7 @@ int tmvp_kem_dec_batch_onekey(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t
     TRY_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
     {
       StageTimer tm_(c, "genmatrix", c->side);
-      if (warp_hash(c, 1))
+      if (hash_form(c, 1) == kHashWarp)
         k_genmatrix_w<<<1, kWarpHashBlock, 0, c->side>>>(P, bsk.dev + P.indcpa_sk_bytes, 0, a_one, 1);
       else
         k_genmatrix<<<1, kHashBlock, 0, c->side>>>(P, bsk.dev + P.indcpa_sk_bytes, 0, a_one, 1);
@@ -1078,7 +1125,7 @@ int tmvp_kem_dec_batch_onekey(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t
   TRY_CUDA(cudaStreamWaitEvent(gs, c->fork_ev, 0));
   {
     StageTimer tm_(c, "genmatrix", gs);
-    if (warp_hash(c, 1))
+    if (hash_form(c, 1) == kHashWarp)
       k_genmatrix_w<<<1, kWarpHashBlock, 0, gs>>>(P, bsk.dev + P.indcpa_sk_bytes, 0, a_one, 1);
     else
       k_genmatrix<<<1, kHashBlock, 0, gs>>>(P, bsk.dev + P.indcpa_sk_bytes, 0, a_one, 1);
@@ -1246,8 +1293,11 @@ int tmvp_indcpa_keypair_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t
   ShakeJob j1{bse.dev, 64, 32, s_stream, (size_t)P.gs_bytes, P.gs_bytes, 0, nullptr, 0, 0};
   {
     StageTimer tm_(c, "shake_jobs", s);
-    if (warp_hash(c, 2 * n))
+    const HashForm f = hash_form(c, 2 * n);
+    if (f == kHashWarp)
       k_shake_jobs_w<<<warp_blocks(2 * n), kWarpHashBlock, 0, s>>>(j0, j1, (int)n);
+    else if (f == kHashPair)
+      k_shake_jobs_p<<<pair_blocks(warp_round(2 * n) + 2 * n), kPairHashBlock, 0, s>>>(j0, j1, (int)n);
     else
       k_shake_jobs<<<blocks_for(warp_round(n) + n, kHashBlock), kHashBlock, 0, s>>>(j0, j1, (int)n);
   }
@@ -1296,8 +1346,11 @@ int tmvp_indcpa_enc_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ct
               (size_t)P.gm_bytes, P.gm_bytes, 0, nullptr, 0, 0};
   {
     StageTimer tm_(c, "shake_jobs", s);
-    if (warp_hash(c, 2 * n))
+    const HashForm f = hash_form(c, 2 * n);
+    if (f == kHashWarp)
       k_shake_jobs_w<<<warp_blocks(2 * n), kWarpHashBlock, 0, s>>>(j0, j1, (int)n);
+    else if (f == kHashPair)
+      k_shake_jobs_p<<<pair_blocks(warp_round(2 * n) + 2 * n), kPairHashBlock, 0, s>>>(j0, j1, (int)n);
     else
       k_shake_jobs<<<blocks_for(warp_round(n) + n, kHashBlock), kHashBlock, 0, s>>>(j0, j1, (int)n);
   }

@@ -125,6 +125,7 @@ def lib(build_if_missing: bool = False):
     L.tmvp_ctx_set_serial.argtypes = [P, ctypes.c_int]
     L.tmvp_ctx_set_front_cap.argtypes = [P, ctypes.c_int]
     L.tmvp_ctx_set_warp_hash.argtypes = [P, S]
+    L.tmvp_ctx_set_pair_hash.argtypes = [P, S]
     L.tmvp_ctx_stage_busy.argtypes = [P, I, ctypes.POINTER(ctypes.c_double)]
     L.tmvp_kem_dec_batch_noalloc.argtypes = [I, S, P, P, P, I, P, P]
     L.tmvp_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]
@@ -423,6 +424,11 @@ class Context:
     def set_warp_hash(self, max_sponges: int):
         """Keccak launches of at most max_sponges sponges run one warp per sponge (0: never)."""
         _check(lib().tmvp_ctx_set_warp_hash(self.h, max_sponges), "tmvp_ctx_set_warp_hash")
+
+    def set_pair_hash(self, max_sponges: int):
+        """Keccak launches too large for the warp form and of at most max_sponges
+        sponges run two threads per sponge (0: never)."""
+        _check(lib().tmvp_ctx_set_pair_hash(self.h, max_sponges), "tmvp_ctx_set_pair_hash")
 
     def keccak_rate(self, perms: int = 64):
         """(Keccak-f[1600] permutations per second at full occupancy, blocks per SM)."""

@@ -225,16 +225,20 @@ int tmvp_ctx_set_serial(tmvp_ctx *ctx, int on);
  * SM; 0 (the default) launches one thread per sponge.  0..64.  Results do
  * not depend on it. */
 int tmvp_ctx_set_front_cap(tmvp_ctx *ctx, int blocks_per_sm);
-/* Keccak launches (GenMatrix, GenSecret, H, G, the final key) of at most
- * max_sponges sponges run one warp per sponge, the state spread over the
- * warp's lanes: about twice as fast per permutation while the GPU is far from
- * full (small batches, latency), slower once it is full.  Larger launches run
- * one thread per sponge.  Launches of short sponges (G, the final key, the
- * key-generation tail) count four times.  0: always one thread per sponge.
- * Default 2048.  Results do not depend on it.  No counterpart in the reference, whose hash
- * kernels run as one block of one thread per instance
+/* The form of each Keccak launch (GenMatrix, GenSecret, H, G, the final
+ * key).  Launches of at most warp_hash sponges run one warp per sponge, the
+ * state spread over the warp's lanes (~2.1 us per permutation while the GPU
+ * is far from full; launches of short sponges, G, the final key and the
+ * key-generation tail, count four times); larger ones of at most pair_hash
+ * sponges run two threads per sponge, each holding half of every state lane
+ * (~3.3 us per permutation up to ~10 K sponges); larger ones one thread per
+ * sponge (~4.7 us per permutation, the best rate once the GPU is full).
+ * Defaults 1024 and 16384; 0 turns a form off.  Results do not depend on
+ * them.  No counterpart in the reference, whose hash kernels run as one
+ * block of one thread per instance
  * (TMVP-Saber/SABER-GPU/src/cuda_kernel.cu:116-127). */
 int tmvp_ctx_set_warp_hash(tmvp_ctx *ctx, size_t max_sponges);
+int tmvp_ctx_set_pair_hash(tmvp_ctx *ctx, size_t max_sponges);
 
 /* ---------------------------------------------------------------------------
  * Request-serving loop with device-resident keys and continuous batching.

@@ -48,6 +48,7 @@ def test_invalid_arguments(T):
     assert T.lib().tmvp_ctx_set_host_chunk(None, 16384) == T.EINVAL
     assert T.lib().tmvp_ctx_set_dev_chunk(None, 32768) == T.EINVAL
     assert T.lib().tmvp_ctx_set_warp_hash(None, 2048) == T.EINVAL
+    assert T.lib().tmvp_ctx_set_pair_hash(None, 16384) == T.EINVAL
     busy = ctypes.c_double()
     assert T.lib().tmvp_ctx_stage_busy(None, 0, ctypes.byref(busy)) == T.EINVAL
     assert T.lib().tmvp_selftest_bounded_wait(None, None) == T.EINVAL
