@@ -22,6 +22,25 @@ struct ShakeJob {
   size_t seed_out_stride, seed_out_off;
 };
 
+// The form of a Keccak launch.  One thread per sponge (this file's kernels)
+// keeps a warp's share of the integer pipe busy: ~4.7 us per permutation
+// however idle the GPU is, and the best rate once the pipe is full.  One warp
+// per sponge (the _w kernels): ~2.1 us per permutation until its shuffles
+// fill the SMs (~1 K GenMatrix sponges).  Two threads per sponge (the _p
+// kernels): ~3.3 us per permutation up to ~10 K sponges, the thread form's
+// integer work per sponge with twice its warps.  Launches of short sponges
+// (G, the final key, the key-generation tail: 1-8 permutations) count four
+// times against the warp form's limit: beside the other stages of a pass
+// they lose there sooner.  kWarpHashDefault / kPairHashDefault are the
+// limits a context starts with (tmvp_ctx_set_warp_hash / _pair_hash).
+constexpr size_t kWarpHashDefault = 1024, kPairHashDefault = 16384;
+enum HashForm { kHashThread, kHashWarp, kHashPair };
+inline HashForm hash_form_for(size_t sponges, bool short_sponges, size_t warp_max, size_t pair_max) {
+  if ((short_sponges ? 4 * sponges : sponges) <= warp_max) return kHashWarp;
+  if (sponges <= pair_max) return kHashPair;
+  return kHashThread;
+}
+
 // Kernels with two sponge roles over n instances start the second role at
 // thread warp_round(n), so that no warp runs both roles: their loops differ
 // in length, and a warp holding both would run one after the other.  Their

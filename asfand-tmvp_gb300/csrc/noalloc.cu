@@ -178,7 +178,16 @@ extern "C" int tmvp_kem_dec_batch_noalloc(tmvp_param_set set, size_t n, uint8_t 
           *kr = base + kOffKr, *fail = base + kOffFail, *hc = base + kOffHc;
   // the error bits must start at zero; every other buffer is fully rewritten
   if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return TMVP_EDEVICE;
-  k_dec_front<<<nblocks(warp_round(n) + n), 128, 0, s>>>(P, sk, ct, a_stream, hc, (int)n, 0);
+  // the Keccak stages take the form a context would give them by default
+  const HashForm ff = hash_form_for(2 * n, false, kWarpHashDefault, kPairHashDefault);
+  const HashForm fs = hash_form_for(n, true, kWarpHashDefault, kPairHashDefault);
+  if (ff == kHashWarp)
+    k_dec_front_w<<<warp_blocks(2 * n), kWarpHashBlock, 0, s>>>(P, sk, ct, a_stream, hc, (int)n, 0);
+  else if (ff == kHashPair)
+    k_dec_front_p<<<pair_blocks(warp_round(2 * n) + 2 * n), kPairHashBlock, 0, s>>>(P, sk, ct, a_stream, hc,
+                                                                                    (int)n, 0);
+  else
+    k_dec_front<<<nblocks(warp_round(n) + n), 128, 0, s>>>(P, sk, ct, a_stream, hc, (int)n, 0);
   CpaArgs a{};
   a.P = P;
   a.n = (int)n;
@@ -189,7 +198,12 @@ extern "C" int tmvp_kem_dec_batch_noalloc(tmvp_param_set set, size_t n, uint8_t 
   a.copy_hpk = 1;
   a.err = err;
   if (cpa_launch(f, kDecrypt, a, s) != 0) return TMVP_EDEVICE;
-  k_dec_g<<<nblocks(n), 128, 0, s>>>(P, mbuf, kr, s_stream, (int)n);
+  if (fs == kHashWarp)
+    k_dec_g_w<<<warp_blocks(n), kWarpHashBlock, 0, s>>>(P, mbuf, kr, s_stream, (int)n);
+  else if (fs == kHashPair)
+    k_dec_g_p<<<pair_blocks(2 * n), kPairHashBlock, 0, s>>>(P, mbuf, kr, s_stream, (int)n);
+  else
+    k_dec_g<<<nblocks(n), 128, 0, s>>>(P, mbuf, kr, s_stream, (int)n);
   CpaArgs b{};
   b.P = P;
   b.n = (int)n;
@@ -204,7 +218,13 @@ extern "C" int tmvp_kem_dec_batch_noalloc(tmvp_param_set set, size_t n, uint8_t 
   b.fail = fail;
   b.err = err;
   if (cpa_launch(f, kReenc, b, s) != 0) return TMVP_EDEVICE;
-  k_final_key<<<nblocks(n), 128, 0, s>>>(P, ct, hc, kr, fail, sk, (size_t)P.sk_bytes, ss, (int)n);
+  if (fs == kHashWarp)
+    k_final_key_w<<<warp_blocks(n), kWarpHashBlock, 0, s>>>(P, ct, hc, kr, fail, sk, (size_t)P.sk_bytes, ss, (int)n);
+  else if (fs == kHashPair)
+    k_final_key_p<<<pair_blocks(2 * n), kPairHashBlock, 0, s>>>(P, ct, hc, kr, fail, sk, (size_t)P.sk_bytes, ss,
+                                                                (int)n);
+  else
+    k_final_key<<<nblocks(n), 128, 0, s>>>(P, ct, hc, kr, fail, sk, (size_t)P.sk_bytes, ss, (int)n);
   k_noalloc_status<<<1, 1, 0, s>>>(err, status_d);
   return cudaGetLastError() == cudaSuccess ? TMVP_OK : TMVP_EDEVICE;
 }

@@ -74,8 +74,8 @@ struct tmvp_ctx {
   size_t dev_chunk = 32768;                        // chunk of device-input decapsulation (0: none)
   bool serial = false;                             // every stage on the caller's stream, one at a time
   int front_cap = 0;                               // Keccak-front blocks per SM (0: one thread per sponge)
-  size_t warp_hash = 1024;                         // Keccak launches of <= this many sponges: a warp per sponge
-  size_t pair_hash = 16384;                        // else of <= this many: two threads per sponge
+  size_t warp_hash = kWarpHashDefault;             // Keccak launches of <= this many sponges: a warp per sponge
+  size_t pair_hash = kPairHashDefault;             // else of <= this many: two threads per sponge
   // set by the caller (tmvp_ctx_set_*): then the autotuner's per-batch choice does not apply
   bool host_chunk_set = false, host_ramp_set = false, dev_chunk_set = false, front_cap_set = false;
   int nsm = 0;                                     // SMs of the device
@@ -321,21 +321,9 @@ inline unsigned blocks_for(size_t threads, unsigned bs) { return (unsigned)((thr
 // Threads per block of the Keccak kernels (one sponge per thread): small
 // blocks spread a batch evenly over the 152 SMs of an ALU-bound stage.
 constexpr unsigned kHashBlock = 64;
-// The form of a Keccak launch.  One thread per sponge (hash_kernels.cu)
-// keeps a warp's share of the integer pipe busy: ~4.7 us per permutation
-// however idle the GPU is, and the best rate once the pipe is full.  One warp
-// per sponge (hash_warp.cu): ~2.1 us per permutation until its shuffles fill
-// the SMs (~1 K GenMatrix sponges).  Two threads per sponge (hash_pair.cu):
-// ~3.3 us per permutation up to ~10 K sponges, the thread form's integer work
-// per sponge with twice its warps.  Launches of short sponges (G, the final
-// key, the key-generation tail: 1-8 permutations) count four times against
-// the warp form's limit: beside the other stages of a pass they lose there
-// sooner.
-enum HashForm { kHashThread, kHashWarp, kHashPair };
+// The form of a Keccak launch under the context's limits (hash_form_for).
 inline HashForm hash_form(const tmvp_ctx *c, size_t sponges, bool short_sponges = false) {
-  if ((short_sponges ? 4 * sponges : sponges) <= c->warp_hash) return kHashWarp;
-  if (sponges <= c->pair_hash) return kHashPair;
-  return kHashThread;
+  return hash_form_for(sponges, short_sponges, c->warp_hash, c->pair_hash);
 }
 
 int check_common(tmvp_ctx *c, int set, size_t n, int form, KemParams *P) {
