@@ -30,14 +30,17 @@ struct ShakeJob {
 // kernels): ~3.3 us per permutation up to ~10 K sponges, the thread form's
 // integer work per sponge with twice its warps.  Launches of short sponges
 // (G, the final key, the key-generation tail: 1-8 permutations) count four
-// times against the warp form's limit: beside the other stages of a pass
-// they lose there sooner.  kWarpHashDefault / kPairHashDefault are the
-// limits a context starts with (tmvp_ctx_set_warp_hash / _pair_hash).
-constexpr size_t kWarpHashDefault = 1024, kPairHashDefault = 16384;
+// times against the warp form's limit and twice against the pair form's:
+// beside the other stages of a pass they lose there sooner (at batch 32768,
+// G and the final key in the pair form: 0.662 against 0.650 ms per pass,
+// while a GenMatrix + H(c) front of 32768 sponges gains: 0.352 against 0.369
+// ms at batch 16384).  kWarpHashDefault / kPairHashDefault are the limits a
+// context starts with (tmvp_ctx_set_warp_hash / _pair_hash).
+constexpr size_t kWarpHashDefault = 1024, kPairHashDefault = 32768;
 enum HashForm { kHashThread, kHashWarp, kHashPair };
 inline HashForm hash_form_for(size_t sponges, bool short_sponges, size_t warp_max, size_t pair_max) {
   if ((short_sponges ? 4 * sponges : sponges) <= warp_max) return kHashWarp;
-  if (sponges <= pair_max) return kHashPair;
+  if ((short_sponges ? 2 * sponges : sponges) <= pair_max) return kHashPair;
   return kHashThread;
 }
 

@@ -228,13 +228,13 @@ int tmvp_ctx_set_front_cap(tmvp_ctx *ctx, int blocks_per_sm);
 /* The form of each Keccak launch (GenMatrix, GenSecret, H, G, the final
  * key).  Launches of at most warp_hash sponges run one warp per sponge, the
  * state spread over the warp's lanes (~2.1 us per permutation while the GPU
- * is far from full; launches of short sponges, G, the final key and the
- * key-generation tail, count four times); larger ones of at most pair_hash
- * sponges run two threads per sponge, each holding half of every state lane
- * (~3.3 us per permutation up to ~10 K sponges); larger ones one thread per
- * sponge (~4.7 us per permutation, the best rate once the GPU is full).
- * Defaults 1024 and 16384; 0 turns a form off.  Results do not depend on
- * them.  No counterpart in the reference, whose hash kernels run as one
+ * is far from full); larger ones of at most pair_hash sponges run two threads
+ * per sponge, each holding half of every state lane (~3.3 us per permutation
+ * up to ~10 K sponges); larger ones one thread per sponge (~4.7 us per
+ * permutation, the best rate once the GPU is full).  Launches of short
+ * sponges (G, the final key, the key-generation tail) count four times
+ * against warp_hash and twice against pair_hash.  Defaults 1024 and 32768;
+ * 0 turns a form off.  Results do not depend on them.  No counterpart in the reference, whose hash kernels run as one
  * block of one thread per instance
  * (TMVP-Saber/SABER-GPU/src/cuda_kernel.cu:116-127). */
 int tmvp_ctx_set_warp_hash(tmvp_ctx *ctx, size_t max_sponges);

@@ -115,9 +115,10 @@ def test_indcpa_cached_and_onekey_paths_every_form(kem, set_id):
 
 
 def test_default_threshold_boundaries(kem):
-    """Around the default limits (warp form: 1024 sponges, the decapsulation
-    front has 2n, G and the final key count four times; pair form: 16384
-    sponges) the default context and each single form agree."""
+    """Around the default limits (warp form: 1024 sponges, pair form: 32768;
+    the decapsulation front has 2n sponges, G and the final key count four
+    times against the first and twice against the second) the default
+    context and each single form agree."""
     import torch
     T, ctx = kem
     dev = torch.device("cuda", 0)
