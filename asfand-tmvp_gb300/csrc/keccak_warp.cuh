@@ -3,12 +3,12 @@
 // halves, and the round exchanges lanes by warp shuffles.
 //
 // This is the latency form.  One thread per sponge (keccak.cuh) issues ~180
-// dependent-enough integer instructions per round through its warp's share of
-// the integer pipe, ~4.7 us per permutation however few sponges run; here a
-// round is 18 shuffles and 16 integer instructions spread over 25 lanes, so a
-// permutation takes a fraction of that while the GPU is far from full.  It
-// costs ~5x the instructions per permutation, so batches large enough to fill
-// the integer pipe use the thread-per-sponge kernels.
+// integer instructions per round through its warp's share of the integer
+// pipe, ~4.7 us per permutation however few sponges run; here a round is 18
+// shuffles and ~16 integer instructions per lane, ~2.1 us per permutation
+// while the GPU is far from full.  It issues ~5x the instructions per
+// permutation, so larger launches take two threads per sponge
+// (keccak_pair.cuh) or one.
 //
 // The round is the same theta / rho / pi / chi / iota as keccak_round (FIPS
 // 202 Algorithms 1-6; the reference's KeccakF1600_StatePermute,
