@@ -326,6 +326,19 @@ inline HashForm hash_form(const tmvp_ctx *c, size_t sponges, bool short_sponges 
   return hash_form_for(sponges, short_sponges, c->warp_hash, c->pair_hash);
 }
 
+// GenMatrix streams of n keys (seed_A at the end of pk + i * pk_stride) in
+// the form the launch size gives.
+void launch_genmatrix(const tmvp_ctx *c, const KemParams &P, const uint8_t *pk, size_t pk_stride,
+                      uint8_t *a_stream, size_t n, cudaStream_t s) {
+  const HashForm f = hash_form(c, n);
+  if (f == kHashWarp)
+    k_genmatrix_w<<<warp_blocks(n), kWarpHashBlock, 0, s>>>(P, pk, pk_stride, a_stream, (int)n);
+  else if (f == kHashPair)
+    k_genmatrix_p<<<pair_blocks(2 * n), kPairHashBlock, 0, s>>>(P, pk, pk_stride, a_stream, (int)n);
+  else
+    k_genmatrix<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, pk, pk_stride, a_stream, (int)n);
+}
+
 int check_common(tmvp_ctx *c, int set, size_t n, int form, KemParams *P) {
   if (!c) return TMVP_EINVAL;
   if (!make_params(set, P)) return TMVP_EINVAL;
@@ -969,13 +982,7 @@ int tmvp_genmatrix_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *a_s
   if (classify(a_stream, n * P.gm_bytes, c->device).host || classify(pk, n * pk_stride, c->device).host)
     return set_err(TMVP_EINVAL);  // device buffers only
   cudaStream_t s = (cudaStream_t)stream;
-  const HashForm f = hash_form(c, n);
-  if (f == kHashWarp)
-    k_genmatrix_w<<<warp_blocks(n), kWarpHashBlock, 0, s>>>(P, pk, pk_stride, a_stream, (int)n);
-  else if (f == kHashPair)
-    k_genmatrix_p<<<pair_blocks(2 * n), kPairHashBlock, 0, s>>>(P, pk, pk_stride, a_stream, (int)n);
-  else
-    k_genmatrix<<<blocks_for(n, kHashBlock), kHashBlock, 0, s>>>(P, pk, pk_stride, a_stream, (int)n);
+  launch_genmatrix(c, P, pk, pk_stride, a_stream, n, s);
   c->launches++;
   return set_err(finish(c, s, false));
 }
@@ -1235,18 +1242,41 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
     }
     return set_err(finish(c, s, bss.host));
   }
-  size_t need = dec_ws_bytes(P, n) + stage_bytes(bss) + stage_bytes(bct) + stage_bytes(bsk);
+  // Host inputs in one chain: with sk in pinned host memory mapped into the
+  // device's address space, GenMatrix (which needs only each key's 32-byte
+  // seed) starts at once from the seeds in place on a high-priority side
+  // stream while ct and sk are copied, and the chain runs with that A (its
+  // front is H(c) alone).
+  const bool one_chain = c->serial || !(c->dev_chunk && n > c->dev_chunk);
+  const uint8_t *sk_map = bsk.host && one_chain && !c->serial ? mapped_host_ptr(bsk.user) : nullptr;
+  const size_t seed_off = P.indcpa_sk_bytes + (size_t)P.l * P.polycompbytes;
+  if (sk_map && (((uintptr_t)sk_map | seed_off | P.sk_bytes) & 7) != 0) sk_map = nullptr;
+  size_t need = dec_ws_bytes(P, n) + stage_bytes(bss) + stage_bytes(bct) + stage_bytes(bsk) +
+                (sk_map ? up(n * P.gm_bytes) : 0);
   if ((r = ensure_ws(c, need))) return set_err(r);
   Arena A{c->ws};
   DecScratch w = dec_scratch(P, n, A);
   stage_assign(bss, A);
   stage_assign(bct, A);
   stage_assign(bsk, A);
+  uint8_t *a_early = sk_map ? A.take(n * P.gm_bytes) : nullptr;
+  if (a_early) {
+    cudaStream_t gs = c->lane_side[0];
+    TRY_CUDA(cudaEventRecord(c->fork_ev, s));
+    TRY_CUDA(cudaStreamWaitEvent(gs, c->fork_ev, 0));
+    {
+      StageTimer tm_(c, "genmatrix", gs);
+      launch_genmatrix(c, P, sk_map + P.indcpa_sk_bytes, P.sk_bytes, a_early, n, gs);
+    }
+    c->launches++;
+    TRY_CUDA(cudaEventRecord(c->gm_ev, gs));
+  }
   if ((r = upload(bct, s)) || (r = upload(bsk, s))) return set_err(r);
-  if (c->dev_chunk && n > c->dev_chunk && !c->serial)
+  if (!one_chain)
     r = dec_lanes(c, P, n, c->dev_chunk, bss.dev, bct.dev, bsk.dev, form, s, w);
   else
-    r = dec_pipeline(c, P, n, bss.dev, bct.dev, bsk.dev, form, s, w);
+    r = dec_pipeline(c, P, n, bss.dev, bct.dev, bsk.dev, form, s, w, true, nullptr, a_early,
+                     a_early ? c->gm_ev : nullptr);
   if (r) return set_err(r);
   if ((r = download(bss, s))) return set_err(r);
   return set_err(finish(c, s, bss.host));

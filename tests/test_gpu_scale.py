@@ -279,3 +279,41 @@ def test_chunked_host_onekey_decapsulation(kem, chunk, ramp, pinned):
     assert torch.equal(out, ref.cpu())
     ss_h = ss.cpu()
     assert torch.equal(out[:n - 2], ss_h[:n - 2]) and not torch.equal(out[n - 2], ss_h[n - 2])
+
+
+@pytest.mark.parametrize("set_id", [1, 2, 4])
+def test_one_chain_host_decapsulation_genmatrix_from_mapped_seeds(kem, set_id):
+    """Host inputs in one chain (up to the host chunk): with pinned sk the
+    GenMatrix launch reads each key's seed in place while ct and sk are
+    copied (in its warp, pair or thread form by size); with pageable sk the
+    chain expands it after the copy.  Both give the device path's keys,
+    tampered ciphertexts rejected."""
+    import torch
+    T, ctx = kem
+    dev = torch.device("cuda", 0)
+    z = T.sizes(set_id)
+    N = 5000
+    coins = torch.from_numpy(T.splitmix_bytes(61 + set_id, N * 96).reshape(N, 96)).to(dev)
+    ec = torch.from_numpy(T.splitmix_bytes(71 + set_id, N * 32).reshape(N, 32)).to(dev)
+    pk = torch.empty((N, z.pk_bytes), dtype=torch.uint8, device=dev)
+    sk = torch.empty((N, z.sk_bytes), dtype=torch.uint8, device=dev)
+    ct = torch.empty((N, z.ct_bytes), dtype=torch.uint8, device=dev)
+    ss = torch.empty((N, 32), dtype=torch.uint8, device=dev)
+    ctx.kem_keypair_ptr(set_id, N, pk, sk, coins)
+    ctx.kem_enc_ptr(set_id, N, ct, ss, pk, ec)
+    ct[5::9, 11] ^= 0x40
+    torch.cuda.synchronize()
+    want = torch.empty_like(ss)
+    ctx.kem_dec_ptr(set_id, N, want, ct, sk)
+    torch.cuda.synchronize()
+    want_h = want.cpu()
+    assert not (want[5::9] == ss[5::9]).all(dim=1).any()
+    for pinned in (True, False):
+        ct_h, sk_h, out = ct.cpu(), sk.cpu(), torch.zeros((N, 32), dtype=torch.uint8)
+        if pinned:
+            ct_h, sk_h, out = ct_h.pin_memory(), sk_h.pin_memory(), out.pin_memory()
+        for n in (1, 300, 2048, 5000):
+            out.zero_()
+            ctx.kem_dec_ptr(set_id, n, out, ct_h, sk_h)
+            torch.cuda.synchronize()
+            assert torch.equal(out[:n], want_h[:n]), f"pinned={pinned} n={n}"
