@@ -460,6 +460,9 @@ def run_ours(args):
             busy = stages_busy.get(k)
             if busy:
                 v["busy_ms_per_step_in_pass"] = busy / args.steps
+                if "mma_instruction_floor_ms" in v:
+                    floor_step = v["mma_instruction_floor_ms"] * n / v["instances_per_launch"]
+                    v["frac_of_mma_floor_in_pass"] = floor_step / (busy / args.steps)
                 if "keccak" in v:
                     key = next(x for x in _STAGE_WORK if k.startswith(x))
                     rate = n * args.steps * _STAGE_WORK[key][2] / (busy / 1e3)
