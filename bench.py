@@ -954,7 +954,7 @@ def main():
     ap.add_argument("--serving-rates", default="100000,200000,400000,800000,1600000,3200000,6400000",
                     help="offered loads of the serving sweep, requests/s (comma list)")
     ap.add_argument("--serving-seconds", type=float, default=0.5)
-    ap.add_argument("--latency-batches", default="1,16,256,4096,65536",
+    ap.add_argument("--latency-batches", default="1,16,256,1024,4096,16384,65536",
                     help="batches of the per-call latency curve (comma list)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (e2e) leg")

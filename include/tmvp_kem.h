@@ -197,8 +197,9 @@ int tmvp_ctx_reserve(tmvp_ctx *ctx, size_t bytes);
 /* Batched decapsulation with host-resident ct / sk copies and processes them
  * in chunks of n instances (one copy stream running ahead of the kernels), so
  * that copies overlap the kernels of earlier chunks; 0 = one copy, then the
- * kernels.  Default 16384; n must be 0 or >= 1024.  Results do not depend
- * on it. */
+ * kernels.  Unless set here (or chosen by tmvp_autotune for the batch size),
+ * a call of b instances uses about b / 4, from 4096 to 16384.  n must be 0
+ * or >= 1024.  Results do not depend on it. */
 int tmvp_ctx_set_host_chunk(tmvp_ctx *ctx, size_t n);
 /* The first `steps` chunks of such a call are n >> steps, n >> (steps - 1),
  * ..., n >> 1 instances (at least 256), so that the kernels start after a
