@@ -29,7 +29,7 @@ struct ShakeJob {
 // fill the SMs (~1 K GenMatrix sponges).  Two threads per sponge (the _p
 // kernels): ~3.3 us per permutation up to ~10 K sponges, the thread form's
 // integer work per sponge with twice its warps.  Launches of short sponges
-// (G, the final key, the key-generation tail: 1-8 permutations) count four
+// (G, the final key, the key-generation tail: 1-10 permutations) count four
 // times against the warp form's limit and twice against the pair form's:
 // beside the other stages of a pass they lose there sooner (at batch 32768,
 // G and the final key in the pair form: 0.662 against 0.650 ms per pass,

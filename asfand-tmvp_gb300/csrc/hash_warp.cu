@@ -36,7 +36,7 @@ __device__ __forceinline__ void lane_store(uint8_t *p, int lane, int nw, uint64_
   if (lane < nw) reinterpret_cast<uint64_t *>(p)[lane] = v;
 }
 
-// word k of lanes [from, from + count) moved to lane k
+// lane k takes the word of lane (k + from) mod 32
 __device__ __forceinline__ uint64_t lanes_down(uint64_t v, int lane, int from) {
   const uint32_t lo = __shfl_sync(0xFFFFFFFFu, (uint32_t)v, (lane + from) & 31);
   const uint32_t hi = __shfl_sync(0xFFFFFFFFu, (uint32_t)(v >> 32), (lane + from) & 31);
