@@ -1266,8 +1266,12 @@ int tmvp_kem_dec_batch(tmvp_ctx *c, tmvp_param_set set, size_t n, uint8_t *ss, c
   const uint8_t *sk_map = bsk.host && one_chain && !c->serial ? mapped_host_ptr(bsk.user) : nullptr;
   const size_t seed_off = P.indcpa_sk_bytes + (size_t)P.l * P.polycompbytes;
   if (sk_map && (((uintptr_t)sk_map | seed_off | P.sk_bytes) & 7) != 0) sk_map = nullptr;
-  size_t need = dec_ws_bytes(P, n) + stage_bytes(bss) + stage_bytes(bct) + stage_bytes(bsk) +
-                (sk_map ? up(n * P.gm_bytes) : 0);
+  size_t need = dec_ws_bytes(P, n) + stage_bytes(bss) + stage_bytes(bct) + stage_bytes(bsk);
+  // (a workspace that cannot hold the early A as well keeps the chain's own GenMatrix)
+  if (sk_map && ensure_ws(c, need + up(n * P.gm_bytes)) == TMVP_OK)
+    need += up(n * P.gm_bytes);
+  else
+    sk_map = nullptr;
   if ((r = ensure_ws(c, need))) return set_err(r);
   Arena A{c->ws};
   DecScratch w = dec_scratch(P, n, A);

@@ -317,3 +317,34 @@ def test_one_chain_host_decapsulation_genmatrix_from_mapped_seeds(kem, set_id):
             ctx.kem_dec_ptr(set_id, n, out, ct_h, sk_h)
             torch.cuda.synchronize()
             assert torch.equal(out[:n], want_h[:n]), f"pinned={pinned} n={n}"
+
+
+def test_one_chain_host_decapsulation_within_a_tight_budget(kem):
+    """With a workspace budget too small for the early GenMatrix streams (and
+    large enough for the chain without them) a pinned-host decapsulation
+    still runs, expanding GenMatrix after the copies."""
+    import torch
+    T, ctx = kem
+    dev = torch.device("cuda", 0)
+    S = T.SABER
+    z = T.sizes(S)
+    n = 4096  # ~33 MB of workspace without the early A, ~48 MB with it
+    coins = torch.from_numpy(T.splitmix_bytes(81, n * 96).reshape(n, 96)).to(dev)
+    ec = torch.from_numpy(T.splitmix_bytes(82, n * 32).reshape(n, 32)).to(dev)
+    pk = torch.empty((n, z.pk_bytes), dtype=torch.uint8, device=dev)
+    sk = torch.empty((n, z.sk_bytes), dtype=torch.uint8, device=dev)
+    ct = torch.empty((n, z.ct_bytes), dtype=torch.uint8, device=dev)
+    ss = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+    ctx.kem_keypair_ptr(S, n, pk, sk, coins)
+    ctx.kem_enc_ptr(S, n, ct, ss, pk, ec)
+    torch.cuda.synchronize()
+    ct_h, sk_h = ct.cpu().pin_memory(), sk.cpu().pin_memory()
+    out = torch.zeros((n, 32), dtype=torch.uint8).pin_memory()
+    c = T.Context(0, mem_budget=40 << 20)
+    try:
+        c.kem_dec_ptr(S, n, out, ct_h, sk_h)
+        torch.cuda.synchronize()
+        assert c.workspace_bytes <= 40 << 20
+    finally:
+        c.close()
+    assert torch.equal(out, ss.cpu())
